@@ -1,0 +1,407 @@
+#!/usr/bin/env python3
+"""Benchmark of the BFS/SSSP hot path on one GB300 (replicas across GPUs).
+
+Workload (the single-GPU configuration the metric is quoted on): R-MAT scale
+22, edge factor 16 (a/b/c/d = .57/.19/.19/.05, seed 2), symmetrised, self
+loops and duplicates removed, vertex ids permuted, int32 CSR, uint32 weights
+U[1,255]; 64 random sources (degree > 0) run one after another, each a
+single-source BFS and a single-source SSSP.  One step = all 128 traversals.
+The graph (1 GB of CSR) is larger than the 129 MB L2, so no flush is needed
+between steps.
+
+value    GTEPS = sum of E_r over the step's traversals / device time of the
+         step (CUDA events on the library's stream around K steps); E_r is
+         the out-degree sum of reached vertices, directed edges counted once.
+e2e      the same metric through the C ABI with HOST buffers: every step
+         re-uploads the pinned CSR and copies each distance vector back.
+roofline the dominant persistent kernel: algorithmic bytes per launch
+         (BFS 8*E_r + 20*V_r, SSSP 12*E_r + 20*V_r) / its mean launch time
+         against the measured HBM copy bandwidth.
+cpu_baseline  the oracle (C restatement of the reference's serial
+         findSerialBFS/SSSP, graph.h:115-184) on the host cores, one source
+         per thread, on a bounded sample of the same workload.
+
+--impl reference times that CPU path alone (the reference's implementation of
+the path; it has no other runnable form on this machine) on the same metric.
+Multi-GPU: launched with torchrun, every rank runs an independent replica of
+the workload on its own GPU with its own sources ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SSSP/BFS GTEPS at RMAT-22; batched queries/s + p99 vs one-at-a-time, 1 GB300"
+UNIT = "GTEPS"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gga", choices=["gga", "reference"])
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--sources", type=int, default=64)
+    ap.add_argument("--variant", default="frontier")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--autotune-trials", type=int, default=1)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------ distributed
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# ------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()) if rows else None}
+
+
+# ------------------------------------------------------------ workload
+
+def make_workload(args, rank: int):
+    import gpugraphalgo_gb300 as gga
+
+    g = gga.Graph.rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, seed=2, wmin=1, wmax=255)
+    deg = g.degrees()
+    rng = np.random.default_rng(2 + 1000 * rank)
+    cand = np.nonzero(deg > 0)[0]
+    srcs = [int(x) for x in rng.choice(cand, size=args.sources, replace=False)]
+    return g, srcs
+
+
+def algorithmic_bytes(algo: str, er: int, vr: int) -> int:
+    return (8 if algo == "bfs" else 12) * er + 20 * vr
+
+
+def read_traffic(kind: str):
+    """dram bytes per launch from the committed ncu summary, scaled per edge."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        f = line.split()
+        if len(f) >= 3 and f[0] == "bytes_per_edge_reached" and f[1] == kind:
+            return float(f[2])
+    return None
+
+
+def cpu_baseline(g, srcs, threads: int, budget_sources: int):
+    """Oracle serial BFS/SSSP (the reference's algorithm) on host threads."""
+    import oracle
+
+    off, col, wt = g.csr()
+    og = oracle.OracleGraph.from_csr(off, col, wt)
+    lib = oracle.load()
+    deg = np.diff(off.astype(np.int64))
+    sample = srcs[:budget_sources]
+    results = {}
+
+    def work(i, s):
+        for algo in ("bfs", "sssp"):
+            d = np.empty(len(off) - 1, np.uint32)
+            lib.oracle_serial(og._h, 1 if algo == "sssp" else 0, s, oracle._p(d))
+            reach = d < oracle.INF
+            results[(i, algo)] = int(deg[reach].sum())
+
+    t0 = time.perf_counter()
+    ths = []
+    for i, s in enumerate(sample):
+        th = threading.Thread(target=work, args=(i, s))
+        th.start()
+        ths.append(th)
+        if len(ths) >= threads:
+            ths.pop(0).join()
+    for th in ths:
+        th.join()
+    dt = time.perf_counter() - t0
+    er = sum(results.values())
+    return er / dt / 1e9, dt, len(sample)
+
+
+def run_reference(args, dist: Dist):
+    """--impl reference: the reference's CPU path (oracle port) on host cores."""
+    if dist.rank != 0:
+        return None
+    g, srcs = make_workload(args, 0)
+    threads = os.cpu_count() or 1
+    per_step = max(2, min(threads, (threads * 6) // max(1, args.steps + args.warmup)))
+    for w in range(args.warmup):
+        cpu_baseline(g, srcs[w * per_step % len(srcs):][:per_step] or srcs[:per_step], threads, per_step)
+    vals, secs = [], 0.0
+    for k in range(args.steps):
+        start = (k * per_step) % len(srcs)
+        v, dt, _ = cpu_baseline(g, (srcs[start:] + srcs[:start])[:per_step], threads, per_step)
+        vals.append(v)
+        secs += dt
+    value = statistics.mean(vals)
+    sample = f"{per_step} sources x (BFS+SSSP) per step, one source per thread, R-MAT-{args.scale}"
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"rmat{args.scale}_ef{args.edge_factor}_seed2_bfs_sssp", "sources": args.sources,
+                   "implementation": "serial in-order Bellman-Ford sweeps (graph.h:115-184), oracle C port",
+                   "parallelism": f"{threads} host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_gga(args, dist: Dist):
+    import gpugraphalgo_gb300 as gga
+
+    ctx = gga.Context(dist.local_rank)
+    dev = ctx.device_info()
+    g, srcs = make_workload(args, dist.rank)
+    info = g.info()
+    g.cudaCopy(ctx)
+    params = ctx.autotune(g, args.autotune_trials)
+    ctx.set_params(skip_reached=1)
+    variant = args.variant
+
+    # E_r / V_r per traversal (fixed by graph and source), outside the timing
+    ctx.set_params(skip_reached=0)
+    reach = {}
+    for s in srcs:
+        for algo in ("bfs", "sssp"):
+            _, st = ctx.solve(g, algo, s, variant, stats=True, keep_on_device=True)
+            reach[(algo, s)] = (st["edges_reached"], st["vertices_reached"])
+    ctx.set_params(skip_reached=1)
+
+    def step(record=None):
+        launches = 0
+        for s in srcs:
+            for algo in ("bfs", "sssp"):
+                _, st = ctx.solve(g, algo, s, variant, stats=True, keep_on_device=True)
+                launches += st["kernel_launches"]
+                if record is not None:
+                    record[algo].append(st["kernel_ms"])
+        return launches
+
+    for _ in range(args.warmup):
+        step()
+    dist.barrier()
+    ctx.synchronize()
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    rec = {"bfs": [], "sssp": []}
+    launches = 0
+    ctx.mark(0)
+    for _ in range(args.steps):
+        launches += step(rec)
+    ctx.mark(1)
+    ctx.synchronize()
+    ms = ctx.elapsed(0, 1)
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+
+    er_step = sum(e for e, _ in reach.values())
+    er_total = dist.sum(er_step * args.steps)
+    value = er_total / (ms_max * 1e-3) / 1e9
+
+    bfs_er = sum(reach[("bfs", s)][0] for s in srcs)
+    sssp_er = sum(reach[("sssp", s)][0] for s in srcs)
+    bfs_ms = sum(rec["bfs"]) / args.steps
+    sssp_ms = sum(rec["sssp"]) / args.steps
+    kinds = {}
+    for algo, tot_ms in (("bfs", bfs_ms), ("sssp", sssp_ms)):
+        byts = sum(algorithmic_bytes(algo, *reach[(algo, s)]) for s in srcs) / len(srcs)
+        per_launch_ms = tot_ms / len(srcs)
+        kinds[algo] = {"bytes_per_launch": byts, "ms_per_launch": per_launch_ms,
+                       "achieved_gbs": byts / (per_launch_ms * 1e-3) / 1e9}
+    dom = "sssp" if sssp_ms >= bfs_ms else "bfs"
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    tpe = read_traffic(dom)
+    er_mean = (sssp_er if dom == "sssp" else bfs_er) / len(srcs)
+    roofline = {"bound": "hbm", "kernel": f"k_frontier<{params['block_threads']},{'true' if dom == 'sssp' else 'false'}>",
+                "achieved": kinds[dom]["achieved_gbs"], "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+                "frac": kinds[dom]["achieved_gbs"] / peak,
+                "traffic": tpe * er_mean if tpe else None,
+                "algorithmic_bytes": kinds[dom]["bytes_per_launch"],
+                "per_kind": kinds}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"rmat{args.scale}_ef{args.edge_factor}_seed2_{args.sources}src_bfs+sssp",
+                   "graph": f"R-MAT scale {args.scale} ef {args.edge_factor} a/b/c=.57/.19/.19 seed 2, symmetrised, "
+                            "dedup, ids permuted, weights U[1,255]",
+                   "vertices": info["nodes_orig"], "edges": info["nedges"], "maxdeg": info["maxdeg"],
+                   "sources": args.sources, "parallelism": "replicas" if dist.world > 1 else "single",
+                   "l2": "inputs larger than L2 (CSR %.2f GB vs 129 MB L2); no flush" % ((4 * (info["nodes_orig"] + 1) + 8 * info["nedges"]) / 1e9),
+                   "variant": variant, "params": params, "device": dev["name"], "sms": dev["sms"]},
+        "bfs_gteps": bfs_er / (bfs_ms * 1e-3) / 1e9,
+        "sssp_gteps": sssp_er / (sssp_ms * 1e-3) / 1e9,
+        "roofline": roofline,
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+
+    # reference algorithm (topology-driven Bellman-Ford, "na_") on the same GPU
+    try:
+        ta = {}
+        for algo in ("bfs", "sssp"):
+            _, st = ctx.solve(g, algo, srcs[0], "topo_atomic", stats=True, keep_on_device=True)
+            ta[algo] = {"ms": st["kernel_ms"], "iterations": st["iterations"],
+                        "gteps": reach[(algo, srcs[0])][0] / (st["kernel_ms"] * 1e-3) / 1e9}
+        out["reference_algorithm_same_gpu"] = ta
+    except Exception as e:  # reported, not fatal
+        out["reference_algorithm_same_gpu"] = {"error": str(e)}
+
+    # end to end through the C ABI with host buffers
+    if not args.no_e2e:
+        g.pin(True)
+        hbuf = np.empty(info["nodes_orig"], np.uint32)
+        try:
+            import torch
+
+            hbuf = torch.empty(info["nodes_orig"], dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+        except Exception:
+            pass
+        dist.barrier()
+        e2e_steps = max(1, min(args.steps, 2))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            g.release_device()
+            for s in srcs:
+                for algo in ("bfs", "sssp"):
+                    ctx.solve(g, algo, s, variant, out=hbuf)
+        ctx.synchronize()
+        dt = time.perf_counter() - t0
+        dt_max = dist.max(dt)
+        out["e2e"] = {"value": dist.sum(er_step * e2e_steps) / dt_max / 1e9, "unit": UNIT,
+                      "h2d_bytes_per_step": 4 * (info["nodes_orig"] + 1) + 8 * info["nedges"],
+                      "d2h_bytes_per_step": 4 * info["nodes_orig"] * 2 * len(srcs),
+                      "steps": e2e_steps}
+        g.cudaCopy(ctx)
+
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, dt, ns = cpu_baseline(g, srcs, threads, min(threads, len(srcs)))
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": min(threads, ns), "kind": "port",
+                               "sample": f"{ns} sources x (BFS+SSSP), one source per thread, {dt:.1f} s wall"}
+    ctx.close()
+    return out
+
+
+def main():
+    args = parse_args()
+    dist = Dist()
+    try:
+        res = run_reference(args, dist) if args.impl == "reference" else run_gga(args, dist)
+        if dist.rank == 0 and res is not None:
+            print(json.dumps(res))
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,420 @@
+"""GB300-native static-graph BFS/SSSP (GPUGraphAlgo's traversal hot path).
+
+Python side of the C ABI in ``include/gga.h``: thin ctypes wrappers used by the
+tests and the benchmark.  All computation happens in ``libgga.so`` (host C and
+sm_103a CUDA kernels).  Method names follow the reference's ``struct Graph``
+(Programs/CUDA_src/Kepler_BFS_SSSP/graph.h:23-64) where one exists:
+``readFromGR``, ``getMaxdeg``, ``getMaxAllowedOutDegree``,
+``getSizeafterLoadBalance``, ``NodeSplit``, ``cudaCopy``; ``verifysolution``,
+``Ary2File`` and ``writeResult`` mirror myutils.h.  Errors raise
+:class:`GGAError` carrying the C status code instead of exiting the process
+(the reference calls ``exit(-1)`` in ``CudaTest``, graph.h:523-533).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+
+INFINITY = 1000000000  # MYINFINITY, bfs_sssp.cu:53
+MAX_WEIGHT = 0xFFFFFFFF - INFINITY
+
+BFS, SSSP = 0, 1
+ALGOS = {"bfs": BFS, "sssp": SSSP}
+
+VARIANTS = {
+    "auto": 0,
+    "frontier": 1,
+    "topo_atomic": 2,  # "na_" build
+    "topo_plain": 3,  # "n_" build
+    "cdp_atomic": 4,  # "da_" build
+    "cdp_plain": 5,  # "d_" build
+}
+
+OK, ERR_INVALID_ARG, ERR_IO, ERR_FORMAT, ERR_SPLIT_RULE = 0, 1, 2, 3, 4
+ERR_NO_MEMORY, ERR_CUDA, ERR_NO_DEVICE, ERR_TIMEOUT, ERR_ADMISSION = 5, 6, 7, 8, 9
+ERR_TOO_LARGE, ERR_NOT_READY, ERR_UNSUPPORTED = 10, 11, 12
+
+
+class GGAError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        lib = N.load()
+        self.status = status
+        msg = lib.gga_last_error().decode(errors="replace")
+        super().__init__(f"{where}: {lib.gga_status_string(status).decode()} ({status}): {msg}")
+
+
+def _check(status: int, where: str):
+    if status != OK:
+        raise GGAError(status, where)
+
+
+def lib():
+    return N.load()
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+def _algo(a) -> int:
+    return ALGOS[a] if isinstance(a, str) else int(a)
+
+
+def _variant(v) -> int:
+    return VARIANTS[v] if isinstance(v, str) else int(v)
+
+
+class Graph:
+    """A host CSR graph (struct Graph); device residency is cached per graph."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+
+    # ---- construction
+    @classmethod
+    def readFromGR(cls, path: str) -> "Graph":
+        h = C.c_void_p()
+        _check(N.load().gga_graph_load_gr(path.encode(), C.byref(h)), f"readFromGR({path})")
+        return cls(h.value)
+
+    load_gr = readFromGR
+
+    @classmethod
+    def from_csr(cls, offsets, cols, weights=None) -> "Graph":
+        off = np.ascontiguousarray(offsets, dtype=np.uint32)
+        col = np.ascontiguousarray(cols, dtype=np.uint32)
+        n, m = len(off) - 1, len(col)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.uint32)
+        h = C.c_void_p()
+        _check(
+            N.load().gga_graph_from_csr(n, m, _ptr(off), _ptr(col) if m else None, None if w is None else _ptr(w), C.byref(h)),
+            "from_csr",
+        )
+        return cls(h.value)
+
+    @classmethod
+    def rmat(cls, scale: int, edge_factor: int = 16, a=0.57, b=0.19, c=0.19, seed: int = 1, wmin: int = 1, wmax: int = 255):
+        h = C.c_void_p()
+        _check(N.load().gga_graph_gen_rmat(scale, edge_factor, a, b, c, seed, wmin, wmax, C.byref(h)), "gen_rmat")
+        return cls(h.value)
+
+    @classmethod
+    def grid(cls, width: int, height: Optional[int] = None, del_prob=0.05, longrange_frac=0.001, seed: int = 3, wmin: int = 1, wmax: int = 1000):
+        h = C.c_void_p()
+        _check(
+            N.load().gga_graph_gen_grid(width, height or width, del_prob, longrange_frac, seed, wmin, wmax, C.byref(h)),
+            "gen_grid",
+        )
+        return cls(h.value)
+
+    def save_gr(self, path: str):
+        _check(N.load().gga_graph_save_gr(self._h, path.encode()), f"save_gr({path})")
+
+    def free(self):
+        if self._h and self._h.value:
+            N.load().gga_graph_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- description
+    def info(self) -> dict:
+        i = N.GraphInfo()
+        _check(N.load().gga_graph_get_info(self._h, C.byref(i)), "info")
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    @property
+    def n(self) -> int:
+        return self.info()["nodes_orig"]
+
+    @property
+    def m(self) -> int:
+        return self.info()["nedges"]
+
+    def csr(self):
+        """Copies of the unsplit 0-based CSR (offsets, cols, weights)."""
+        o, c, w = N.PU32(), N.PU32(), N.PU32()
+        _check(N.load().gga_graph_csr(self._h, C.byref(o), C.byref(c), C.byref(w)), "csr")
+        n, m = self.n, self.m
+        off = np.ctypeslib.as_array(o, shape=(n + 1,)).copy()
+        col = np.ctypeslib.as_array(c, shape=(m,)).copy() if m else np.zeros(0, np.uint32)
+        wt = np.ctypeslib.as_array(w, shape=(m,)).copy() if m else np.zeros(0, np.uint32)
+        return off, col, wt
+
+    def degrees(self) -> np.ndarray:
+        off = self.csr()[0]
+        return np.diff(off.astype(np.int64)).astype(np.uint32)
+
+    # ---- split rules (graph.h:338-414)
+    def getMaxdeg(self) -> int:
+        v = C.c_uint32()
+        _check(N.load().gga_max_degree(self._h, C.byref(v)), "getMaxdeg")
+        return v.value
+
+    def getMaxAllowedOutDegree(self, buckets: int = 10) -> int:
+        v = C.c_uint32()
+        _check(N.load().gga_max_allowed_out_degree(self._h, buckets, C.byref(v)), "getMaxAllowedOutDegree")
+        return v.value
+
+    def getSizeafterLoadBalance(self, level: int, buckets: int = 10):
+        """Returns (MAX_EDGES_ALLOWED, split vertex count)."""
+        mda, nn = C.c_uint32(), C.c_uint32()
+        _check(N.load().gga_size_after_split(self._h, level, buckets, C.byref(mda), C.byref(nn)), "getSizeafterLoadBalance")
+        return mda.value, nn.value
+
+    def NodeSplit(self, ctx: "Context", level: int, buckets: int = 10):
+        """Device-side node split (graph.h:415-522); level 0 removes it."""
+        _check(N.load().gga_node_split(ctx.handle, self._h, level, buckets), f"NodeSplit({level},{buckets})")
+
+    node_split = NodeSplit
+
+    def split_maps(self, ctx: "Context") -> dict:
+        """The split graph in the reference's layout (1-based psrc, slot-0 edge)."""
+        i = self.info()
+        nn, m = i["nnodes"], i["nedges"]
+        out = {
+            "psrc": np.zeros(nn + 1, np.uint32),
+            "noutgoing": np.zeros(nn, np.uint32),
+            "edgessrcdst": np.zeros(m + 1, np.uint32),
+            "childCount": np.zeros(nn, np.uint32),
+            "IsParent": np.zeros(nn, np.uint32),
+            "parentNode": np.zeros(nn, np.uint32),
+        }
+        _check(
+            N.load().gga_graph_split_maps(
+                ctx.handle, self._h, *[_ptr(out[k]) for k in ("psrc", "noutgoing", "edgessrcdst", "childCount", "IsParent", "parentNode")]
+            ),
+            "split_maps",
+        )
+        return out
+
+    def child_index(self, ctx: "Context"):
+        """(myChildIndex, myChildCount), bfs_sssp.cu:256-283."""
+        cnt = C.c_uint32(0)
+        st = N.load().gga_child_index(ctx.handle, self._h, C.byref(cnt), None, None)
+        if st not in (OK, ERR_INVALID_ARG):
+            _check(st, "child_index")
+        idx = np.zeros(max(cnt.value, 1), np.uint32)
+        cc = np.zeros(max(cnt.value, 1), np.uint32)
+        _check(N.load().gga_child_index(ctx.handle, self._h, C.byref(cnt), _ptr(idx), _ptr(cc)), "child_index")
+        return idx[: cnt.value], cc[: cnt.value]
+
+    def pin(self, on: bool = True):
+        _check(N.load().gga_graph_pin(self._h, 1 if on else 0), "pin")
+
+    def release_device(self):
+        _check(N.load().gga_graph_release_device(self._h), "release_device")
+
+    def cudaCopy(self, ctx: "Context"):
+        _check(N.load().gga_graph_upload(ctx.handle, self._h), "cudaCopy")
+
+    upload = cudaCopy
+
+    # ---- checks and output (myutils.h)
+    def verifysolution(self, dist: np.ndarray, algo="bfs") -> int:
+        d = np.ascontiguousarray(dist, dtype=np.uint32)
+        v = C.c_uint64()
+        _check(N.load().gga_verify(self._h, _algo(algo), _ptr(d), C.byref(v)), "verifysolution")
+        return v.value
+
+    verify = verifysolution
+
+    def Ary2File(self, path: str, dist: np.ndarray):
+        d = np.ascontiguousarray(dist, dtype=np.uint32)
+        _check(N.load().gga_write_dist(path.encode(), self._h, _ptr(d)), "Ary2File")
+
+    def reached(self, dist: np.ndarray):
+        d = np.ascontiguousarray(dist, dtype=np.uint32)
+        vr, er = C.c_uint64(), C.c_uint64()
+        _check(N.load().gga_reached(self._h, _ptr(d), C.byref(vr), C.byref(er)), "reached")
+        return vr.value, er.value
+
+
+def writeResult(path: str, **fields):
+    """Appends one 17-column result.vi row (myutils.h:86-113)."""
+    r = N.ResultRow()
+    for k, v in fields.items():
+        setattr(r, k, v.encode() if isinstance(v, str) else v)
+    _check(N.load().gga_write_result_row(path.encode(), C.byref(r)), "writeResult")
+
+
+class Context:
+    """A device context: stream, events and scratch on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        _check(N.load().gga_ctx_create(device, C.byref(self._h)), f"ctx_create({device})")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h and self._h.value:
+            N.load().gga_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def device_info(self):
+        sms = C.c_int()
+        name = C.create_string_buffer(256)
+        _check(N.load().gga_ctx_device_info(self._h, C.byref(sms), name, 256), "device_info")
+        return {"sms": sms.value, "name": name.value.decode()}
+
+    def mark(self, slot: int):
+        _check(N.load().gga_ctx_mark(self._h, slot), "mark")
+
+    def elapsed(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        _check(N.load().gga_ctx_elapsed(self._h, a, b, C.byref(ms)), "elapsed")
+        return ms.value
+
+    def synchronize(self):
+        _check(N.load().gga_ctx_synchronize(self._h), "synchronize")
+
+    def set_params(self, **kw):
+        p = N.Params()
+        _check(N.load().gga_get_params(self._h, C.byref(p)), "get_params")
+        for k, v in kw.items():
+            setattr(p, k, v)
+        _check(N.load().gga_set_params(self._h, C.byref(p)), "set_params")
+
+    def reset_params(self):
+        """Back to the per-graph defaults derived from the degree profile."""
+        _check(N.load().gga_set_params(self._h, None), "reset_params")
+
+    def params(self) -> dict:
+        p = N.Params()
+        _check(N.load().gga_get_params(self._h, C.byref(p)), "get_params")
+        return p.as_dict()
+
+    def autotune(self, graph: Graph, trials: int = 0) -> dict:
+        p = N.Params()
+        _check(N.load().gga_autotune(self._h, graph.handle, trials, C.byref(p)), "autotune")
+        return p.as_dict()
+
+    def solve(self, graph: Graph, algo, src: int, variant="auto", out=None, stats: bool = False,
+              keep_on_device: bool = False):
+        """Single-source BFS levels / SSSP distances in original vertex order.
+
+        out: numpy array, or any object with a ``data_ptr()`` (device buffer);
+        keep_on_device leaves the result in the context's device buffer."""
+        if keep_on_device:
+            ptr = None
+        else:
+            if out is None:
+                out = np.empty(graph.n, np.uint32)
+            ptr = C.c_void_p(out.data_ptr()) if hasattr(out, "data_ptr") else _ptr(out)
+        s = N.Stats()
+        _check(
+            N.load().gga_solve(self._h, graph.handle, _algo(algo), src, _variant(variant), ptr, C.byref(s)),
+            f"solve({algo}, src={src}, {variant})",
+        )
+        return (out, s.as_dict()) if stats else out
+
+    def bfs(self, graph: Graph, src: int, variant="auto", **kw):
+        return self.solve(graph, BFS, src, variant, **kw)
+
+    def sssp(self, graph: Graph, src: int, variant="auto", **kw):
+        return self.solve(graph, SSSP, src, variant, **kw)
+
+    def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False):
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        out = np.empty((len(s), graph.n), np.uint32)
+        st = N.Stats()
+        _check(N.load().gga_msbfs(self._h, graph.handle, len(s), _ptr(s), _ptr(out), C.byref(st)), "msbfs")
+        return (out, st.as_dict()) if stats else out
+
+    def sssp_batch(self, graph: Graph, srcs: Sequence[int], stats: bool = False):
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        out = np.empty((len(s), graph.n), np.uint32)
+        st = N.Stats()
+        _check(N.load().gga_sssp_batch(self._h, graph.handle, len(s), _ptr(s), _ptr(out), C.byref(st)), "sssp_batch")
+        return (out, st.as_dict()) if stats else out
+
+    def multi_solve(self, queries, stats: bool = False):
+        """queries: list of (graph, algo, src) -> list of distance arrays."""
+        outs = [np.empty(g.n, np.uint32) for g, _, _ in queries]
+        arr = (N.Query * len(queries))()
+        for i, (g, a, s) in enumerate(queries):
+            arr[i].graph = g.handle.value
+            arr[i].algo = _algo(a)
+            arr[i].src = s
+            arr[i].dist_out = outs[i].ctypes.data
+        st = N.Stats()
+        _check(N.load().gga_multi_solve(self._h, len(queries), arr, C.byref(st)), "multi_solve")
+        return (outs, st.as_dict()) if stats else outs
+
+
+class Server:
+    """Continuous-batching query loop over HBM-resident graphs."""
+
+    def __init__(self, ctx: Context, graphs: Sequence[Graph], mem_cap_bytes: int, max_slots: int = 64):
+        self._graphs = list(graphs)
+        arr = (C.c_void_p * len(graphs))(*[g.handle.value for g in graphs])
+        self._h = C.c_void_p()
+        _check(N.load().gga_server_create(ctx.handle, len(graphs), arr, mem_cap_bytes, max_slots, C.byref(self._h)), "server_create")
+        self._outs = {}
+
+    def submit(self, graph_index: int, algo, src: int) -> int:
+        out = np.empty(self._graphs[graph_index].n, np.uint32)
+        t = C.c_uint64()
+        _check(N.load().gga_server_submit(self._h, graph_index, _algo(algo), src, _ptr(out), C.byref(t)), "server_submit")
+        self._outs[t.value] = out
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000):
+        lat = C.c_double()
+        _check(N.load().gga_server_wait(self._h, ticket, timeout_ms, C.byref(lat)), "server_wait")
+        return self._outs.pop(ticket), lat.value
+
+    def poll(self, ticket: int):
+        lat = C.c_double()
+        st = N.load().gga_server_wait(self._h, ticket, 0, C.byref(lat))
+        if st == ERR_NOT_READY:
+            return None
+        _check(st, "server_poll")
+        return self._outs.pop(ticket), lat.value
+
+    def stats(self) -> dict:
+        s = N.ServerStats()
+        _check(N.load().gga_server_get_stats(self._h, C.byref(s)), "server_stats")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def close(self):
+        if self._h and self._h.value:
+            N.load().gga_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def version() -> str:
+    return N.load().gga_version().decode()

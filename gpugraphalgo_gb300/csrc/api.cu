@@ -1,0 +1,461 @@
+/*
+ * C ABI: device contexts and single-source solves.
+ *
+ * The reference's driver (bfs_sssp.cu:103-539) reads the graph, splits it,
+ * copies eight arrays to the device, initialises dist on the host, loops the
+ * relax kernel with two synchronous memcpys per iteration and copies dist
+ * back.  Here a context owns a stream, events and reusable device scratch; a
+ * solve is: upload once (cached) -> one persistent launch (frontier engine)
+ * or the reference's host loop (TOPO/CDP variants) -> gather the parents'
+ * distances in original order -> one copy to the caller's buffer.
+ */
+#include <mutex>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "ctx.cuh"
+
+/* ------------------------------------------------------------ context */
+
+gga_status ctx_activate(gga_ctx *c) {
+    GGA_CK(cudaSetDevice(c->device));
+    return GGA_OK;
+}
+
+gga_status gga_ctx_create(int device, gga_ctx **out) {
+    if (!out) return gga_fail(GGA_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+        return gga_fail(GGA_ERR_NO_DEVICE, "no CUDA device (%s)", e == cudaSuccess ? "count 0" : cudaGetErrorString(e));
+    if (device < 0 || device >= count) return gga_fail(GGA_ERR_INVALID_ARG, "device %d of %d", device, count);
+    GGA_CK(cudaSetDevice(device));
+    gga_ctx *c = new (std::nothrow) gga_ctx();
+    if (!c) return gga_fail(GGA_ERR_NO_MEMORY, "context");
+    c->device = device;
+    cudaDeviceProp p;
+    e = cudaGetDeviceProperties(&p, device);
+    if (e != cudaSuccess) { delete c; return gga_fail(GGA_ERR_CUDA, "device properties: %s", cudaGetErrorString(e)); }
+    c->sms = p.multiProcessorCount;
+    c->l2_bytes = (size_t)p.l2CacheSize;
+    snprintf(c->name, sizeof c->name, "%s", p.name);
+    e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->user_ev[i]);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->dflag, 64 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->hflag, 64 * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        gga_ctx_destroy(c);
+        return gga_fail(GGA_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
+    }
+    memset(&c->params, 0, sizeof c->params);
+    *out = c;
+    return GGA_OK;
+}
+
+void gga_ctx_destroy(gga_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    ctx_batch_release(c);
+    frontier_scratch_free(&c->fs);
+    cudaFree(c->dflag);
+    cudaFreeHost(c->hflag);
+    cudaFree(c->heavy);
+    for (int i = 0; i < 4; ++i)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int i = 0; i < 8; ++i)
+        if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+}
+
+gga_status gga_ctx_device_info(gga_ctx *c, int *sm_count, char *name, size_t name_len) {
+    if (!c) return gga_fail(GGA_ERR_INVALID_ARG, "NULL context");
+    if (sm_count) *sm_count = c->sms;
+    if (name && name_len) {
+        strncpy(name, c->name, name_len - 1);
+        name[name_len - 1] = 0;
+    }
+    return GGA_OK;
+}
+
+gga_status gga_ctx_mark(gga_ctx *c, int slot) {
+    if (!c || slot < 0 || slot >= 8) return gga_fail(GGA_ERR_INVALID_ARG, "bad context or slot");
+    GGA_CK(cudaSetDevice(c->device));
+    GGA_CK(cudaEventRecord(c->user_ev[slot], c->st));
+    return GGA_OK;
+}
+
+gga_status gga_ctx_elapsed(gga_ctx *c, int a, int b, double *ms) {
+    if (!c || !ms || a < 0 || a >= 8 || b < 0 || b >= 8) return gga_fail(GGA_ERR_INVALID_ARG, "bad context or slot");
+    GGA_CK(cudaSetDevice(c->device));
+    GGA_CK(cudaEventSynchronize(c->user_ev[b]));
+    float f = 0;
+    GGA_CK(cudaEventElapsedTime(&f, c->user_ev[a], c->user_ev[b]));
+    *ms = f;
+    return GGA_OK;
+}
+
+gga_status gga_ctx_synchronize(gga_ctx *c) {
+    if (!c) return gga_fail(GGA_ERR_INVALID_ARG, "NULL context");
+    GGA_CK(cudaSetDevice(c->device));
+    GGA_CK(cudaStreamSynchronize(c->st));
+    return GGA_OK;
+}
+
+gga_status gga_graph_pin(gga_graph *g, int pin) {
+    if (!g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL graph");
+    uint32_t *arr[3] = {g->off, g->col, g->wt};
+    size_t len[3] = {((size_t)g->n + 1) * 4, ((size_t)g->m + 1) * 4, ((size_t)g->m + 1) * 4};
+    for (int i = 0; i < 3; ++i) {
+        cudaError_t e = pin ? cudaHostRegister(arr[i], len[i], cudaHostRegisterDefault) : cudaHostUnregister(arr[i]);
+        if (e != cudaSuccess && e != cudaErrorHostMemoryAlreadyRegistered && e != cudaErrorHostMemoryNotRegistered)
+            return gga_fail(GGA_ERR_CUDA, "host register: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+    }
+    return GGA_OK;
+}
+
+gga_status gga_graph_release_device(gga_graph *g) {
+    if (!g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL graph");
+    pthread_mutex_lock(&g->lock);
+    if (g->dev && gga_dev_graph_release_hook) gga_dev_graph_release_hook(g);
+    g->split_level = 0;
+    g->ns = g->mda = g->parents_with_children = 0;
+    pthread_mutex_unlock(&g->lock);
+    return GGA_OK;
+}
+
+gga_status gga_graph_upload(gga_ctx *c, gga_graph *g) {
+    if (!c || !g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    gga_status s = ctx_activate(c);
+    if (s) return s;
+    return dev_graph_ensure(g, c->device, c->st);
+}
+
+/* ------------------------------------------------------------ split */
+
+gga_status dev_node_split(gga_graph *g, int32_t level, int32_t buckets, cudaStream_t st);
+gga_status dev_split_maps(gga_graph *g, uint32_t *psrc, uint32_t *noutgoing, uint32_t *edgessrcdst,
+                          uint32_t *child_count, uint32_t *is_parent, uint32_t *parent_node, cudaStream_t st);
+gga_status dev_child_index(gga_graph *g, uint32_t *count, uint32_t *cidx, uint32_t *ccnt, cudaStream_t st);
+
+gga_status gga_node_split(gga_ctx *c, gga_graph *g, int32_t level, int32_t buckets) {
+    if (!c || !g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    gga_status s = ctx_activate(c);
+    if (!s) s = dev_graph_ensure(g, c->device, c->st);
+    if (!s) s = dev_node_split(g, level, buckets, c->st);
+    return s;
+}
+
+gga_status gga_graph_split_maps(gga_ctx *c, const gga_graph *g, uint32_t *psrc, uint32_t *noutgoing,
+                                uint32_t *edgessrcdst, uint32_t *child_count, uint32_t *is_parent,
+                                uint32_t *parent_node) {
+    if (!c || !g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    gga_status s = ctx_activate(c);
+    if (!s) s = dev_graph_ensure((gga_graph *)g, c->device, c->st);
+    if (!s) s = dev_split_maps((gga_graph *)g, psrc, noutgoing, edgessrcdst, child_count, is_parent, parent_node, c->st);
+    return s;
+}
+
+gga_status gga_child_index(gga_ctx *c, const gga_graph *g, uint32_t *count, uint32_t *cidx, uint32_t *ccnt) {
+    if (!c || !g || !count) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    gga_status s = ctx_activate(c);
+    if (!s) s = dev_graph_ensure((gga_graph *)g, c->device, c->st);
+    if (!s) s = dev_child_index((gga_graph *)g, count, cidx, ccnt, c->st);
+    return s;
+}
+
+/* ------------------------------------------------------------ params */
+
+gga_status gga_set_params(gga_ctx *c, const gga_params *p) {
+    if (!c) return gga_fail(GGA_ERR_INVALID_ARG, "NULL context");
+    if (!p) {
+        c->params_set = false;
+        memset(&c->params, 0, sizeof c->params);
+        return GGA_OK;
+    }
+    if (p->block_threads && p->block_threads != 256 && p->block_threads != 512 && p->block_threads != 1024)
+        return gga_fail(GGA_ERR_INVALID_ARG, "block_threads must be 256, 512 or 1024");
+    if (p->cdp_mode > 2) return gga_fail(GGA_ERR_INVALID_ARG, "cdp_mode must be 0, 1 or 2");
+    c->params = *p;
+    c->params_set = true;
+    return GGA_OK;
+}
+
+gga_status gga_get_params(gga_ctx *c, gga_params *p) {
+    if (!c || !p) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    *p = c->params;
+    return GGA_OK;
+}
+
+/* Degree-profile defaults (gga_autotune refines them with timed trials). */
+gga_params ctx_default_params(const gga_graph *g) {
+    gga_params p;
+    memset(&p, 0, sizeof p);
+    p.block_threads = 256;
+    p.huge_degree = 4096;
+    uint64_t wsum = 0;
+    const uint32_t stride = g->m > (1u << 20) ? g->m >> 20 : 1;
+    uint32_t cnt = 0;
+    for (uint32_t e = 0; e < g->m; e += stride, ++cnt) wsum += g->wt[e];
+    const double wavg = cnt ? (double)wsum / cnt : 1.0;
+    const double davg = g->n ? (double)g->m / g->n : 1.0;
+    /* bucket width ~ a few average weights over the average degree */
+    double delta = wavg * 8.0 / (davg > 1.0 ? davg : 1.0);
+    if (delta < 1.0) delta = 1.0;
+    p.sssp_delta = (uint32_t)delta;
+    p.use_split = 1;
+    p.cdp_level = 1;
+    p.cdp_buckets = 10;
+    return p;
+}
+
+static gga_params effective_params(gga_ctx *c, const gga_graph *g) {
+    gga_params d = ctx_default_params(g);
+    if (!c->params_set) return d;
+    gga_params p = c->params;
+    if (!p.block_threads) p.block_threads = d.block_threads;
+    if (!p.huge_degree) p.huge_degree = d.huge_degree;
+    if (!p.cdp_buckets) p.cdp_buckets = d.cdp_buckets;
+    if (!p.cdp_level) p.cdp_level = d.cdp_level;
+    return p;
+}
+
+/* ------------------------------------------------------------ solve */
+
+__global__ void k_gather_parents(const uint32_t *dist, const uint32_t *first, uint32_t n, uint32_t *out) {
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n; u += (uint64_t)gridDim.x * blockDim.x)
+        out[u] = dist[first[u]];
+}
+
+__global__ void k_reached(const uint32_t *dist, const uint32_t *off, uint32_t n, unsigned long long *acc) {
+    unsigned long long vr = 0, er = 0;
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n; u += (uint64_t)gridDim.x * blockDim.x)
+        if (dist[u] < GGA_INFINITY) {
+            vr++;
+            er += off[u + 1] - off[u];
+        }
+    vr = __reduce_add_sync(0xffffffffu, (uint32_t)vr);
+    for (int d = 16; d > 0; d >>= 1) er += __shfl_down_sync(0xffffffffu, er, d);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(acc, vr);
+        atomicAdd(acc + 1, er);
+    }
+}
+
+bool ptr_is_device(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+unsigned ctx_grid(const gga_ctx *c, uint64_t items, unsigned bs) {
+    uint64_t b = (items + bs - 1) / bs;
+    uint64_t cap = (uint64_t)c->sms * 32;
+    if (b > cap) b = cap;
+    return b ? (unsigned)b : 1;
+}
+
+/* Copies the original-order result (device) to the caller and fills the
+ * reached-vertex statistics. */
+gga_status ctx_finish_output(gga_ctx *c, const DevGraph *d, const uint32_t *dev_out, uint32_t *dist_out,
+                             gga_stats *stats) {
+    const size_t bytes = (size_t)d->n * sizeof(uint32_t);
+    if (dist_out && dev_out != dist_out)
+        GGA_CK(cudaMemcpyAsync(dist_out, dev_out, bytes,
+                               ptr_is_device(dist_out) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+    if (stats) {
+        unsigned long long *acc = (unsigned long long *)(c->dflag + 32);
+        GGA_CK(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), c->st));
+        k_reached<<<ctx_grid(c, d->n, 256), 256, 0, c->st>>>(dev_out, d->off, d->n, acc);
+        GGA_CK(cudaMemcpyAsync(c->hflag + 32, acc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+    }
+    GGA_CK(cudaStreamSynchronize(c->st));
+    if (stats) {
+        const unsigned long long *h = (const unsigned long long *)(c->hflag + 32);
+        stats->vertices_reached = h[0];
+        stats->edges_reached = h[1];
+    }
+    return GGA_OK;
+}
+
+struct TopoResult {
+    uint32_t iterations, launches, cdp_children, cdp_fallbacks;
+    float ktime, sktime;
+};
+gga_status topo_run(const DevGraph *d, bool split, gga_variant variant, bool sssp, uint32_t src,
+                    uint32_t max_allowed, uint32_t cdp_mode, uint32_t *dist, uint32_t *scratch_heavy,
+                    uint32_t *dflag, uint32_t *hflag, int sms, cudaStream_t st, cudaEvent_t *ev,
+                    TopoResult *res);
+
+gga_status ctx_validate_solve(const gga_graph *g, gga_algo algo, uint32_t src) {
+    if (algo != GGA_BFS && algo != GGA_SSSP) return gga_fail(GGA_ERR_INVALID_ARG, "unknown algorithm %d", (int)algo);
+    if (src >= g->n) return gga_fail(GGA_ERR_INVALID_ARG, "source %u >= %u vertices", src, g->n);
+    if (algo == GGA_SSSP && g->maxw > GGA_MAX_WEIGHT)
+        return gga_fail(GGA_ERR_INVALID_ARG, "edge weight %u > %u: dist + weight would wrap in uint32", g->maxw,
+                        GGA_MAX_WEIGHT);
+    return GGA_OK;
+}
+
+gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_variant variant,
+                     uint32_t *dist_out, gga_stats *stats) {
+    const double t0 = gga_now_ms();
+    if (!c || !g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    gga_status s = ctx_validate_solve(g, algo, src);
+    if (s) return s;
+    if ((int)variant < GGA_VARIANT_AUTO || (int)variant > GGA_VARIANT_CDP_PLAIN)
+        return gga_fail(GGA_ERR_INVALID_ARG, "unknown variant %d", (int)variant);
+    std::lock_guard<std::mutex> lk(c->mu);
+    if ((s = ctx_activate(c))) return s;
+    if ((s = dev_graph_ensure(g, c->device, c->st))) return s;
+    const DevGraph *d = dev_graph_of(g);
+    const gga_params p = effective_params(c, g);
+    const bool sssp = algo == GGA_SSSP;
+    const bool split = d->level != 0;
+    gga_stats st;
+    memset(&st, 0, sizeof st);
+
+    if (variant == GGA_VARIANT_AUTO || variant == GGA_VARIANT_FRONTIER) {
+        const bool use_split = split && p.use_split;
+        const GraphView v = dev_graph_view(d, use_split);
+        if ((s = frontier_scratch_ensure(&c->fs, v.n > d->n ? v.n : d->n, d->m))) return s;
+        FrontierResult r;
+        s = frontier_run(&c->fs, v, use_split ? d->first : nullptr, src, sssp, p, c->sms, c->st, c->ev[0], c->ev[1], &r);
+        if (s) return s;
+        st.iterations = r.rounds;
+        st.kernel_launches = r.launches;
+        st.edges_relaxed = r.edges_relaxed;
+        st.kernel_ms = r.kernel_ms;
+        const uint32_t *res = c->fs.dist;
+        if (use_split) {
+            k_gather_parents<<<ctx_grid(c, d->n, 256), 256, 0, c->st>>>(c->fs.dist, d->first, d->n, c->fs.out);
+            st.kernel_launches++;
+            res = c->fs.out;
+        }
+        if ((s = ctx_finish_output(c, d, res, dist_out, stats && !p.skip_reached ? &st : nullptr))) return s;
+    } else {
+        const bool cdp = variant == GGA_VARIANT_CDP_ATOMIC || variant == GGA_VARIANT_CDP_PLAIN;
+        uint32_t max_allowed = d->maxdeg;
+        if (cdp) {
+            /* bfs_sssp.cu:224-236: histogram rule for a negative level, else ceil(maxdeg/level) */
+            if (p.cdp_level < 0) {
+                if ((s = gga_max_allowed_out_degree(g, p.cdp_buckets, &max_allowed))) return s;
+            } else {
+                const uint32_t lv = p.cdp_level > 0 ? (uint32_t)p.cdp_level : 1u;
+                max_allowed = (uint32_t)(((uint64_t)d->maxdeg + lv - 1) / lv);
+            }
+            if (c->heavy_cap < d->n) {
+                cudaFree(c->heavy);
+                c->heavy = nullptr;
+                c->heavy_cap = 0;
+                GGA_CK(cudaMalloc((void **)&c->heavy, (size_t)d->n * sizeof(uint32_t)));
+                c->heavy_cap = d->n;
+            }
+            if (p.cdp_pending_limit)
+                GGA_CK(cudaDeviceSetLimit(cudaLimitDevRuntimePendingLaunchCount, p.cdp_pending_limit));
+        }
+        const GraphView v = dev_graph_view(d, split && !cdp);
+        if ((s = frontier_scratch_ensure(&c->fs, v.n > d->n ? v.n : d->n, d->m))) return s;
+        TopoResult r;
+        s = topo_run(d, split, variant, sssp, src, max_allowed, p.cdp_mode, c->fs.dist, c->heavy, c->dflag, c->hflag,
+                     c->sms, c->st, c->ev, &r);
+        if (s) return s;
+        st.iterations = r.iterations;
+        st.kernel_launches = r.launches;
+        st.kernel_ms = r.ktime;
+        st.aux_ms = r.sktime;
+        st.cdp_children = r.cdp_children;
+        st.cdp_fallbacks = r.cdp_fallbacks;
+        const uint32_t *res = c->fs.dist;
+        if (split && !cdp) {
+            k_gather_parents<<<ctx_grid(c, d->n, 256), 256, 0, c->st>>>(c->fs.dist, d->first, d->n, c->fs.out);
+            st.kernel_launches++;
+            res = c->fs.out;
+        }
+        if ((s = ctx_finish_output(c, d, res, dist_out, stats && !p.skip_reached ? &st : nullptr))) return s;
+    }
+    st.total_ms = gga_now_ms() - t0;
+    if (stats) *stats = st;
+    return GGA_OK;
+}
+
+gga_status gga_bfs(gga_ctx *c, gga_graph *g, uint32_t src, gga_variant variant, uint32_t *dist_out, gga_stats *stats) {
+    return gga_solve(c, g, GGA_BFS, src, variant, dist_out, stats);
+}
+
+gga_status gga_sssp(gga_ctx *c, gga_graph *g, uint32_t src, gga_variant variant, uint32_t *dist_out, gga_stats *stats) {
+    return gga_solve(c, g, GGA_SSSP, src, variant, dist_out, stats);
+}
+
+/* ------------------------------------------------------------ autotune */
+
+gga_status gga_autotune(gga_ctx *c, gga_graph *g, uint32_t trials, gga_params *chosen) {
+    if (!c || !g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    gga_params best = ctx_default_params(g);
+    if (c->params_set) {
+        best.use_split = c->params.use_split;
+        best.cdp_mode = c->params.cdp_mode;
+        best.cdp_level = c->params.cdp_level ? c->params.cdp_level : best.cdp_level;
+        best.cdp_buckets = c->params.cdp_buckets ? c->params.cdp_buckets : best.cdp_buckets;
+    }
+    if (trials) {
+        /* time SSSP from the highest-degree vertex for a few bucket widths
+         * and CTA sizes; keep the fastest (all give identical distances) */
+        uint32_t src = 0, md = 0;
+        for (uint32_t u = 0; u < g->n; ++u) {
+            const uint32_t dgr = g->off[u + 1] - g->off[u];
+            if (dgr > md) { md = dgr; src = u; }
+        }
+        uint32_t *tmp = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(c->mu);
+            gga_status s = ctx_activate(c);
+            if (!s) s = dev_graph_ensure(g, c->device, c->st);
+            if (s) return s;
+            GGA_CK(cudaMalloc((void **)&tmp, (size_t)g->n * sizeof(uint32_t)));
+        }
+        const uint32_t base = best.sssp_delta;
+        const uint32_t deltas[] = {base / 4 ? base / 4 : 1, base / 2 ? base / 2 : 1, base, base * 2, base * 4, 0};
+        const uint32_t sizes[] = {256, 512};
+        double best_ms = 1e30;
+        gga_params saved = c->params;
+        const bool saved_set = c->params_set;
+        for (uint32_t bs : sizes) {
+            for (uint32_t dl : deltas) {
+                gga_params p = best;
+                p.block_threads = bs;
+                p.sssp_delta = dl;
+                c->params = p;
+                c->params_set = true;
+                double tsum = 0;
+                gga_status s = GGA_OK;
+                for (uint32_t t = 0; t < trials && !s; ++t) {
+                    gga_stats st;
+                    s = gga_solve(c, g, g->maxw <= GGA_MAX_WEIGHT ? GGA_SSSP : GGA_BFS, src, GGA_VARIANT_FRONTIER, tmp, &st);
+                    tsum += st.kernel_ms;
+                }
+                if (!s && tsum < best_ms) {
+                    best_ms = tsum;
+                    best = p;
+                }
+            }
+        }
+        c->params = saved;
+        c->params_set = saved_set;
+        cudaFree(tmp);
+    }
+    c->params = best;
+    c->params_set = true;
+    if (chosen) *chosen = best;
+    return GGA_OK;
+}

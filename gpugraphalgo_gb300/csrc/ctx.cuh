@@ -1,0 +1,37 @@
+/*
+ * The device context behind gga_ctx (one per host thread).
+ */
+#pragma once
+#include <mutex>
+
+#include "frontier.cuh"
+
+struct BatchScratch;
+
+struct gga_ctx {
+    int device = 0;
+    int sms = 0;
+    size_t l2_bytes = 0;
+    char name[256] = {0};
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t user_ev[8] = {};
+    gga_params params;
+    bool params_set = false;
+    FrontierScratch fs = {};
+    uint32_t *dflag = nullptr; /* 64 words of device flags / counters */
+    uint32_t *hflag = nullptr; /* pinned mirror */
+    uint32_t *heavy = nullptr; /* CDP heavy-vertex list */
+    uint32_t heavy_cap = 0;
+    BatchScratch *batch = nullptr;
+    std::mutex mu;
+};
+
+gga_status ctx_activate(gga_ctx *c);
+gga_params ctx_default_params(const gga_graph *g);
+gga_status ctx_validate_solve(const gga_graph *g, gga_algo algo, uint32_t src);
+gga_status ctx_finish_output(gga_ctx *c, const DevGraph *d, const uint32_t *dev_out, uint32_t *dist_out,
+                             gga_stats *stats);
+unsigned ctx_grid(const gga_ctx *c, uint64_t items, unsigned bs);
+bool ptr_is_device(const void *p);
+void ctx_batch_release(gga_ctx *c);

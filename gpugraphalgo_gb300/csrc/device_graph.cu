@@ -1,0 +1,468 @@
+/*
+ * Device residency of a graph (Graph::cudaCopy, graph.h:683-699) and the
+ * device-side node-split builder (Graph::NodeSplit, graph.h:415-522, with the
+ * INT_SPLIT slicing of bfs_sssp.cu:60 and the child-index lists of
+ * bfs_sssp.cu:256-283).
+ *
+ * Split on the device, in five launches over HBM-resident arrays:
+ *   1. degree histogram -> MDA (getMaxAllowedOutDegree, graph.h:359-385) when
+ *      the level is negative; ceil(maxdeg/level) otherwise (graph.h:390);
+ *   2. pieces[u] = max(1, ceil(deg/MDA))                     (graph.h:401-410);
+ *   3. exclusive scan of pieces -> first[u] = u + presum[u]  (graph.h:429-456);
+ *   4. one thread per split id fills psrc/noutgoing slices, childCount,
+ *      IsParent and parentNode                               (graph.h:458-495);
+ *   5. edge targets remapped, dst' = first[dst]              (graph.h:500-502).
+ * The arrays are identical to the reference's (tests compare them element by
+ * element); only psrc is stored 0-based.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include "gga_device.cuh"
+
+/* ------------------------------------------------------------------ scan */
+
+static constexpr uint32_t SCAN_BS = 1024, SCAN_ITEMS = 4;
+static constexpr uint32_t SCAN_TILE = SCAN_BS * SCAN_ITEMS;
+
+__global__ void __launch_bounds__(SCAN_BS) k_tile_sums(const uint32_t *in, uint32_t count, uint32_t *sums) {
+    __shared__ uint32_t ws[32];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < SCAN_ITEMS; ++i)
+        if (base + i < count) s += in[base + i];
+    uint32_t tot;
+    block_exclusive_scan(s, ws, &tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(SCAN_BS) k_tile_scan(const uint32_t *in, uint32_t count,
+                                                      const uint32_t *tile_base, uint32_t *out) {
+    __shared__ uint32_t ws[32];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < SCAN_ITEMS; ++i) {
+        v[i] = base + i < count ? in[base + i] : 0;
+        s += v[i];
+    }
+    uint32_t tot;
+    uint32_t p = block_exclusive_scan(s, ws, &tot) + tile_base[blockIdx.x];
+#pragma unroll
+    for (uint32_t i = 0; i < SCAN_ITEMS; ++i) {
+        if (base + i < count) out[base + i] = p;
+        p += v[i];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[count] = p;
+}
+
+/* out[0..count] = exclusive prefix sums of in[0..count-1]; out[count] = total.
+ * `in` and `out` may alias only if identical. */
+gga_status dev_exclusive_scan(const uint32_t *in, uint32_t *out, uint32_t count, cudaStream_t st) {
+    if (count == 0) {
+        GGA_CK(cudaMemsetAsync(out, 0, sizeof(uint32_t), st));
+        return GGA_OK;
+    }
+    uint32_t tiles = (count + SCAN_TILE - 1) / SCAN_TILE;
+    uint32_t *sums = nullptr;
+    GGA_CK(cudaMallocAsync((void **)&sums, ((size_t)tiles + 1) * 2 * sizeof(uint32_t), st));
+    uint32_t *scanned = sums + tiles + 1;
+    k_tile_sums<<<tiles, SCAN_BS, 0, st>>>(in, count, sums);
+    gga_status s = GGA_OK;
+    if (tiles > 1) {
+        s = dev_exclusive_scan(sums, scanned, tiles, st);
+    } else {
+        cudaMemsetAsync(scanned, 0, sizeof(uint32_t), st);
+    }
+    if (s == GGA_OK) k_tile_scan<<<tiles, SCAN_BS, 0, st>>>(in, count, scanned, out);
+    cudaFreeAsync(sums, st);
+    GGA_CK(cudaGetLastError());
+    return s;
+}
+
+/* ------------------------------------------------------------ residency */
+
+static void dev_free_split(DevGraph *d) {
+    cudaFree(d->s_off); cudaFree(d->s_col); cudaFree(d->s_cc); cudaFree(d->s_isp);
+    cudaFree(d->s_par); cudaFree(d->first); cudaFree(d->cidx); cudaFree(d->ccnt);
+    d->s_off = d->s_col = d->s_cc = d->s_isp = d->s_par = d->first = d->cidx = d->ccnt = nullptr;
+    d->level = 0;
+    d->ns = d->mda = d->npar = 0;
+}
+
+static void dev_graph_release(gga_graph *g) {
+    DevGraph *d = (DevGraph *)g->dev;
+    if (!d) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(d->device);
+    dev_free_split(d);
+    cudaFree(d->off); cudaFree(d->col); cudaFree(d->wt);
+    if (prev >= 0) cudaSetDevice(prev);
+    free(d);
+    g->dev = nullptr;
+    g->dev_device = -1;
+}
+
+DevGraph *dev_graph_of(gga_graph *g) { return (DevGraph *)g->dev; }
+
+GraphView dev_graph_view(const DevGraph *d, bool split) {
+    GraphView v;
+    if (split && d->level != 0) {
+        v.off = d->s_off; v.col = d->s_col; v.wt = d->wt; v.cc = d->s_cc; v.n = d->ns; v.m = d->m;
+    } else {
+        v.off = d->off; v.col = d->col; v.wt = d->wt; v.cc = nullptr; v.n = d->n; v.m = d->m;
+    }
+    return v;
+}
+
+/* Uploads g to `device` once; later calls return at once (cudaCopy,
+ * graph.h:683-699 copies eight arrays; the relaxation needs three). */
+gga_status dev_graph_ensure(gga_graph *g, int device, cudaStream_t st) {
+    if (g->dev) {
+        if (g->dev_device != device)
+            return gga_fail(GGA_ERR_INVALID_ARG, "graph is resident on device %d, context uses %d",
+                            g->dev_device, device);
+        return GGA_OK;
+    }
+    pthread_mutex_lock(&g->lock);
+    gga_status s = GGA_OK;
+    if (!g->dev) {
+        gga_dev_graph_release_hook = dev_graph_release;
+        DevGraph *d = (DevGraph *)calloc(1, sizeof *d);
+        if (!d) {
+            pthread_mutex_unlock(&g->lock);
+            return gga_fail(GGA_ERR_NO_MEMORY, "DevGraph");
+        }
+        d->device = device;
+        d->n = g->n;
+        d->m = g->m;
+        d->maxdeg = g->maxdeg;
+        size_t mpad = ((size_t)g->m + 4) & ~(size_t)3; /* room for 16-byte vector loads */
+        cudaError_t e = cudaMalloc((void **)&d->off, ((size_t)g->n + 1) * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d->col, mpad * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d->wt, mpad * sizeof(uint32_t));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d->off, g->off, ((size_t)g->n + 1) * sizeof(uint32_t),
+                                cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && g->m)
+            e = cudaMemcpyAsync(d->col, g->col, (size_t)g->m * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && g->m)
+            e = cudaMemcpyAsync(d->wt, g->wt, (size_t)g->m * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d->col + g->m, 0, (mpad - g->m) * sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d->wt + g->m, 0, (mpad - g->m) * sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            cudaFree(d->off); cudaFree(d->col); cudaFree(d->wt);
+            free(d);
+            s = gga_fail(GGA_ERR_CUDA, "graph upload (%u vertices, %u edges): %s", g->n, g->m,
+                         cudaGetErrorString(e));
+        } else {
+            g->dev = d;
+            g->dev_device = device;
+        }
+    }
+    pthread_mutex_unlock(&g->lock);
+    return s;
+}
+
+/* ------------------------------------------------------------ split */
+
+__global__ void k_max_degree(const uint32_t *off, uint32_t n, uint32_t *out) {
+    uint32_t best = 0;
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n;
+         u += (uint64_t)gridDim.x * blockDim.x)
+        best = max(best, off[u + 1] - off[u]);
+    best = __reduce_max_sync(0xffffffffu, best);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, best);
+}
+
+/* Bucket = (int)((deg / (float)(maxdeg+1)) * buckets) in round-to-nearest
+ * single precision, as graph.h:365 computes it on the host. */
+__global__ void k_degree_histogram(const uint32_t *off, uint32_t n, const uint32_t *maxdeg,
+                                   int32_t buckets, uint32_t *histo) {
+    extern __shared__ uint32_t sh[];
+    const bool use_smem = buckets <= 8192;
+    if (use_smem)
+        for (int32_t i = threadIdx.x; i < buckets; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    const float fm = (float)(int32_t)(*maxdeg + 1u), fb = (float)buckets;
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        float q = __fdiv_rn((float)(off[u + 1] - off[u]), fm);
+        int32_t idx = (int32_t)__fmul_rn(q, fb);
+        if (idx >= buckets) idx = buckets - 1;
+        atomicAdd(use_smem ? &sh[idx] : &histo[idx], 1u);
+    }
+    __syncthreads();
+    if (use_smem)
+        for (int32_t i = threadIdx.x; i < buckets; i += blockDim.x)
+            if (sh[i]) atomicAdd(&histo[i], sh[i]);
+}
+
+/* MAX_EDGES_ALLOWED from the split level or the histogram (first maximum). */
+__global__ void k_split_limit(const uint32_t *histo, int32_t buckets, int32_t level,
+                              const uint32_t *maxdeg, uint32_t *mda) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t md = *maxdeg;
+    if (level > 0) {
+        *mda = (uint32_t)(((uint64_t)md + (uint32_t)level - 1) / (uint32_t)level);
+        return;
+    }
+    int32_t best = -1, bi = -1;
+    for (int32_t i = 0; i < buckets; ++i)
+        if ((int32_t)histo[i] > best) { best = (int32_t)histo[i]; bi = i; }
+    int32_t maxdeg1 = (int32_t)md + 1;
+    *mda = (uint32_t)((maxdeg1 / buckets) * (bi + 1));
+}
+
+__global__ void k_pieces(const uint32_t *off, uint32_t n, const uint32_t *mda, uint32_t *pieces,
+                         uint32_t *err) {
+    const uint32_t lim = *mda;
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t d = off[u + 1] - off[u];
+        uint32_t p = 1;
+        if (d) {
+            if (lim == 0) {
+                atomicExch(err, GGA_DEV_SPLIT_RULE);
+                p = 1;
+            } else {
+                p = (uint32_t)(((uint64_t)d + lim - 1) / lim);
+            }
+        }
+        pieces[u] = p;
+    }
+}
+
+/* One thread per split id k: owner u has first[u] <= k < first[u+1]. */
+__global__ void k_split_fill(const uint32_t *off, uint32_t n, uint32_t m, const uint32_t *first,
+                             uint32_t ns, uint32_t *s_off, uint32_t *s_cc, uint32_t *s_isp,
+                             uint32_t *s_par) {
+    for (uint64_t k64 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k64 < ns;
+         k64 += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t k = (uint32_t)k64;
+        uint32_t lo = 0, hi = n; /* last u with first[u] <= k */
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (first[mid] <= k) lo = mid; else hi = mid;
+        }
+        uint32_t u = lo;
+        uint32_t j = k - first[u];
+        uint32_t pieces = first[u + 1] - first[u];
+        uint32_t deg = off[u + 1] - off[u];
+        uint32_t local = deg ? (deg + pieces - 1) / pieces : 0; /* INT_SPLIT, graph.h:462 */
+        s_off[k] = off[u] + j * local;
+        s_cc[k] = j == 0 ? pieces - 1 : 0;
+        s_isp[k] = j == 0 ? 1u : 0u;
+        s_par[k] = u;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) s_off[ns] = m;
+}
+
+__global__ void k_remap_targets(const uint32_t *col, uint32_t m, const uint32_t *first, uint32_t *s_col) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+         e += (uint64_t)gridDim.x * blockDim.x)
+        s_col[e] = first[col[e]];
+}
+
+__global__ void k_flag_parents(const uint32_t *s_cc, uint32_t ns, uint32_t *flags) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < ns;
+         k += (uint64_t)gridDim.x * blockDim.x)
+        flags[k] = s_cc[k] ? 1u : 0u;
+}
+
+__global__ void k_compact_parents(const uint32_t *s_cc, uint32_t ns, const uint32_t *pos,
+                                  uint32_t *cidx, uint32_t *ccnt) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < ns;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t c = s_cc[k];
+        if (c) {
+            cidx[pos[k]] = (uint32_t)k;
+            ccnt[pos[k]] = c;
+        }
+    }
+}
+
+static unsigned grid_for(uint64_t items, unsigned bs) {
+    uint64_t b = (items + bs - 1) / bs;
+    if (b < 1) b = 1;
+    if (b > 152u * 64u) b = 152u * 64u;
+    return (unsigned)b;
+}
+
+/* Builds the split for `level`/`buckets` on the device (ctx stream `st`). */
+gga_status dev_node_split(gga_graph *g, int32_t level, int32_t buckets, cudaStream_t st) {
+    DevGraph *d = (DevGraph *)g->dev;
+    if (!d) return gga_fail(GGA_ERR_INVALID_ARG, "graph not resident");
+    dev_free_split(d);
+    g->split_level = 0;
+    g->ns = g->mda = g->parents_with_children = 0;
+    if (level == 0) return GGA_OK;
+    if (level < 0 && buckets <= 0)
+        return gga_fail(GGA_ERR_INVALID_ARG, "buckets must be positive (got %d)", buckets);
+
+    const uint32_t n = d->n, m = d->m;
+    uint32_t *scal = nullptr; /* [0]=maxdeg [1]=mda [2]=err */
+    uint32_t *histo = nullptr, *pieces = nullptr;
+    gga_status s = GGA_OK;
+    uint32_t hs[3];
+    int32_t nb = level < 0 ? buckets : 1;
+    GGA_CK(cudaMallocAsync((void **)&scal, 4 * sizeof(uint32_t), st));
+    GGA_CK(cudaMallocAsync((void **)&histo, (size_t)nb * sizeof(uint32_t), st));
+    GGA_CK(cudaMallocAsync((void **)&pieces, ((size_t)n + 1) * sizeof(uint32_t), st));
+    cudaMemsetAsync(scal, 0, 4 * sizeof(uint32_t), st);
+    cudaMemsetAsync(histo, 0, (size_t)nb * sizeof(uint32_t), st);
+    k_max_degree<<<grid_for(n, 256), 256, 0, st>>>(d->off, n, scal);
+    if (level < 0) {
+        size_t sm = buckets <= 8192 ? (size_t)buckets * sizeof(uint32_t) : 0;
+        k_degree_histogram<<<grid_for(n, 256), 256, sm, st>>>(d->off, n, scal, buckets, histo);
+    }
+    k_split_limit<<<1, 32, 0, st>>>(histo, nb, level, scal, scal + 1);
+    k_pieces<<<grid_for(n, 256), 256, 0, st>>>(d->off, n, scal + 1, pieces, scal + 2);
+    cudaError_t e = cudaMemcpyAsync(hs, scal, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        s = gga_fail(GGA_ERR_CUDA, "split limit: %s", cudaGetErrorString(e));
+        goto done;
+    }
+    if (hs[2] == GGA_DEV_SPLIT_RULE) {
+        s = gga_fail(GGA_ERR_SPLIT_RULE,
+                     "edge limit is 0 (maxdeg %u, level %d, buckets %d): the reference divides by zero",
+                     hs[0], level, buckets);
+        goto done;
+    }
+    GGA_CK(cudaMalloc((void **)&d->first, ((size_t)n + 1) * sizeof(uint32_t)));
+    s = dev_exclusive_scan(pieces, d->first, n, st);
+    if (s) goto done;
+    {
+        uint32_t ns = 0;
+        e = cudaMemcpyAsync(&ns, d->first + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { s = gga_fail(GGA_ERR_CUDA, "split size: %s", cudaGetErrorString(e)); goto done; }
+        if (ns > GGA_MAX_NODES) { s = gga_fail(GGA_ERR_TOO_LARGE, "split gives %u vertices", ns); goto done; }
+        size_t mpad = ((size_t)m + 4) & ~(size_t)3;
+        e = cudaMalloc((void **)&d->s_off, ((size_t)ns + 1) * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d->s_cc, (size_t)ns * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d->s_isp, (size_t)ns * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d->s_par, (size_t)ns * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d->s_col, mpad * sizeof(uint32_t));
+        if (e != cudaSuccess) { s = gga_fail(GGA_ERR_CUDA, "split arrays: %s", cudaGetErrorString(e)); goto done; }
+        cudaMemsetAsync(d->s_col + m, 0, (mpad - m) * sizeof(uint32_t), st);
+        k_split_fill<<<grid_for(ns, 256), 256, 0, st>>>(d->off, n, m, d->first, ns, d->s_off, d->s_cc,
+                                                        d->s_isp, d->s_par);
+        k_remap_targets<<<grid_for(m, 256), 256, 0, st>>>(d->col, m, d->first, d->s_col);
+        /* child index lists: reuse `pieces` as flags when large enough */
+        uint32_t *flags = nullptr, *pos = nullptr;
+        GGA_CK(cudaMallocAsync((void **)&flags, ((size_t)ns + 1) * 2 * sizeof(uint32_t), st));
+        pos = flags + ns + 1;
+        k_flag_parents<<<grid_for(ns, 256), 256, 0, st>>>(d->s_cc, ns, flags);
+        s = dev_exclusive_scan(flags, pos, ns, st);
+        uint32_t npar = 0;
+        if (s == GGA_OK) {
+            e = cudaMemcpyAsync(&npar, pos + ns, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e == cudaSuccess) e = cudaMalloc((void **)&d->cidx, ((size_t)npar + 1) * sizeof(uint32_t));
+            if (e == cudaSuccess) e = cudaMalloc((void **)&d->ccnt, ((size_t)npar + 1) * sizeof(uint32_t));
+            if (e == cudaSuccess)
+                k_compact_parents<<<grid_for(ns, 256), 256, 0, st>>>(d->s_cc, ns, pos, d->cidx, d->ccnt);
+            if (e == cudaSuccess) e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) s = gga_fail(GGA_ERR_CUDA, "child index: %s", cudaGetErrorString(e));
+        }
+        cudaFreeAsync(flags, st);
+        if (s) goto done;
+        d->level = level;
+        d->buckets = buckets;
+        d->ns = ns;
+        d->mda = hs[1];
+        d->npar = npar;
+        d->maxdeg = hs[0];
+        g->split_level = level;
+        g->split_buckets = buckets;
+        g->ns = ns;
+        g->mda = hs[1];
+        g->parents_with_children = npar;
+    }
+done:
+    cudaFreeAsync(scal, st);
+    cudaFreeAsync(histo, st);
+    cudaFreeAsync(pieces, st);
+    if (s) dev_free_split(d);
+    cudaStreamSynchronize(st);
+    return s;
+}
+
+/* Reference-layout export of the (split) graph. */
+__global__ void k_export_psrc(const uint32_t *s_off, uint32_t ns, uint32_t m, uint32_t *psrc,
+                              uint32_t *nout) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k <= ns;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        if (k < ns) {
+            if (psrc) psrc[k] = s_off[k] + 1;
+            if (nout) nout[k] = s_off[k + 1] - s_off[k];
+        } else if (psrc) {
+            psrc[ns] = m; /* graph.h:498 */
+        }
+    }
+}
+
+gga_status dev_split_maps(gga_graph *g, uint32_t *psrc, uint32_t *noutgoing, uint32_t *edgessrcdst,
+                          uint32_t *child_count, uint32_t *is_parent, uint32_t *parent_node,
+                          cudaStream_t st) {
+    DevGraph *d = (DevGraph *)g->dev;
+    const bool split = d->level != 0;
+    const uint32_t n = split ? d->ns : d->n, m = d->m;
+    uint32_t *tmp = nullptr;
+    GGA_CK(cudaMallocAsync((void **)&tmp, ((size_t)n + 1) * 2 * sizeof(uint32_t), st));
+    uint32_t *t_psrc = tmp, *t_nout = tmp + n + 1;
+    k_export_psrc<<<grid_for(n + 1, 256), 256, 0, st>>>(split ? d->s_off : d->off, n, m, t_psrc, t_nout);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && psrc)
+        e = cudaMemcpyAsync(psrc, t_psrc, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && noutgoing)
+        e = cudaMemcpyAsync(noutgoing, t_nout, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && edgessrcdst) {
+        edgessrcdst[0] = 0; /* null slot; left uninitialised by the reference */
+        if (m)
+            e = cudaMemcpyAsync(edgessrcdst + 1, split ? d->s_col : d->col, (size_t)m * 4,
+                                cudaMemcpyDeviceToHost, st);
+    }
+    if (split) {
+        if (e == cudaSuccess && child_count)
+            e = cudaMemcpyAsync(child_count, d->s_cc, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && is_parent)
+            e = cudaMemcpyAsync(is_parent, d->s_isp, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && parent_node)
+            e = cudaMemcpyAsync(parent_node, d->s_par, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFreeAsync(tmp, st);
+    cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return gga_fail(GGA_ERR_CUDA, "split export: %s", cudaGetErrorString(e));
+    if (!split) {
+        for (uint32_t i = 0; i < n; ++i) {
+            if (child_count) child_count[i] = 0;
+            if (is_parent) is_parent[i] = 1;
+            if (parent_node) parent_node[i] = i;
+        }
+    }
+    return GGA_OK;
+}
+
+gga_status dev_child_index(gga_graph *g, uint32_t *count, uint32_t *cidx, uint32_t *ccnt, cudaStream_t st) {
+    DevGraph *d = (DevGraph *)g->dev;
+    uint32_t np = d->level ? d->npar : 0;
+    if (*count < np || (np && (!cidx || !ccnt))) {
+        *count = np;
+        return gga_fail(GGA_ERR_INVALID_ARG, "child index needs capacity %u", np);
+    }
+    *count = np;
+    if (np) {
+        GGA_CK(cudaMemcpyAsync(cidx, d->cidx, (size_t)np * 4, cudaMemcpyDeviceToHost, st));
+        GGA_CK(cudaMemcpyAsync(ccnt, d->ccnt, (size_t)np * 4, cudaMemcpyDeviceToHost, st));
+        GGA_CK(cudaStreamSynchronize(st));
+    }
+    return GGA_OK;
+}

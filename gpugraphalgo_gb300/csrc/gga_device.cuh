@@ -1,0 +1,175 @@
+/*
+ * Device-side declarations shared by the CUDA translation units.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gga_internal.h"
+
+#define GGA_CK(call)                                                                       \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return gga_fail(GGA_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,       \
+                            cudaGetErrorString(e_));                                       \
+    } while (0)
+
+/* Device-resident graph (one per gga_graph).  The unsplit CSR is 0-based;
+ * the split view is the reference's NodeSplit result re-based to 0
+ * (s_off[k] = psrc[k] - 1 for k < ns). */
+struct DevGraph {
+    int device;
+    uint32_t n, m;
+    uint32_t *off; /* n+1 */
+    uint32_t *col; /* m */
+    uint32_t *wt;  /* m */
+    uint32_t maxdeg;
+
+    /* node split (graph.h:415-522) */
+    int32_t level, buckets;
+    uint32_t ns, mda, npar;
+    uint32_t *s_off;   /* ns+1, s_off[ns] = m */
+    uint32_t *s_col;   /* m, targets remapped to the parent's split id */
+    uint32_t *s_cc;    /* ns, childCount (at parents) */
+    uint32_t *s_isp;   /* ns, IsParent */
+    uint32_t *s_par;   /* ns, parentNode (original id) */
+    uint32_t *first;   /* n+1, split id of each original vertex's parent */
+    uint32_t *cidx;    /* npar, myChildIndex */
+    uint32_t *ccnt;    /* npar, myChildCount */
+};
+
+/* The graph a relaxation engine walks: either the unsplit CSR or the split one. */
+struct GraphView {
+    const uint32_t *off;
+    const uint32_t *col;
+    const uint32_t *wt;
+    const uint32_t *cc; /* child counts (split view) or nullptr */
+    uint32_t n;
+    uint32_t m;
+};
+
+/* Error codes written by kernels into their control blocks. */
+enum : uint32_t {
+    GGA_DEV_OK = 0,
+    GGA_DEV_TIMEOUT = 1,
+    GGA_DEV_OVERFLOW = 2,
+    GGA_DEV_SPLIT_RULE = 3
+};
+
+/* ---- small device helpers ---------------------------------------------- */
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t global_timer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+/* Bounded grid barrier for persistent cooperative launches.  Sense is a
+ * generation counter; a block that waits longer than timeout_ns (or sees the
+ * error word set) records GGA_DEV_TIMEOUT and returns false instead of
+ * spinning on.  Every block must call it the same number of times. */
+struct GridBarrier {
+    uint32_t count;
+    uint32_t gen;
+};
+
+__device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err, uint32_t nblocks,
+                                             uint32_t &gen_local, uint64_t timeout_ns) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t g = gen_local;
+        __threadfence();
+        uint32_t prev = atomicAdd(&bar->count, 1u);
+        if (prev == nblocks - 1) {
+            bar->count = 0;
+            st_release_u32(&bar->gen, g + 1);
+        } else {
+            uint64_t t0 = global_timer_ns();
+            uint32_t spins = 0;
+            while (ld_acquire_u32(&bar->gen) == g) {
+                if ((++spins & 63u) == 0) {
+                    if (ld_relaxed_u32(err) != GGA_DEV_OK) break;
+                    if (global_timer_ns() - t0 > timeout_ns) {
+                        atomicCAS(err, GGA_DEV_OK, GGA_DEV_TIMEOUT);
+                        break;
+                    }
+                }
+                __nanosleep(20);
+            }
+        }
+        __threadfence();
+        gen_local = g + 1;
+    }
+    __syncthreads();
+    return ld_relaxed_u32(err) == GGA_DEV_OK;
+}
+
+/* Exclusive block scan of one uint32 per thread (blockDim.x a multiple of
+ * 32, <= 1024).  `warp_sums` needs 32 entries of shared memory.  Returns the
+ * exclusive prefix; *total receives the block sum. */
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t *warp_sums,
+                                                         uint32_t *total) {
+    const uint32_t lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t v = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= (uint32_t)d) v += y;
+    }
+    if (lane == 31) warp_sums[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t s = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, d);
+            if (lane >= (uint32_t)d) s += y;
+        }
+        if (lane < nw) warp_sums[lane] = s; /* inclusive over warps */
+    }
+    __syncthreads();
+    uint32_t base = wid ? warp_sums[wid - 1] : 0;
+    *total = warp_sums[nw - 1];
+    __syncthreads();
+    return base + v - x;
+}
+
+/* ---- host-side entry points implemented in the .cu files ----------------- */
+
+#ifdef __cplusplus
+extern "C++" {
+#endif
+/* device_graph.cu */
+gga_status dev_graph_ensure(gga_graph *g, int device, cudaStream_t st);
+DevGraph *dev_graph_of(gga_graph *g);
+gga_status dev_exclusive_scan(const uint32_t *in, uint32_t *out, uint32_t count, cudaStream_t st);
+GraphView dev_graph_view(const DevGraph *d, bool split);
+#ifdef __cplusplus
+}
+#endif

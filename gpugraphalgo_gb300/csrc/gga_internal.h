@@ -1,0 +1,65 @@
+/*
+ * Internal declarations shared by the host C code and the CUDA sources.
+ * Not part of the ABI.
+ */
+#ifndef GGA_INTERNAL_H
+#define GGA_INTERNAL_H
+
+#include <pthread.h>
+#include <stdint.h>
+
+#include "../../include/gga.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Vertex and edge limits: ids, offsets and counts are uint32 on the device. */
+#define GGA_MAX_NODES 0x80000000u
+#define GGA_MAX_EDGES 0xFFFFFFF0u
+
+/* Host-side graph.  The CSR is 0-based: vertex u owns edges
+ * [off[u], off[u+1]).  The reference keeps the same arrays 1-based with a null
+ * edge slot 0 (graph.h:251-254); the 1-based view is produced on export. */
+struct gga_graph {
+    uint32_t n;     /* original vertices */
+    uint32_t m;     /* directed edges */
+    uint32_t *off;  /* n+1 */
+    uint32_t *col;  /* m */
+    uint32_t *wt;   /* m */
+    uint32_t maxdeg;
+    uint32_t maxw;
+    int symmetric;
+
+    /* node split (graph.h:415-522); arrays live on the device */
+    int32_t split_level;
+    int32_t split_buckets;
+    uint32_t mda;
+    uint32_t ns;                    /* split vertex count n' */
+    uint32_t parents_with_children; /* myParentCount */
+
+    /* device residency, owned; see device_graph.cu */
+    void *dev;
+    int dev_device;
+    pthread_mutex_t lock;
+};
+
+/* Thread-local error message; returns `st` for tail calls. */
+gga_status gga_fail(gga_status st, const char *fmt, ...);
+void gga_clear_error(void);
+
+/* Allocates an empty graph with n vertices and m edges (arrays uninitialised). */
+gga_status gga_graph_alloc(uint32_t n, uint32_t m, gga_graph **out);
+/* Recomputes maxdeg / maxw from the CSR. */
+void gga_graph_refresh_stats(gga_graph *g);
+
+/* Device-state teardown hook set by device_graph.cu (NULL before first use). */
+extern void (*gga_dev_graph_release_hook)(gga_graph *g);
+
+/* Host wall clock in milliseconds. */
+double gga_now_ms(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

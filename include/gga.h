@@ -1,0 +1,299 @@
+/*
+ * gga.h — C ABI of the GB300-native static-graph BFS/SSSP engine.
+ *
+ * The reference (GPUGraphAlgo, Programs/CUDA_src/Kepler_BFS_SSSP/) exposes no
+ * library: its surface is the `Graph` struct (graph.h:23-64), its host methods,
+ * the relax kernels (cudaKernels.h) and the fixed-point loop in main()
+ * (bfs_sssp.cu:103-539).  Every entry point below names the reference item it
+ * replaces.  Conventions that differ from the reference on purpose:
+ *   - every call returns a gga_status; nothing calls exit() or abort()
+ *     (the reference exits in CudaTest, graph.h:523-533, and aborts on mmap
+ *     failure, graph.h:614,627);
+ *   - the caller owns output buffers; the library owns graph and device state;
+ *   - the source vertex is a parameter (the reference hard-codes original
+ *     vertex 0, bfs_sssp.cu:203);
+ *   - distance outputs hold one value per ORIGINAL vertex in original order,
+ *     which is exactly what Ary2File writes (parents only, myutils.h:51-62).
+ * Distances are uint32 with GGA_INFINITY (= MYINFINITY, bfs_sssp.cu:53) for
+ * unreachable vertices.  BFS distances are levels (every edge weight taken as 1).
+ *
+ * Threading: one gga_ctx per host thread; calls on different contexts may run
+ * concurrently.  A gga_graph may be shared by contexts on the same device.
+ */
+#ifndef GGA_H
+#define GGA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GGA_INFINITY 1000000000u /* MYINFINITY, bfs_sssp.cu:53 / graph.h:96 */
+#define GGA_MSBFS_MAX_SOURCES 64 /* one uint64 lane word per vertex */
+#define GGA_SSSP_BATCH_MAX_SOURCES 32 /* one warp lane per source */
+/* Largest edge weight for which dist + weight cannot wrap in uint32 while
+ * dist <= GGA_INFINITY; heavier weights are rejected (the reference's unsigned
+ * arithmetic would wrap, bfs_sssp.cu/cudaKernels.h:323). */
+#define GGA_MAX_WEIGHT (0xFFFFFFFFu - GGA_INFINITY)
+
+typedef enum gga_status {
+    GGA_OK = 0,
+    GGA_ERR_INVALID_ARG = 1, /* bad pointer, size or enum */
+    GGA_ERR_IO = 2,          /* open/read/write failed (readFromGR returns 1) */
+    GGA_ERR_FORMAT = 3,      /* malformed .gr (bad version, truncated, dst >= n) */
+    GGA_ERR_SPLIT_RULE = 4,  /* histogram rule gave MDA 0: the reference divides by zero */
+    GGA_ERR_NO_MEMORY = 5,   /* host allocation failed */
+    GGA_ERR_CUDA = 6,        /* a CUDA runtime call failed (message via gga_last_error) */
+    GGA_ERR_NO_DEVICE = 7,   /* no CUDA device / extension unusable */
+    GGA_ERR_TIMEOUT = 8,     /* a bounded device-side wait ran out; context stays usable */
+    GGA_ERR_ADMISSION = 9,   /* request exceeds the configured device-memory cap */
+    GGA_ERR_TOO_LARGE = 10,  /* graph exceeds the uint32 vertex/edge limits */
+    GGA_ERR_NOT_READY = 11,  /* serving ticket not finished yet */
+    GGA_ERR_UNSUPPORTED = 12
+} gga_status;
+
+typedef enum gga_algo { GGA_BFS = 0, GGA_SSSP = 1 } gga_algo;
+
+/* Relaxation engine.  All variants return identical distances. */
+typedef enum gga_variant {
+    GGA_VARIANT_AUTO = 0,        /* frontier engine with autotuned parameters */
+    GGA_VARIANT_FRONTIER = 1,    /* data-driven frontier, persistent kernel, CTA-cooperative expansion */
+    GGA_VARIANT_TOPO_ATOMIC = 2, /* "na_" build: M_my_drelax, cudaKernels.h:285-344 */
+    GGA_VARIANT_TOPO_PLAIN = 3,  /* "n_" build: my_updateDist + my_drelax_no_atomic, cudaKernels.h:129-220 */
+    GGA_VARIANT_CDP_ATOMIC = 4,  /* "da_" build: my_drelax_dynamicP, cudaKernels.h:438-520 (CDP2) */
+    GGA_VARIANT_CDP_PLAIN = 5    /* "d_" build: as da_ with plain stores */
+} gga_variant;
+
+typedef struct gga_graph gga_graph;
+typedef struct gga_ctx gga_ctx;
+
+/* Per-call statistics (the reference's SResult, graph.h:66-84, plus work counters). */
+typedef struct gga_stats {
+    uint32_t iterations;       /* fixed-point iterations / BFS levels / near-far rounds */
+    uint32_t kernel_launches;  /* kernels this call launched from the host */
+    uint64_t vertices_reached; /* original vertices with dist < GGA_INFINITY */
+    uint64_t edges_reached;    /* E_r: sum of out-degrees of reached original vertices */
+    uint64_t edges_relaxed;    /* edge visits actually performed (work, >= E_r for SSSP) */
+    uint32_t cdp_children;     /* device-side launches made by CDP variants */
+    uint32_t cdp_fallbacks;    /* inline relaxations after a failed device launch */
+    double kernel_ms;          /* device time of the relax kernels (ktime) by CUDA events */
+    double aux_ms;             /* child-distance update time (sktime) */
+    double total_ms;           /* whole call, host wall clock, copies included */
+} gga_stats;
+
+/* Read-only description of a graph and of its node split. */
+typedef struct gga_graph_info {
+    uint32_t nnodes;       /* vertices after split (== nodes_orig when not split) */
+    uint32_t nodes_orig;   /* vertices before split (nodes_b4_ns) */
+    uint32_t nedges;       /* directed edges (unchanged by the split) */
+    uint32_t maxdeg;       /* getMaxdeg of the unsplit graph */
+    int32_t split_level;   /* 0 = not split */
+    int32_t split_buckets; /* histogram buckets used when split_level < 0 */
+    uint32_t mda;          /* MAX_EDGES_ALLOWED of the split (0 when not split) */
+    uint32_t parents_with_children; /* myParentCount, bfs_sssp.cu:257-262 */
+    uint32_t max_weight;
+    int32_t symmetric;     /* 1 generated symmetric, 0 unknown */
+} gga_graph_info;
+
+/* ---- errors ----------------------------------------------------------- */
+const char *gga_status_string(gga_status s);
+/* Message of the last failing call on this host thread (never NULL). */
+const char *gga_last_error(void);
+/* Library version string. */
+const char *gga_version(void);
+
+/* ---- host graph (graph.h: struct Graph, L0) ----------------------------- */
+
+/* Graph::readFromGR, graph.h:599-682.  Galois .gr v1: u64 header
+ * {version=1, sizeEdgeTy, n, m}, u64 outIdx[n] (end offsets), u32 outs[m],
+ * 4-byte pad when m is odd, u32 edgeData[m] (always read as u32, as the
+ * reference does, graph.h:644,672). */
+gga_status gga_graph_load_gr(const char *path, gga_graph **out);
+/* Writes the same format with 4-byte weights. */
+gga_status gga_graph_save_gr(const gga_graph *g, const char *path);
+/* Builds a graph from a 0-based CSR: offsets[n+1], cols[m], weights[m]
+ * (weights NULL = all 1).  Arrays are copied. */
+gga_status gga_graph_from_csr(uint32_t n, uint32_t m, const uint32_t *offsets,
+                              const uint32_t *cols, const uint32_t *weights,
+                              gga_graph **out);
+/* Seeded R-MAT (a, b, c; d = 1-a-b-c) with 2^scale vertices and
+ * edge_factor * 2^scale generated edges; symmetrised, self-loops and
+ * duplicates removed, vertex ids randomly permuted; weights uniform in
+ * [wmin, wmax], equal in both directions. */
+gga_status gga_graph_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b,
+                              double c, uint64_t seed, uint32_t wmin, uint32_t wmax,
+                              gga_graph **out);
+/* Seeded width x height 4-neighbour grid, row-major ids; each undirected grid
+ * edge deleted with probability del_prob; plus round(longrange_frac * grid
+ * edges) random undirected long-range edges; weights uniform in [wmin, wmax]. */
+gga_status gga_graph_gen_grid(uint32_t width, uint32_t height, double del_prob,
+                              double longrange_frac, uint64_t seed, uint32_t wmin,
+                              uint32_t wmax, gga_graph **out);
+void gga_graph_free(gga_graph *g);
+gga_status gga_graph_get_info(const gga_graph *g, gga_graph_info *info);
+/* Borrowed pointers to the unsplit 0-based host CSR (valid until free). */
+gga_status gga_graph_csr(const gga_graph *g, const uint32_t **offsets, const uint32_t **cols,
+                         const uint32_t **weights);
+
+/* ---- node split (graph.h L1) --------------------------------------------- */
+
+/* Graph::getMaxdeg, graph.h:338-347. */
+gga_status gga_max_degree(const gga_graph *g, uint32_t *maxdeg);
+/* Graph::getMaxAllowedOutDegree, graph.h:359-385 (degree histogram rule). */
+gga_status gga_max_allowed_out_degree(const gga_graph *g, int32_t buckets, uint32_t *mda);
+/* Graph::getSizeafterLoadBalance, graph.h:386-414: MDA and the split vertex
+ * count for `level` (>0: ceil(maxdeg/level); <0: histogram rule). */
+gga_status gga_size_after_split(const gga_graph *g, int32_t level, int32_t buckets,
+                                uint32_t *mda, uint32_t *new_nnodes);
+/* Graph::NodeSplit, graph.h:415-522, built by device kernels on ctx's GPU.
+ * level 0 removes any split.  Returns GGA_ERR_SPLIT_RULE where the reference
+ * would divide by zero.  The split graph stays resident on the device. */
+gga_status gga_node_split(gga_ctx *ctx, gga_graph *g, int32_t level, int32_t buckets);
+/* Copies the split graph out in the reference's own layout (1-based psrc with
+ * psrc[n'] = nedges, graph.h:498; edgessrcdst[0] null slot).  Any pointer may
+ * be NULL.  Sizes: psrc n'+1, noutgoing/child_count/is_parent/parent_node n',
+ * edgessrcdst m+1. */
+gga_status gga_graph_split_maps(gga_ctx *ctx, const gga_graph *g, uint32_t *psrc,
+                                uint32_t *noutgoing, uint32_t *edgessrcdst,
+                                uint32_t *child_count, uint32_t *is_parent,
+                                uint32_t *parent_node);
+/* myChildIndex / myChildCount, bfs_sssp.cu:256-283: parents that have
+ * children (ascending split id) and their child counts.  `count` in/out:
+ * capacity in, number of parents out. */
+gga_status gga_child_index(gga_ctx *ctx, const gga_graph *g, uint32_t *count,
+                           uint32_t *child_index, uint32_t *child_count);
+
+/* ---- device context (graph.h L2) ---------------------------------------- */
+
+gga_status gga_ctx_create(int device, gga_ctx **out);
+void gga_ctx_destroy(gga_ctx *ctx);
+/* Graph::cudaCopy, graph.h:683-699: uploads g (done lazily by the solvers). */
+gga_status gga_graph_upload(gga_ctx *ctx, gga_graph *g);
+/* Number of SMs and device name of ctx's GPU. */
+gga_status gga_ctx_device_info(gga_ctx *ctx, int *sm_count, char *name, size_t name_len);
+/* CUDA-event timing on ctx's stream (the stream every solve launches on):
+ * gga_ctx_mark records event `slot` (0..7); gga_ctx_elapsed waits for slot b
+ * and returns the milliseconds between slots a and b. */
+gga_status gga_ctx_mark(gga_ctx *ctx, int slot);
+gga_status gga_ctx_elapsed(gga_ctx *ctx, int a, int b, double *ms);
+gga_status gga_ctx_synchronize(gga_ctx *ctx);
+/* Page-locks (pin != 0) or unlocks the host CSR so uploads run at full
+ * host-to-device bandwidth. */
+gga_status gga_graph_pin(gga_graph *g, int pin);
+/* Drops the device copy (and split); the next solve uploads again. */
+gga_status gga_graph_release_device(gga_graph *g);
+
+/* ---- single-source solve (bfs_sssp.cu:372-468 loop, L3/L4) -------------- */
+
+/* dist_out: host or device buffer of nodes_orig uint32, or NULL to leave the
+ * result in the context's device buffer (until its next solve).  stats may
+ * be NULL. */
+gga_status gga_bfs(gga_ctx *ctx, gga_graph *g, uint32_t src, gga_variant variant,
+                   uint32_t *dist_out, gga_stats *stats);
+gga_status gga_sssp(gga_ctx *ctx, gga_graph *g, uint32_t src, gga_variant variant,
+                    uint32_t *dist_out, gga_stats *stats);
+gga_status gga_solve(gga_ctx *ctx, gga_graph *g, gga_algo algo, uint32_t src,
+                     gga_variant variant, uint32_t *dist_out, gga_stats *stats);
+
+/* Frontier-engine parameters (picked by gga_autotune when not set). */
+typedef struct gga_params {
+    uint32_t block_threads;  /* CTA size: 256, 512 or 1024 */
+    uint32_t huge_degree;    /* vertices above this are expanded by the whole grid */
+    uint32_t sssp_delta;     /* near-far bucket width (0 = plain improved-vertex frontier) */
+    uint32_t use_split;      /* expand over the node-split graph when one exists */
+    uint32_t blocks_per_sm;  /* persistent grid = SMs x this (0 = occupancy maximum) */
+    /* CDP variants: heavy-vertex threshold as bfs_sssp.cu:224-236 derives it
+     * (level > 0: ceil(maxdeg/level); level < 0: histogram rule with buckets) */
+    int32_t cdp_level;
+    int32_t cdp_buckets;
+    /* 0: one CDP2 tail launch per iteration over all heavy vertices;
+     * 1: one fire-and-forget <<<1,32>>> child per heavy vertex (the
+     *    reference's dynamicP_relax_coal shape); 2: no device launches */
+    uint32_t cdp_mode;
+    uint32_t cdp_pending_limit; /* cudaLimitDevRuntimePendingLaunchCount to set (0 = leave) */
+    uint32_t skip_reached;      /* 1: gga_stats leaves vertices/edges_reached 0 (saves one launch) */
+} gga_params;
+/* p = NULL returns to the per-graph defaults. */
+gga_status gga_set_params(gga_ctx *ctx, const gga_params *p);
+gga_status gga_get_params(gga_ctx *ctx, gga_params *p);
+/* Picks parameters for g from its degree profile (and short timed trials when
+ * trials > 0) and stores them in ctx. */
+gga_status gga_autotune(gga_ctx *ctx, gga_graph *g, uint32_t trials, gga_params *chosen);
+
+/* ---- verification and output (myutils.h, L5) ---------------------------- */
+
+/* verifysolution, myutils.h:1-18: number of edges with wt>0 and
+ * dist[u]+wt < dist[v] (weights taken as 1 for BFS), on the split graph when
+ * g is split.  dist: host array of nodes_orig entries. */
+gga_status gga_verify(const gga_graph *g, gga_algo algo, const uint32_t *dist, uint64_t *nerr);
+/* Ary2File, myutils.h:51-62: one "%u\n" line per original vertex. */
+gga_status gga_write_dist(const char *path, const gga_graph *g, const uint32_t *dist);
+/* E_r and V_r for a distance vector (host array of nodes_orig entries). */
+gga_status gga_reached(const gga_graph *g, const uint32_t *dist, uint64_t *vertices_reached,
+                       uint64_t *edges_reached);
+
+/* The 17-column row writeResult appends to result.vi (myutils.h:86-113;
+ * fields = SResult, graph.h:66-84). */
+typedef struct gga_result_row {
+    char exename[100];
+    char algo[10];
+    char graphfile[200];
+    uint32_t bucket_size, nnode, nedge, ns_nnode, ns_nedge, extranode, maxdeg, splitlevel,
+        max_edges_allowed, iterations, runtime;
+    float time, ktime, sktime;
+} gga_result_row;
+gga_status gga_write_result_row(const char *path, const gga_result_row *row);
+
+/* ---- batched queries ---------------------------------------------------- */
+
+/* Bit-packed multi-source BFS: nsrc <= 64 sources in one traversal (one
+ * uint64 lane word per vertex).  dist_out: nsrc x nodes_orig, source-major. */
+gga_status gga_msbfs(gga_ctx *ctx, gga_graph *g, uint32_t nsrc, const uint32_t *srcs,
+                     uint32_t *dist_out, gga_stats *stats);
+/* Batched SSSP: nsrc <= 32 sources, one warp lane per source.
+ * dist_out: nsrc x nodes_orig, source-major. */
+gga_status gga_sssp_batch(gga_ctx *ctx, gga_graph *g, uint32_t nsrc, const uint32_t *srcs,
+                          uint32_t *dist_out, gga_stats *stats);
+
+/* One query of a multi-graph batch. */
+typedef struct gga_query {
+    gga_graph *graph;
+    uint32_t algo; /* gga_algo */
+    uint32_t src;
+    uint32_t *dist_out; /* host or device, nodes_orig entries */
+} gga_query;
+/* Runs nq queries over any mix of graphs in one persistent launch. */
+gga_status gga_multi_solve(gga_ctx *ctx, uint32_t nq, const gga_query *queries, gga_stats *stats);
+
+/* ---- serving ------------------------------------------------------------ */
+
+typedef struct gga_server gga_server;
+typedef struct gga_server_stats {
+    uint64_t submitted, completed, rejected;
+    uint32_t max_inflight;
+    uint32_t supersteps;
+    uint64_t state_bytes_peak; /* peak per-query device state admitted */
+} gga_server_stats;
+
+/* Starts a request loop over resident graphs; per-query device state
+ * (distances, frontiers) is admitted against mem_cap_bytes; at most
+ * max_slots queries share the device at once. */
+gga_status gga_server_create(gga_ctx *ctx, uint32_t ngraphs, gga_graph *const *graphs,
+                             uint64_t mem_cap_bytes, uint32_t max_slots, gga_server **out);
+/* Queues a query; returns at once with a ticket.  dist_out (host) must stay
+ * valid until the ticket completes. */
+gga_status gga_server_submit(gga_server *s, uint32_t graph_index, gga_algo algo, uint32_t src,
+                             uint32_t *dist_out, uint64_t *ticket);
+/* Waits up to timeout_ms (0 = poll) for a ticket; latency_us = completion -
+ * submission.  GGA_ERR_NOT_READY if still running. */
+gga_status gga_server_wait(gga_server *s, uint64_t ticket, uint32_t timeout_ms,
+                           double *latency_us);
+gga_status gga_server_get_stats(gga_server *s, gga_server_stats *st);
+void gga_server_destroy(gga_server *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GGA_H */

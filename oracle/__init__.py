@@ -1,0 +1,201 @@
+"""ORACLE — test infrastructure, not product code.
+
+ctypes binding of ``oracle/liboracle.so`` (the C restatement of the
+reference's host algorithms in ``gga_oracle.c``) and a runner for the
+reference's own host code built into ``oracle/_ref/`` (development host only).
+Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package, always as the checker or the CPU baseline,
+never as part of the GPU path being measured.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+INF = 1000000000
+
+_lib = None
+
+
+def build(quiet: bool = True) -> None:
+    """Compiles liboracle.so (gcc only); the reference build is `make ref`."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    lib = C.CDLL(LIB_PATH)
+    P, U = C.c_void_p, C.c_uint32
+    lib.oracle_load_gr.restype = P
+    lib.oracle_load_gr.argtypes = [C.c_char_p]
+    lib.oracle_from_csr.restype = P
+    lib.oracle_from_csr.argtypes = [U, U, P, P, P]
+    lib.oracle_free.argtypes = [P]
+    lib.oracle_dims.argtypes = [P, P, P, P, P]
+    lib.oracle_arrays.argtypes = [P] * 8
+    lib.oracle_max_degree.restype = U
+    lib.oracle_max_degree.argtypes = [P]
+    lib.oracle_max_allowed_out_degree.restype = U
+    lib.oracle_max_allowed_out_degree.argtypes = [P, C.c_int]
+    lib.oracle_size_after_split.restype = C.c_int
+    lib.oracle_size_after_split.argtypes = [P, C.c_int, C.c_int, P, P]
+    lib.oracle_node_split.restype = C.c_int
+    lib.oracle_node_split.argtypes = [P, C.c_int, C.c_int]
+    lib.oracle_child_index.restype = U
+    lib.oracle_child_index.argtypes = [P, P, P]
+    lib.oracle_serial.restype = U
+    lib.oracle_serial.argtypes = [P, C.c_int, U, P]
+    lib.oracle_init_dist.argtypes = [P, U, P]
+    lib.oracle_verify.restype = C.c_uint64
+    lib.oracle_verify.argtypes = [P, C.c_int, P]
+    lib.oracle_ary2file.restype = C.c_int
+    lib.oracle_ary2file.argtypes = [C.c_char_p, P, P, U]
+    _lib = lib
+    return lib
+
+
+def _p(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+class OracleGraph:
+    """The reference's struct Graph, restated (1-based psrc layout)."""
+
+    def __init__(self, handle):
+        if not handle:
+            raise RuntimeError("oracle: could not load graph")
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def from_csr(cls, off, col, wt):
+        off = np.ascontiguousarray(off, np.uint32)
+        col = np.ascontiguousarray(col, np.uint32)
+        wt = np.ascontiguousarray(wt, np.uint32)
+        if len(col) == 0:
+            col = np.zeros(1, np.uint32)
+            wt = np.zeros(1, np.uint32)
+            m = 0
+        else:
+            m = len(col)
+        return cls(load().oracle_from_csr(len(off) - 1, m, _p(off), _p(col), _p(wt)))
+
+    @classmethod
+    def load_gr(cls, path: str):
+        return cls(load().oracle_load_gr(path.encode()))
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().oracle_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def dims(self):
+        n, m, nb, mda = (C.c_uint32() for _ in range(4))
+        load().oracle_dims(self._h, C.byref(n), C.byref(m), C.byref(nb), C.byref(mda))
+        return {"nnodes": n.value, "nedges": m.value, "nodes_b4_ns": nb.value, "mda": mda.value}
+
+    def arrays(self) -> dict:
+        d = self.dims()
+        n, m = d["nnodes"], d["nedges"]
+        out = {
+            "psrc": np.zeros(n + 1, np.uint32),
+            "noutgoing": np.zeros(max(n, 1), np.uint32),
+            "edgessrcdst": np.zeros(m + 1, np.uint32),
+            "edgessrcwt": np.zeros(m + 1, np.uint32),
+            "childCount": np.zeros(max(n, 1), np.uint32),
+            "IsParent": np.zeros(max(n, 1), np.uint32),
+            "parentNode": np.zeros(max(n, 1), np.uint32),
+        }
+        load().oracle_arrays(self._h, *[_p(out[k]) for k in
+                                        ("psrc", "noutgoing", "edgessrcdst", "edgessrcwt", "childCount", "IsParent", "parentNode")])
+        for k in ("noutgoing", "childCount", "IsParent", "parentNode"):
+            out[k] = out[k][:n]
+        return out
+
+    def max_degree(self) -> int:
+        return load().oracle_max_degree(self._h)
+
+    def max_allowed_out_degree(self, buckets: int) -> int:
+        return load().oracle_max_allowed_out_degree(self._h, buckets)
+
+    def size_after_split(self, level: int, buckets: int):
+        mda, cnt = C.c_uint32(), C.c_uint32()
+        rc = load().oracle_size_after_split(self._h, level, buckets, C.byref(mda), C.byref(cnt))
+        return rc, mda.value, cnt.value
+
+    def node_split(self, level: int, buckets: int = 10) -> int:
+        return load().oracle_node_split(self._h, level, buckets)
+
+    def child_index(self):
+        n = self.dims()["nnodes"]
+        idx = np.zeros(max(n, 1), np.uint32)
+        cnt = np.zeros(max(n, 1), np.uint32)
+        p = load().oracle_child_index(self._h, _p(idx), _p(cnt))
+        return idx[:p], cnt[:p]
+
+    def serial(self, algo: str, src: int):
+        """findSerialBFS / findSerialSSSP: (dist, passes)."""
+        n = self.dims()["nnodes"]
+        d = np.zeros(n, np.uint32)
+        passes = load().oracle_serial(self._h, 1 if algo == "sssp" else 0, src, _p(d))
+        return d, passes
+
+    def init_dist(self, parent_src: int):
+        n = self.dims()["nnodes"]
+        d = np.zeros(n, np.uint32)
+        load().oracle_init_dist(self._h, parent_src, _p(d))
+        return d
+
+    def verify(self, algo: str, dist_split) -> int:
+        d = np.ascontiguousarray(dist_split, np.uint32)
+        return int(load().oracle_verify(self._h, 1 if algo == "sssp" else 0, _p(d)))
+
+
+def serial_distances(off, col, wt, algo: str, src: int) -> np.ndarray:
+    """Oracle BFS levels / SSSP distances on the unsplit graph."""
+    return OracleGraph.from_csr(off, col, wt).serial(algo, src)[0]
+
+
+# ---------------------------------------------------------------- reference build
+
+def ref_available() -> bool:
+    return all(os.path.exists(os.path.join(REF_DIR, f"ref_{a}")) for a in ("bfs", "sssp"))
+
+
+def run_reference(gr_path: str, algo: str, level: int, buckets: int, src: int, workdir: str | None = None) -> dict:
+    """Runs oracle/_ref/ref_<algo> (the reference's own host code) and reads
+    its dumps.  Returns {"returncode", "stdout", arrays..., meta...}."""
+    exe = os.path.join(REF_DIR, f"ref_{algo}")
+    own = workdir is None
+    wd = workdir or tempfile.mkdtemp(prefix="gga_ref_")
+    prefix = os.path.join(wd, "out")
+    p = subprocess.run([exe, gr_path, str(level), str(buckets), str(src), prefix], capture_output=True, text=True)
+    res = {"returncode": p.returncode, "stdout": p.stdout}
+    if p.returncode == 0:
+        for k in ("dist", "psrc", "noutgoing", "edgessrcdst", "childCount", "IsParent", "parentNode"):
+            res[k] = np.fromfile(f"{prefix}.{k}.u32", dtype="<u4")
+        with open(f"{prefix}.ary.txt") as f:
+            res["ary_txt"] = f.read()
+        for line in open(f"{prefix}.meta"):
+            k, v = line.strip().split("=", 1)
+            res[k] = v if k == "algo" else int(v)
+        for line in p.stdout.splitlines():
+            if "no of errors" in line:
+                res["nerr"] = int(line.split("=")[1].strip().rstrip("."))
+    if own:
+        subprocess.run(["rm", "-rf", wd])
+    return res

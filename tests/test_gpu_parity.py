@@ -1,0 +1,241 @@
+"""GPU parity: every engine and split configuration against the reference's
+recorded outputs (tests/golden) and the oracle, bit for bit.
+
+Integer distances are unique, so all variants must agree exactly: BFS levels
+and SSSP distances of the reference's serial code (graph.h:115-184), the
+split arrays of NodeSplit (graph.h:415-522) and zero verifysolution errors
+(myutils.h:1-18)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import gpugraphalgo_gb300 as gga
+import oracle
+from conftest import build_golden_graph
+from _util import digest
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = ["frontier", "topo_atomic", "topo_plain", "cdp_atomic", "cdp_plain"]
+
+
+def _golden_items(golden):
+    meta, arrays = golden
+    for name, e in sorted(meta["graphs"].items()):
+        yield name, e, arrays
+
+
+def test_unsplit_all_variants_match_reference(golden, ctx):
+    for name, e, arrays in _golden_items(golden):
+        g = build_golden_graph(name, e, arrays)
+        for key, rec in e["dist"].items():
+            algo, src = key.split("/")
+            want = arrays[f"{name}/dist/{key}"]
+            for v in VARIANTS:
+                got = ctx.solve(g, algo, int(src), v)
+                assert digest(got) == rec["sha256"], (name, key, v, np.nonzero(got != want)[0][:5])
+            assert g.verifysolution(got, algo) == 0
+
+
+def test_device_split_matches_reference(golden, ctx):
+    for name, e, arrays in _golden_items(golden):
+        g = build_golden_graph(name, e, arrays)
+        for key, rec in e["split"].items():
+            level, buckets = map(int, key.split("/"))
+            if rec.get("crash"):
+                with pytest.raises(gga.GGAError) as ex:
+                    g.NodeSplit(ctx, level, buckets)
+                assert ex.value.status == gga.ERR_SPLIT_RULE, (name, key)
+                assert g.info()["split_level"] == 0
+                continue
+            g.NodeSplit(ctx, level, buckets)
+            info = g.info()
+            assert (info["mda"], info["nnodes"]) == (rec["mda"], rec["nnodes"]), (name, key)
+            maps = g.split_maps(ctx)
+            for k in ("psrc", "noutgoing", "childCount", "IsParent", "parentNode"):
+                assert digest(maps[k]) == rec[f"{k}_sha256"], (name, key, k)
+            assert digest(maps["edgessrcdst"][1:]) == rec["edgessrcdst_sha256"], (name, key)
+            idx, cnt = g.child_index(ctx)
+            np.testing.assert_array_equal(idx, np.nonzero(maps["childCount"])[0])
+            np.testing.assert_array_equal(cnt, maps["childCount"][idx])
+            assert info["parents_with_children"] == len(idx)
+        g.NodeSplit(ctx, 0)
+        assert g.info()["split_level"] == 0
+
+
+def test_split_graph_all_variants_match_reference(golden, ctx):
+    for name, e, arrays in _golden_items(golden):
+        g = build_golden_graph(name, e, arrays)
+        for key, rec in e["split"].items():
+            if rec.get("crash"):
+                continue
+            level, buckets = map(int, key.split("/"))
+            g.NodeSplit(ctx, level, buckets)
+            for dkey, drec in e["dist"].items():
+                algo, src = dkey.split("/")
+                for v in ("frontier", "topo_atomic", "topo_plain"):
+                    got = ctx.solve(g, algo, int(src), v)
+                    assert digest(got) == drec["sha256"], (name, key, dkey, v)
+        g.NodeSplit(ctx, 0)
+
+
+@pytest.mark.parametrize("bs", [256, 512, 1024])
+@pytest.mark.parametrize("huge", [1, 7, 4096])
+@pytest.mark.parametrize("delta", [0, 1, 37, 100000])
+def test_frontier_parameters_do_not_change_answers(golden, ctx, bs, huge, delta):
+    meta, arrays = golden
+    name = "c1_rmat14"
+    e = meta["graphs"][name]
+    g = build_golden_graph(name, e, arrays)
+    ctx.set_params(block_threads=bs, huge_degree=huge, sssp_delta=delta, use_split=1)
+    try:
+        for key, rec in e["dist"].items():
+            algo, src = key.split("/")
+            assert digest(ctx.solve(g, algo, int(src), "frontier")) == rec["sha256"], key
+        g.NodeSplit(ctx, -1, 10)
+        for key, rec in e["dist"].items():
+            algo, src = key.split("/")
+            assert digest(ctx.solve(g, algo, int(src), "frontier")) == rec["sha256"], key
+        g.NodeSplit(ctx, 0)
+    finally:
+        ctx.reset_params()
+
+
+def _oracle_dist(g, algo, src):
+    return oracle.serial_distances(*g.csr(), algo, src)
+
+
+@pytest.mark.parametrize("seed", [21, 22])
+def test_random_rmat_against_oracle(ctx, seed):
+    g = gga.Graph.rmat(16, 16, seed=seed)
+    deg = g.degrees()
+    rng = np.random.default_rng(seed)
+    srcs = [int(np.argmax(deg)), int(rng.integers(g.n))]
+    for algo in ("bfs", "sssp"):
+        for s in srcs:
+            want = _oracle_dist(g, algo, s)
+            for v in ("frontier", "topo_atomic"):
+                np.testing.assert_array_equal(ctx.solve(g, algo, s, v), want)
+    g.NodeSplit(ctx, -1, 10)
+    for algo in ("bfs", "sssp"):
+        want = _oracle_dist(g, algo, srcs[0])
+        for v in ("frontier", "topo_plain", "cdp_atomic"):
+            np.testing.assert_array_equal(ctx.solve(g, algo, srcs[0], v), want)
+
+
+def test_grid_deep_against_oracle(ctx):
+    g = gga.Graph.grid(256, 256, 0.05, 0.001, seed=3, wmin=1, wmax=1000)
+    for algo in ("bfs", "sssp"):
+        want = _oracle_dist(g, algo, 0)
+        got, st = ctx.solve(g, algo, 0, "frontier", stats=True)
+        np.testing.assert_array_equal(got, want)
+        assert st["iterations"] > 50
+
+
+def test_edge_cases(ctx):
+    # single vertex, no edges
+    g = gga.Graph.from_csr([0, 0], [])
+    assert ctx.bfs(g, 0).tolist() == [0]
+    # zero-degree source: everything else unreachable
+    g = gga.Graph.from_csr([0, 0, 1, 2], [2, 1], [5, 5])
+    for v in VARIANTS:
+        assert ctx.sssp(g, 0, v).tolist() == [0, gga.INFINITY, gga.INFINITY]
+    # self loops and parallel edges (allowed by from_csr)
+    off, col, wt = [0, 3, 4, 4], [0, 1, 1, 2], [4, 9, 2, 1]
+    g = gga.Graph.from_csr(off, col, wt)
+    for v in VARIANTS:
+        assert ctx.sssp(g, 0, v).tolist() == [0, 2, 3]
+        assert ctx.bfs(g, 0, v).tolist() == [0, 1, 2]
+    # directed (asymmetric) graph and zero weights
+    g = gga.Graph.from_csr([0, 2, 3, 3, 4], [1, 2, 3, 1], [0, 7, 0, 0])
+    for v in VARIANTS:
+        assert ctx.sssp(g, 0, v).tolist() == [0, 0, 7, 0]
+        assert ctx.bfs(g, 3, v).tolist() == [gga.INFINITY, 1, gga.INFINITY, 0]
+    # weight limit: the heaviest accepted weight cannot wrap; above MYINFINITY
+    # the target stays unreached, as the reference's compare leaves it
+    g = gga.Graph.from_csr([0, 1, 1], [1], [gga.MAX_WEIGHT])
+    for v in VARIANTS:
+        assert ctx.sssp(g, 0, v).tolist() == [0, gga.INFINITY]
+    g = gga.Graph.from_csr([0, 1, 1], [1], [gga.MAX_WEIGHT + 1])
+    with pytest.raises(gga.GGAError) as e:
+        ctx.sssp(g, 0)
+    assert e.value.status == gga.ERR_INVALID_ARG
+    assert ctx.bfs(g, 0).tolist() == [0, 1]
+    # bad source
+    with pytest.raises(gga.GGAError):
+        ctx.bfs(g, 5)
+
+
+def test_distances_above_infinity_stay_unreached(ctx):
+    """A path longer than MYINFINITY is not relaxed (alt < dist fails at 1e9),
+    exactly as the reference's unsigned compare behaves."""
+    w = [600000000, 600000000]
+    g = gga.Graph.from_csr([0, 1, 2, 2], [1, 2], w)
+    want = _oracle_dist(g, "sssp", 0)
+    assert want.tolist() == [0, 600000000, gga.INFINITY]
+    for v in VARIANTS:
+        np.testing.assert_array_equal(ctx.sssp(g, 0, v), want)
+
+
+def test_source_is_split_parent(golden, ctx):
+    meta, arrays = golden
+    e = meta["graphs"]["hub40_oddm"]
+    g = build_golden_graph("hub40_oddm", e, arrays)
+    g.NodeSplit(ctx, 7, 10)
+    assert g.split_maps(ctx)["childCount"][0] > 0  # vertex 0 (the hub) has children
+    for key, rec in e["dist"].items():
+        algo, src = key.split("/")
+        if src == "0":
+            for v in ("frontier", "topo_atomic", "topo_plain"):
+                assert digest(ctx.solve(g, algo, 0, v)) == rec["sha256"]
+
+
+def test_cdp_modes_and_fallback(ctx):
+    g = gga.Graph.rmat(14, 16, seed=5)
+    s = int(np.argmax(g.degrees()))
+    want = {a: _oracle_dist(g, a, s) for a in ("bfs", "sssp")}
+    try:
+        for mode in (0, 1, 2):
+            ctx.set_params(cdp_level=20, cdp_mode=mode)
+            for a in ("bfs", "sssp"):
+                for v in ("cdp_atomic", "cdp_plain"):
+                    got, st = ctx.solve(g, a, s, v, stats=True)
+                    np.testing.assert_array_equal(got, want[a])
+                    if mode == 2:
+                        assert st["cdp_children"] == 0
+                    else:
+                        assert st["cdp_children"] + st["cdp_fallbacks"] > 0
+        # the reference's shape with a tiny pending-launch budget: launches
+        # that do not fit fall back to inline relaxation (cudaKernels.h:483-512)
+        ctx.set_params(cdp_level=40, cdp_mode=1, cdp_pending_limit=4)
+        for a in ("bfs", "sssp"):
+            got, st = ctx.solve(g, a, s, "cdp_atomic", stats=True)
+            np.testing.assert_array_equal(got, want[a])
+    finally:
+        ctx.set_params(cdp_pending_limit=2048)
+        ctx.reset_params()
+
+
+def test_device_output_buffer(ctx):
+    torch = pytest.importorskip("torch")
+    g = gga.Graph.rmat(12, 8, seed=4)
+    want = ctx.bfs(g, 1)
+    out = torch.empty(g.n, dtype=torch.int32, device="cuda")
+    lib = gga.lib()
+    import ctypes
+
+    s = gga._native.Stats()
+    rc = lib.gga_solve(ctx.handle, g.handle, gga.BFS, 1, 1, ctypes.c_void_p(out.data_ptr()), ctypes.byref(s))
+    assert rc == 0
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), want)
+
+
+def test_stats_report_reached(ctx):
+    g = gga.Graph.rmat(14, 8, seed=1)
+    d, st = ctx.bfs(g, 0, stats=True)
+    vr, er = g.reached(d)
+    assert st["vertices_reached"] == vr and st["edges_reached"] == er
+    assert st["edges_relaxed"] == er  # BFS expands each reached vertex once
+    assert st["kernel_ms"] > 0 and st["kernel_launches"] >= 1
