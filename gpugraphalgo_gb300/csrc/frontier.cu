@@ -40,7 +40,7 @@ struct Args {
     const uint32_t *first; /* split view: original -> parent split id */
     uint32_t n;
     uint32_t *dist, *bits, *farbits, *stamp;
-    uint32_t *q0, *q1, *hq0, *hq1, *hqb0, *hqb1, *far0, *far1;
+    uint32_t *q0, *q1, *hq0, *hq1, *hqb0, *hqb1, *far0, *far1, *far2;
     FrontierCtl *ctl;
     uint32_t cap, hcap;
     uint32_t src;
@@ -51,6 +51,9 @@ struct Args {
 };
 
 __device__ __forceinline__ uint32_t *sel(uint32_t p, uint32_t *a, uint32_t *b) { return p ? b : a; }
+__device__ __forceinline__ uint32_t *sel3(uint32_t p, uint32_t *a, uint32_t *b, uint32_t *c) {
+    return p == 0 ? a : (p == 1 ? b : c);
+}
 
 __device__ __forceinline__ void set_err(FrontierCtl *c, uint32_t code) { atomicCAS(&c->err, GGA_DEV_OK, code); }
 
@@ -113,7 +116,7 @@ __device__ __forceinline__ void push_far(const Args &a, uint32_t v, bool want, u
     base = __shfl_sync(FULL, base, leader);
     if (want) {
         const uint32_t idx = base + __popc(mask & lanemask_lt());
-        if (idx < a.cap) sel(fp, a.far0, a.far1)[idx] = v;
+        if (idx < a.cap) sel3(fp, a.far0, a.far1, a.far2)[idx] = v;
         else set_err(a.ctl, GGA_DEV_OVERFLOW);
     }
 }
@@ -193,6 +196,7 @@ __global__ void __launch_bounds__(BS) k_frontier(Args a) {
     if (blockIdx.x == 0 && tid == 0) {
         ctl->far_min[0] = NONE;
         ctl->far_min[1] = NONE;
+        ctl->far_min[2] = NONE;
     }
     if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) return;
 
@@ -214,6 +218,10 @@ __global__ void __launch_bounds__(BS) k_frontier(Args a) {
     uint32_t thr = SSSP ? (a.delta ? a.delta : NONE) : 0;
     uint32_t fp = 0;
     uint32_t round = 0;
+    /* Every decision below reads only counters that no block writes during
+     * the current round: the round's input queue (pushes go to the next
+     * slot) and, when that queue is empty, the far pile (nothing relaxes).
+     * So all blocks take the same branch and meet the same barriers. */
     for (;; ++round) {
         const uint32_t r3 = round % 3, r3n = (round + 1) % 3, cur = round & 1, nxt = cur ^ 1;
         /* an overflowing push sets the error word, so a queue past its
@@ -231,6 +239,51 @@ __global__ void __launch_bounds__(BS) k_frontier(Args a) {
             ctl->qcount[r3nn] = 0;
             ctl->work[r3nn] = 0;
             ctl->huge[r3nn] = 0;
+        }
+        if (units == 0) {
+            if (!SSSP) break;
+            const uint32_t fc = min(ld_relaxed_u32(&ctl->far_count[fp]), a.cap);
+            if (fc == 0) break;
+            /* ---- near queue drained: raise the threshold and split the far
+             * pile into the next round's near queue and the other pile */
+            const uint32_t fmin = ld_relaxed_u32(&ctl->far_min[fp]);
+            const uint32_t thr_old = thr;
+            const uint32_t lowest = max(thr, fmin);
+            thr = lowest > NONE - a.delta ? NONE : lowest + a.delta;
+            const uint32_t fq = fp == 2 ? 0 : fp + 1; /* pile that keeps the far items */
+            if (blockIdx.x == 0 && tid == 0) {
+                /* three piles rotate: the one after fq was read by the
+                 * previous far pass (a barrier ago) and is written by the
+                 * next one (a barrier ahead), so it can be cleared now */
+                const uint32_t dead = fq == 2 ? 0 : fq + 1;
+                ctl->far_count[dead] = 0;
+                ctl->far_min[dead] = NONE;
+                ctl->far_phases++;
+            }
+            const uint32_t *fin = sel3(fp, a.far0, a.far1, a.far2);
+            for (uint64_t base = (uint64_t)blockIdx.x * BS; base < fc; base += gthreads) {
+                const uint64_t i = base + tid;
+                bool to_near = false, keep = false;
+                uint32_t v = 0, d = NONE;
+                if (i < fc) {
+                    v = __ldcg(fin + i);
+                    d = __ldcg(a.dist + v);
+                    if (d >= thr) {
+                        keep = true;
+                    } else {
+                        atomicAnd(a.farbits + (v >> 5), ~(1u << (v & 31)));
+                        if (d >= thr_old) to_near = atomicExch(a.stamp + v, round + 1) != round + 1;
+                    }
+                }
+                push_near(a, v, to_near, nxt, r3n);
+                const uint32_t kmin = __reduce_min_sync(FULL, keep ? d : NONE);
+                if (kmin != NONE && lane_id() == __ffs(__ballot_sync(FULL, keep && d == kmin)) - 1)
+                    atomicMin(&ctl->far_min[fq], kmin);
+                push_far(a, v, keep, fq);
+            }
+            if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+            fp = fq;
+            continue;
         }
         for (;;) {
             if (tid == 0) s_unit = atomicAdd(&ctl->work[r3], 1u);
@@ -283,7 +336,7 @@ __global__ void __launch_bounds__(BS) k_frontier(Args a) {
                     const uint32_t b = __ldg(a.off + v), d = __ldg(a.off + v + 1) - b;
                     const uint32_t start = (c - __ldcg(hqbin + lo)) * a.chunk_edges;
                     s_hstart = b + start;
-                    s_hcnt = min(a.chunk_edges, d - start);
+                    s_hcnt = start < d ? min(a.chunk_edges, d - start) : 0u;
                     s_hdu = SSSP ? __ldcg(a.dist + v) : 0;
                 }
                 __syncthreads();
@@ -303,50 +356,9 @@ __global__ void __launch_bounds__(BS) k_frontier(Args a) {
             __syncthreads();
         }
         if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
-
-        const uint32_t nq2 = ld_relaxed_u32(&ctl->qcount[r3n]);
-        const unsigned long long hh2 = ld_relaxed_u64(&ctl->huge[r3n]);
-        if (nq2 != 0 || (hh2 >> 32) != 0) continue;
-        if (!SSSP) break;
-        const uint32_t fc = min(ld_relaxed_u32(&ctl->far_count[fp]), a.cap);
-        if (fc == 0) break;
-
-        /* ---- near queue drained: raise the threshold, split the far pile */
-        const uint32_t fmin = ld_relaxed_u32(&ctl->far_min[fp]);
-        const uint32_t thr_old = thr;
-        const uint32_t lowest = max(thr, fmin);
-        thr = lowest > NONE - a.delta ? NONE : lowest + a.delta;
-        const uint32_t *fin = sel(fp, a.far0, a.far1);
-        for (uint64_t base = (uint64_t)blockIdx.x * BS; base < fc; base += gthreads) {
-            const uint64_t i = base + tid;
-            bool to_near = false, keep = false;
-            uint32_t v = 0, d = NONE;
-            if (i < fc) {
-                v = __ldcg(fin + i);
-                d = __ldcg(a.dist + v);
-                if (d >= thr) {
-                    keep = true;
-                } else {
-                    atomicAnd(a.farbits + (v >> 5), ~(1u << (v & 31)));
-                    if (d >= thr_old) to_near = atomicExch(a.stamp + v, round + 1) != round + 1;
-                }
-            }
-            push_near(a, v, to_near, nxt, r3n);
-            const uint32_t kmin = __reduce_min_sync(FULL, keep ? d : NONE);
-            if (kmin != NONE && lane_id() == __ffs(__ballot_sync(FULL, keep && d == kmin)) - 1)
-                atomicMin(&ctl->far_min[fp ^ 1], kmin);
-            push_far(a, v, keep, fp ^ 1);
-        }
-        if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
-        if (blockIdx.x == 0 && tid == 0) {
-            ctl->far_count[fp] = 0;
-            ctl->far_min[fp] = NONE;
-            ctl->far_phases++;
-        }
-        fp ^= 1;
     }
     if (tid == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);
-    if (blockIdx.x == 0 && tid == 0) ctl->rounds = round + 1;
+    if (blockIdx.x == 0 && tid == 0) ctl->rounds = round;
 }
 
 template <int BS, bool SSSP>
@@ -382,7 +394,7 @@ static gga_status alloc_u32(uint32_t **p, size_t n) {
 void frontier_scratch_free(FrontierScratch *s) {
     cudaFree(s->dist); cudaFree(s->bits); cudaFree(s->farbits); cudaFree(s->stamp);
     cudaFree(s->q0); cudaFree(s->q1); cudaFree(s->hq0); cudaFree(s->hq1);
-    cudaFree(s->hqb0); cudaFree(s->hqb1); cudaFree(s->far0); cudaFree(s->far1);
+    cudaFree(s->hqb0); cudaFree(s->hqb1); cudaFree(s->far0); cudaFree(s->far1); cudaFree(s->far2);
     cudaFree(s->out); cudaFree(s->ctl);
     memset(s, 0, sizeof *s);
 }
@@ -398,7 +410,8 @@ gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m) {
         (st = alloc_u32(&s->farbits, words)) || (st = alloc_u32(&s->stamp, cap)) ||
         (st = alloc_u32(&s->q0, cap)) || (st = alloc_u32(&s->q1, cap)) || (st = alloc_u32(&s->hq0, cap)) ||
         (st = alloc_u32(&s->hq1, cap)) || (st = alloc_u32(&s->hqb0, cap)) || (st = alloc_u32(&s->hqb1, cap)) ||
-        (st = alloc_u32(&s->far0, cap)) || (st = alloc_u32(&s->far1, cap)) || (st = alloc_u32(&s->out, cap))) {
+        (st = alloc_u32(&s->far0, cap)) || (st = alloc_u32(&s->far1, cap)) || (st = alloc_u32(&s->far2, cap)) ||
+        (st = alloc_u32(&s->out, cap))) {
         frontier_scratch_free(s);
         return st;
     }
@@ -422,7 +435,7 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     a.n = view.n;
     a.dist = s->dist; a.bits = s->bits; a.farbits = s->farbits; a.stamp = s->stamp;
     a.q0 = s->q0; a.q1 = s->q1; a.hq0 = s->hq0; a.hq1 = s->hq1; a.hqb0 = s->hqb0; a.hqb1 = s->hqb1;
-    a.far0 = s->far0; a.far1 = s->far1;
+    a.far0 = s->far0; a.far1 = s->far1; a.far2 = s->far2;
     a.ctl = s->ctl;
     a.cap = s->cap;
     a.hcap = s->hcap;

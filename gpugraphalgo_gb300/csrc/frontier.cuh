@@ -12,8 +12,8 @@ struct FrontierCtl {
     uint32_t qcount[3];           /* near-queue counts, rotating by round */
     uint32_t work[3];             /* work-unit tickets, rotating by round */
     unsigned long long huge[3];   /* (items << 32) | edge chunks, rotating */
-    uint32_t far_count[2];
-    uint32_t far_min[2];
+    uint32_t far_count[3];        /* three far piles rotate across far passes */
+    uint32_t far_min[3];
     uint32_t far_phases;
     uint32_t overflow_at;
     unsigned long long edges_relaxed;
@@ -30,7 +30,7 @@ struct FrontierScratch {
     uint32_t *stamp;     /* cap: SSSP last round a vertex was queued */
     uint32_t *q0, *q1;   /* near queues */
     uint32_t *hq0, *hq1, *hqb0, *hqb1; /* huge items and their first chunk */
-    uint32_t *far0, *far1;
+    uint32_t *far0, *far1, *far2;
     uint32_t *out;       /* cap: gathered original-order output */
     FrontierCtl *ctl;
 };
