@@ -58,7 +58,7 @@ class GraphInfo(C.Structure):
 class Params(C.Structure):
     _fields_ = [
         ("block_threads", u32),
-        ("huge_degree", u32),
+        ("unit_iters", u32),
         ("sssp_delta", u32),
         ("use_split", u32),
         ("blocks_per_sm", u32),

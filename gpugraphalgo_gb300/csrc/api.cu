@@ -200,7 +200,7 @@ gga_params ctx_default_params(const gga_graph *g) {
     gga_params p;
     memset(&p, 0, sizeof p);
     p.block_threads = 256;
-    p.huge_degree = 4096;
+    p.unit_iters = 4;
     uint64_t wsum = 0;
     const uint32_t stride = g->m > (1u << 20) ? g->m >> 20 : 1;
     uint32_t cnt = 0;
@@ -222,7 +222,7 @@ static gga_params effective_params(gga_ctx *c, const gga_graph *g) {
     if (!c->params_set) return d;
     gga_params p = c->params;
     if (!p.block_threads) p.block_threads = d.block_threads;
-    if (!p.huge_degree) p.huge_degree = d.huge_degree;
+    if (!p.unit_iters) p.unit_iters = d.unit_iters;
     if (!p.cdp_buckets) p.cdp_buckets = d.cdp_buckets;
     if (!p.cdp_level) p.cdp_level = d.cdp_level;
     return p;
@@ -280,7 +280,8 @@ gga_status ctx_finish_output(gga_ctx *c, const DevGraph *d, const uint32_t *dev_
         k_reached<<<ctx_grid(c, d->n, 256), 256, 0, c->st>>>(dev_out, d->off, d->n, acc);
         GGA_CK(cudaMemcpyAsync(c->hflag + 32, acc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
     }
-    GGA_CK(cudaStreamSynchronize(c->st));
+    gga_status w = dev_wait(c->st, 60.0);
+    if (w) return w;
     if (stats) {
         const unsigned long long *h = (const unsigned long long *)(c->hflag + 32);
         stats->vertices_reached = h[0];

@@ -20,6 +20,23 @@
 
 #include "gga_device.cuh"
 
+#include <time.h>
+#include <unistd.h>
+
+gga_status dev_wait(cudaStream_t st, double limit_s) {
+    const double t0 = gga_now_ms();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaSuccess) return GGA_OK;
+        if (e != cudaErrorNotReady) return gga_fail(GGA_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+        const double el = gga_now_ms() - t0;
+        if (el > limit_s * 1e3)
+            return gga_fail(GGA_ERR_TIMEOUT, "device work still running after %.0f s; end the process to free the GPU",
+                            limit_s);
+        if (el > 5.0) usleep(50);
+    }
+}
+
 /* ------------------------------------------------------------------ scan */
 
 static constexpr uint32_t SCAN_BS = 1024, SCAN_ITEMS = 4;

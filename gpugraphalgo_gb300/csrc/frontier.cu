@@ -8,45 +8,59 @@
  *   - the frontier is data driven: only vertices whose distance changed are
  *     expanded (BFS: level synchronous; SSSP: near-far buckets of width
  *     `delta`, or a plain improved-vertex frontier when delta = 0);
- *   - a CTA takes 256..1024 frontier vertices, scans their degrees and walks
- *     the concatenated edge lists with all its threads, so consecutive lanes
- *     read consecutive edges (coalesced) whatever the degree skew;
- *   - vertices above `huge_degree` are cut into fixed edge chunks that any
- *     CTA can take, so the 10^5-degree hubs of R-MAT do not serialise a CTA;
- *   - work units are handed out by an atomic ticket (dynamic balancing);
- *   - pushes are warp-aggregated (__ballot_sync/__popc, one atomic per warp)
- *     and deduplicated: BFS by a visited bitmap, SSSP by a per-vertex round
+ *   - expansion is EDGE balanced: every queued vertex carries the exclusive
+ *     offset of its edge range in the round's concatenated edge list, and
+ *     the list is cut into fixed units of U = block_threads * unit_iters
+ *     edges.  A CTA takes a unit by atomic ticket, loads the unit's queue
+ *     entries into shared memory and walks the unit with consecutive threads
+ *     on consecutive edges (coalesced), so a 10^5-degree R-MAT hub is spread
+ *     over many CTAs like any other edges;
+ *   - pushes are staged per CTA in shared memory (shared atomics only) and
+ *     published once per unit with ONE 64-bit atomicAdd that allocates queue
+ *     slots and edge offsets together; the same flush marks the next round's
+ *     unit boundaries, so no separate scan pass is needed;
+ *   - deduplication: BFS by a visited bitmap, SSSP by a per-vertex round
  *     stamp (near queue) and a "far pile" bitmap;
  *   - relaxation is atomicMin on uint32 distances, as the reference does;
  *   - rounds are separated by a bounded grid barrier (no host round trip);
  *     a barrier that waits past its limit sets an error word and the kernel
  *     returns, so the host gets GGA_ERR_TIMEOUT instead of a hung GPU.
+ * Synchronisation is block-uniform by construction: no warp collective is
+ * reached under data-dependent control flow, and every __syncthreads is
+ * reached by all threads of the CTA after decisions read from shared memory.
  * On a node-split graph (graph.h:415-522) the engine walks the split view:
- * edges target parents, and reaching a parent reaches its children too
- * (their distances mirror the parent's, cudaKernels.h:326-330), each child
- * being expanded as its own work item over its slice of the edges.
+ * edges target parents, reaching a parent reaches its children too (their
+ * distances mirror the parent's, cudaKernels.h:326-330), and a parent's
+ * queue entry covers its own and its children's contiguous edge slices.
  */
 #include <stdio.h>
+#include <string.h>
 
 #include "frontier.cuh"
 
 namespace {
 
-constexpr uint32_t FULL = 0xffffffffu;
 constexpr uint32_t NONE = 0xffffffffu;
+constexpr uint32_t MIN_UNIT = 512;  /* smallest edges-per-unit the buffers are sized for */
+constexpr uint32_t MAX_UNIT = 4096; /* largest edges-per-unit (shared-memory bound) */
 
 struct Args {
     const uint32_t *off, *col, *wt, *cc;
     const uint32_t *first; /* split view: original -> parent split id */
-    uint32_t n;
+    uint32_t n, m;
     uint32_t *dist, *bits, *farbits, *stamp;
-    uint32_t *q0, *q1, *hq0, *hq1, *hqb0, *hqb1, *far0, *far1, *far2;
+    uint32_t *qv0, *qv1, *qo0, *qo1, *qb0, *qb1, *uf0, *uf1;
+    uint32_t *far0, *far1, *far2;
     FrontierCtl *ctl;
-    uint32_t cap, hcap;
+    uint32_t cap;  /* queue entries */
+    uint32_t ucap; /* unit-boundary entries */
     uint32_t src;
-    uint32_t huge_degree, chunk_edges;
+    uint32_t unit;  /* edges per unit = BS * iters */
+    uint32_t iters; /* CTA-wide iterations per unit */
+    uint32_t scap;  /* staging slots per CTA = BS * (iters + 1) */
     uint32_t delta;
     uint32_t nblocks;
+    uint32_t max_rounds;
     unsigned long long timeout_ns;
 };
 
@@ -57,129 +71,187 @@ __device__ __forceinline__ uint32_t *sel3(uint32_t p, uint32_t *a, uint32_t *b, 
 
 __device__ __forceinline__ void set_err(FrontierCtl *c, uint32_t code) { atomicCAS(&c->err, GGA_DEV_OK, code); }
 
-/* Queue the pieces of vertex v (v itself plus its split children) for the
- * next round.  Must be called by all 32 lanes of a warp (want may differ). */
-__device__ __forceinline__ void push_near(const Args &a, uint32_t v, bool want, uint32_t nxt, uint32_t r3n) {
-    bool simple = false;
-    uint32_t pieces = 1;
-    if (want) {
-        if (a.cc) pieces = a.cc[v] + 1;
-        if (pieces == 1) {
-            const uint32_t d = __ldg(a.off + v + 1) - __ldg(a.off + v);
-            simple = d != 0 && d <= a.huge_degree;
-            if (d == 0) want = false; /* nothing to expand */
-        }
-    }
-    const uint32_t mask = __ballot_sync(FULL, simple);
-    if (mask) {
-        const uint32_t leader = __ffs(mask) - 1;
-        uint32_t base = 0;
-        if (lane_id() == leader) base = atomicAdd(&a.ctl->qcount[r3n], (uint32_t)__popc(mask));
-        base = __shfl_sync(FULL, base, leader);
-        if (simple) {
-            const uint32_t idx = base + __popc(mask & lanemask_lt());
-            if (idx < a.cap) sel(nxt, a.q0, a.q1)[idx] = v;
-            else set_err(a.ctl, GGA_DEV_OVERFLOW);
-        }
-    }
-    if (want && !simple) {
-        for (uint32_t k = 0; k < pieces; ++k) {
-            const uint32_t w = v + k;
-            const uint32_t b = __ldg(a.off + w), d = __ldg(a.off + w + 1) - b;
-            if (d == 0) continue;
-            if (d <= a.huge_degree) {
-                const uint32_t idx = atomicAdd(&a.ctl->qcount[r3n], 1u);
-                if (idx < a.cap) sel(nxt, a.q0, a.q1)[idx] = w;
-                else set_err(a.ctl, GGA_DEV_OVERFLOW);
-            } else {
-                const uint32_t nch = (d + a.chunk_edges - 1) / a.chunk_edges;
-                const unsigned long long old = atomicAdd(&a.ctl->huge[r3n], (1ull << 32) | nch);
-                const uint32_t it = (uint32_t)(old >> 32);
-                if (it < a.hcap) {
-                    sel(nxt, a.hq0, a.hq1)[it] = w;
-                    sel(nxt, a.hqb0, a.hqb1)[it] = (uint32_t)old;
-                } else {
-                    set_err(a.ctl, GGA_DEV_OVERFLOW);
-                }
-            }
-        }
+/* Edge range of queue entry v: its own slice plus its split children's. */
+__device__ __forceinline__ void item_range(const Args &a, uint32_t v, uint32_t &beg, uint32_t &deg) {
+    beg = __ldg(a.off + v);
+    const uint32_t last = a.cc ? v + a.cc[v] : v;
+    deg = __ldg(a.off + last + 1) - beg;
+}
+
+/* Shared-memory layout of one CTA (dynamic shared memory):
+ *   table : t_o[U+1], t_b[U+1] (+ t_du[U+1] for SSSP)   the unit's queue entries
+ *   stage : sv[scap], sb[scap], sd[scap] (+ sf[scap])     staged pushes
+ * Staging uses shared-memory atomics only; every collective step (flushes,
+ * scans, the unit table) is entered by the whole CTA under block-uniform
+ * control flow decided from shared memory after a __syncthreads. */
+struct Ctrl {
+    uint32_t nn, fn, fmin;   /* staged near / far counts, smallest far distance */
+    uint32_t base_i, base_e; /* flush allocation */
+    uint32_t unit, i0, cnt;  /* current unit */
+    uint32_t nitems, total, fc, fm;
+    uint32_t ws[32];         /* block-scan scratch */
+};
+
+/* Stage a near-queue entry (any thread, any time between flushes). */
+__device__ __forceinline__ void stage_near(const Args &a, Ctrl &C, uint32_t *sv, uint32_t *sb, uint32_t *sd,
+                                           uint32_t v, uint32_t b, uint32_t d) {
+    const uint32_t k = atomicAdd(&C.nn, 1u);
+    if (k < a.scap) {
+        sv[k] = v;
+        sb[k] = b;
+        sd[k] = d;
+    } else {
+        set_err(a.ctl, GGA_DEV_OVERFLOW);
     }
 }
 
-/* Add v to the far pile `fp` (warp-uniform call). */
-__device__ __forceinline__ void push_far(const Args &a, uint32_t v, bool want, uint32_t fp) {
-    const uint32_t mask = __ballot_sync(FULL, want);
-    if (!mask) return;
-    const uint32_t leader = __ffs(mask) - 1;
-    uint32_t base = 0;
-    if (lane_id() == leader) base = atomicAdd(&a.ctl->far_count[fp], (uint32_t)__popc(mask));
-    base = __shfl_sync(FULL, base, leader);
-    if (want) {
-        const uint32_t idx = base + __popc(mask & lanemask_lt());
-        if (idx < a.cap) sel3(fp, a.far0, a.far1, a.far2)[idx] = v;
-        else set_err(a.ctl, GGA_DEV_OVERFLOW);
-    }
+__device__ __forceinline__ void stage_far(const Args &a, Ctrl &C, uint32_t *sf, uint32_t v) {
+    const uint32_t k = atomicAdd(&C.fn, 1u);
+    if (k < a.scap) sf[k] = v;
+    else set_err(a.ctl, GGA_DEV_OVERFLOW_FAR);
 }
 
-/* Relax one edge to v with candidate distance alt; returns through the
- * out-parameters whether v goes to the near queue or the far pile.
- * Called under warp-uniform control flow; `active` masks idle lanes. */
+/* Publish the CTA's staged near-queue entries: a block scan of their degrees,
+ * ONE 64-bit atomicAdd that allocates queue slots (high word) and edge
+ * offsets (low word), coalesced writes of the entries, and the unit
+ * boundaries k*U that fall inside the allocated edge range.  Called by every
+ * thread of the CTA with the same nn (read from shared memory between two
+ * __syncthreads); no thread stages while it runs. */
+template <int BS>
+__device__ __forceinline__ void flush_near(const Args &a, Ctrl &C, uint32_t *sv, uint32_t *sb, uint32_t *sd,
+                                           uint32_t nn, uint32_t nxt, uint32_t r3n) {
+    if (nn == 0) return;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t chunk = (nn + BS - 1) / BS;
+    const uint32_t j0 = min(tid * chunk, nn), j1 = min(j0 + chunk, nn);
+    uint32_t local = 0;
+    for (uint32_t j = j0; j < j1; ++j) local += sd[j];
+    uint32_t tot;
+    uint32_t run = block_exclusive_scan(local, C.ws, &tot);
+    for (uint32_t j = j0; j < j1; ++j) { /* degrees -> exclusive prefix within this flush */
+        const uint32_t d = sd[j];
+        sd[j] = run;
+        run += d;
+    }
+    if (tid == 0) {
+        const unsigned long long old =
+            atomicAdd(&a.ctl->qctr[r3n], ((unsigned long long)nn << 32) | (unsigned long long)tot);
+        C.base_i = (uint32_t)(old >> 32);
+        C.base_e = (uint32_t)old;
+    }
+    __syncthreads();
+    const uint32_t bi = C.base_i, be = C.base_e;
+    uint32_t *qv = sel(nxt, a.qv0, a.qv1), *qo = sel(nxt, a.qo0, a.qo1), *qb = sel(nxt, a.qb0, a.qb1);
+    uint32_t *uf = sel(nxt, a.uf0, a.uf1);
+    for (uint32_t j = tid; j < nn; j += BS) {
+        const uint32_t i = bi + j;
+        if (i < a.cap) {
+            qv[i] = sv[j];
+            qo[i] = be + sd[j];
+            qb[i] = sb[j];
+        } else {
+            set_err(a.ctl, GGA_DEV_OVERFLOW);
+        }
+    }
+    /* unit boundaries inside [be, be + tot): the entry holding edge k*U */
+    const uint64_t k0 = ((uint64_t)be + a.unit - 1) / a.unit, k1 = ((uint64_t)be + tot + a.unit - 1) / a.unit;
+    for (uint64_t k = k0 + tid; k < k1; k += BS) {
+        const uint32_t rel = (uint32_t)(k * a.unit - be);
+        uint32_t lo = 0, hi = nn; /* last j with sd[j] <= rel */
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (sd[mid] <= rel) lo = mid; else hi = mid;
+        }
+        if (k < a.ucap) uf[k] = bi + lo;
+        else set_err(a.ctl, GGA_DEV_OVERFLOW_UNITS);
+    }
+    __syncthreads();
+    if (tid == 0) C.nn = 0;
+    __syncthreads();
+}
+
+/* Publish the CTA's staged far-pile entries (same calling rules). */
+template <int BS>
+__device__ __forceinline__ void flush_far(const Args &a, Ctrl &C, uint32_t *sf, uint32_t fn, uint32_t fp) {
+    if (fn == 0) return;
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) C.base_i = atomicAdd(&a.ctl->far_count[fp], fn);
+    __syncthreads();
+    const uint32_t base = C.base_i;
+    uint32_t *pile = sel3(fp, a.far0, a.far1, a.far2);
+    for (uint32_t j = tid; j < fn; j += BS) {
+        if (base + j < a.cap) pile[base + j] = sf[j];
+        else set_err(a.ctl, GGA_DEV_OVERFLOW_FAR);
+    }
+    __syncthreads();
+    if (tid == 0) C.fn = 0;
+    __syncthreads();
+}
+
+/* Block-uniform checkpoint: wait for all staging, read the counts, and
+ * publish a buffer when it is at least `limit` full (limit 1 = always). */
+template <int BS, bool SSSP>
+__device__ __forceinline__ void checkpoint(const Args &a, Ctrl &C, uint32_t *sv, uint32_t *sb, uint32_t *sd,
+                                           uint32_t *sf, uint32_t nxt, uint32_t r3n, uint32_t fp, uint32_t limit) {
+    __syncthreads();
+    const uint32_t nn = C.nn, fn = SSSP ? C.fn : 0u;
+    __syncthreads();
+    if (nn >= limit) flush_near<BS>(a, C, sv, sb, sd, nn, nxt, r3n);
+    if (SSSP && fn >= limit) flush_far<BS>(a, C, sf, fn, fp);
+}
+
+/* Relax one edge to v with candidate distance alt (atomicMin on uint32, as
+ * M_my_drelax does, cudaKernels.h:323-330); reports whether v joins the
+ * near queue or the far pile (farval = its new distance). */
 template <bool SSSP>
-__device__ __forceinline__ void relax(const Args &a, bool active, uint32_t v, uint32_t alt, uint32_t round,
-                                      uint32_t thr, uint32_t fp, uint32_t nxt, uint32_t r3n) {
-    bool near = false, far = false;
-    uint32_t farval = NONE;
-    if (active) {
-        if (!SSSP) {
-            const uint32_t bit = 1u << (v & 31);
-            if (!(__ldcg(a.bits + (v >> 5)) & bit)) {
-                const uint32_t old = atomicOr(a.bits + (v >> 5), bit);
-                if (!(old & bit)) {
-                    a.dist[v] = alt;
-                    if (a.cc) {
-                        const uint32_t c = a.cc[v];
-                        for (uint32_t k = 1; k <= c; ++k) a.dist[v + k] = alt;
-                    }
-                    near = true;
-                }
-            }
-        } else if (alt < __ldcg(a.dist + v)) {
-            const uint32_t old = atomicMin(a.dist + v, alt);
-            if (alt < old) {
+__device__ __forceinline__ void relax_edge(const Args &a, uint32_t v, uint32_t alt, uint32_t round, uint32_t thr,
+                                           bool &near, bool &far, uint32_t &farval) {
+    near = false;
+    far = false;
+    farval = NONE;
+    if (!SSSP) {
+        const uint32_t bit = 1u << (v & 31);
+        if (!(__ldcg(a.bits + (v >> 5)) & bit)) {
+            const uint32_t old = atomicOr(a.bits + (v >> 5), bit);
+            if (!(old & bit)) {
+                a.dist[v] = alt;
                 if (a.cc) {
                     const uint32_t c = a.cc[v];
-                    for (uint32_t k = 1; k <= c; ++k) atomicMin(a.dist + v + k, alt);
+                    for (uint32_t k = 1; k <= c; ++k) a.dist[v + k] = alt;
                 }
-                if (alt < thr) {
-                    near = atomicExch(a.stamp + v, round + 1) != round + 1;
-                } else {
-                    farval = alt;
-                    const uint32_t bit = 1u << (v & 31);
-                    far = !(atomicOr(a.farbits + (v >> 5), bit) & bit);
-                }
+                near = true;
             }
         }
-    }
-    push_near(a, v, near, nxt, r3n);
-    if (SSSP) {
-        const uint32_t wmin = __reduce_min_sync(FULL, farval);
-        if (wmin != NONE && lane_id() == __ffs(__ballot_sync(FULL, farval == wmin)) - 1)
-            atomicMin(&a.ctl->far_min[fp], wmin);
-        push_far(a, v, far, fp);
+    } else if (alt < __ldcg(a.dist + v)) {
+        const uint32_t old = atomicMin(a.dist + v, alt);
+        if (alt < old) {
+            if (a.cc) {
+                const uint32_t c = a.cc[v];
+                for (uint32_t k = 1; k <= c; ++k) atomicMin(a.dist + v + k, alt);
+            }
+            if (alt < thr) {
+                near = atomicExch(a.stamp + v, round + 1) != round + 1;
+            } else {
+                farval = alt;
+                const uint32_t bit = 1u << (v & 31);
+                far = !(atomicOr(a.farbits + (v >> 5), bit) & bit);
+            }
+        }
     }
 }
 
 template <int BS, bool SSSP>
-__global__ void __launch_bounds__(BS) k_frontier(Args a) {
-    __shared__ uint32_t s_incl[BS];
-    __shared__ uint32_t s_adj[BS];
-    __shared__ uint32_t s_du[SSSP ? BS : 1];
-    __shared__ uint32_t s_ws[32];
-    __shared__ uint32_t s_unit, s_hstart, s_hcnt, s_hdu;
+__global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_frontier(Args a) {
+    extern __shared__ uint32_t dyn[];
+    __shared__ Ctrl C;
 
     FrontierCtl *ctl = a.ctl;
     const uint32_t tid = threadIdx.x;
     const uint64_t gtid = (uint64_t)blockIdx.x * BS + tid, gthreads = (uint64_t)gridDim.x * BS;
+    const uint32_t U = a.unit, S = a.scap;
+    uint32_t *t_o = dyn, *t_b = dyn + (U + 1), *t_du = dyn + 2 * (U + 1);
+    uint32_t *stage = dyn + (SSSP ? 3u : 2u) * (U + 1);
+    uint32_t *sv = stage, *sb = stage + S, *sd = stage + 2 * S, *sf = stage + 3 * S;
     uint32_t gen = 0;
     unsigned long long relaxed = 0;
 
@@ -193,62 +265,78 @@ __global__ void __launch_bounds__(BS) k_frontier(Args a) {
         if (SSSP) a.farbits[i] = 0;
         else a.bits[i] = 0;
     }
-    if (blockIdx.x == 0 && tid == 0) {
-        ctl->far_min[0] = NONE;
-        ctl->far_min[1] = NONE;
-        ctl->far_min[2] = NONE;
+    if (tid == 0) {
+        C.nn = 0;
+        C.fn = 0;
+        C.fmin = NONE;
+        if (blockIdx.x == 0) {
+            ctl->far_min[0] = NONE;
+            ctl->far_min[1] = NONE;
+            ctl->far_min[2] = NONE;
+        }
     }
     if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) return;
 
     /* ---- the source: original vertex src -> its parent split id and pieces
      * (bfs_sssp.cu:301-318 zeroes the parent and its children) */
-    if (blockIdx.x == 0 && tid < 32) {
+    if (blockIdx.x == 0 && tid == 0) {
         const uint32_t s0 = a.first ? a.first[a.src] : a.src;
         const uint32_t cnt = a.cc ? a.cc[s0] + 1 : 1;
-        for (uint32_t k = tid; k < cnt; k += 32) a.dist[s0 + k] = 0;
-        if (tid == 0) {
-            if (!SSSP) a.bits[s0 >> 5] |= 1u << (s0 & 31);
-            else a.stamp[s0] = 0;
+        for (uint32_t k = 0; k < cnt; ++k) a.dist[s0 + k] = 0;
+        if (!SSSP) a.bits[s0 >> 5] |= 1u << (s0 & 31);
+        uint32_t b, d;
+        item_range(a, s0, b, d);
+        if (d) {
+            ctl->qctr[0] = (1ull << 32) | d;
+            a.qv0[0] = s0;
+            a.qo0[0] = 0;
+            a.qb0[0] = b;
+            for (uint32_t k = 0; (uint64_t)k * U < d && k < a.ucap; ++k) a.uf0[k] = 0;
         }
-        __syncwarp();
-        push_near(a, s0, tid == 0, 0, 0);
     }
     if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) return;
 
     uint32_t thr = SSSP ? (a.delta ? a.delta : NONE) : 0;
     uint32_t fp = 0;
     uint32_t round = 0;
-    /* Every decision below reads only counters that no block writes during
-     * the current round: the round's input queue (pushes go to the next
-     * slot) and, when that queue is empty, the far pile (nothing relaxes).
-     * So all blocks take the same branch and meet the same barriers. */
+    /* Each block reads a round's counters once (thread 0) and shares them, and
+     * those counters are not written during the round (pushes go to the next
+     * slot; when the queue is empty nothing relaxes, so the far pile is
+     * stable).  All blocks therefore take the same branches and meet the
+     * same barriers, and all threads of a block the same __syncthreads. */
     for (;; ++round) {
         const uint32_t r3 = round % 3, r3n = (round + 1) % 3, cur = round & 1, nxt = cur ^ 1;
-        /* an overflowing push sets the error word, so a queue past its
-         * capacity is never consumed; the clamps only keep reads in bounds */
-        const uint32_t qn = min(ld_relaxed_u32(&ctl->qcount[r3]), a.cap);
-        const unsigned long long hh = ld_relaxed_u64(&ctl->huge[r3]);
-        const uint32_t hitems = min((uint32_t)(hh >> 32), a.hcap), hchunks = hitems ? (uint32_t)hh : 0u;
-        const uint32_t nchunks = (qn + BS - 1) / BS;
-        const uint32_t units = nchunks + hchunks;
-        const uint32_t *qin = sel(cur, a.q0, a.q1);
-        const uint32_t *hqin = sel(cur, a.hq0, a.hq1);
-        const uint32_t *hqbin = sel(cur, a.hqb0, a.hqb1);
+        if (tid == 0) {
+            const unsigned long long qc = ld_relaxed_u64(&ctl->qctr[r3]);
+            /* an overflowing push sets the error word, so an over-full queue
+             * is never consumed; the clamps only keep reads in bounds */
+            const uint32_t ni = min((uint32_t)(qc >> 32), a.cap);
+            C.nitems = ni;
+            C.total = ni ? (uint32_t)qc : 0u;
+            C.fc = SSSP ? min(ld_relaxed_u32(&ctl->far_count[fp]), a.cap) : 0u;
+            C.fm = SSSP ? ld_relaxed_u32(&ctl->far_min[fp]) : NONE;
+        }
+        __syncthreads();
+        const uint32_t nitems = C.nitems, total = C.total, fc = C.fc, fm = C.fm;
+        const uint32_t units = min((uint32_t)(((uint64_t)total + U - 1) / U), a.ucap);
+        __syncthreads(); /* C is rewritten below */
+        if (round >= a.max_rounds) { /* safety net; every block stops in the same round */
+            if (blockIdx.x == 0 && tid == 0) set_err(ctl, GGA_DEV_ROUND_LIMIT);
+            break;
+        }
+        const uint32_t *qv = sel(cur, a.qv0, a.qv1), *qo = sel(cur, a.qo0, a.qo1), *qb = sel(cur, a.qb0, a.qb1);
+        const uint32_t *uf = sel(cur, a.uf0, a.uf1);
         if (blockIdx.x == 0 && tid == 0) {
             const uint32_t r3nn = (round + 2) % 3;
-            ctl->qcount[r3nn] = 0;
+            ctl->qctr[r3nn] = 0;
             ctl->work[r3nn] = 0;
-            ctl->huge[r3nn] = 0;
         }
         if (units == 0) {
-            if (!SSSP) break;
-            const uint32_t fc = min(ld_relaxed_u32(&ctl->far_count[fp]), a.cap);
-            if (fc == 0) break;
+            if (!SSSP || fc == 0) break;
             /* ---- near queue drained: raise the threshold and split the far
-             * pile into the next round's near queue and the other pile */
-            const uint32_t fmin = ld_relaxed_u32(&ctl->far_min[fp]);
+             * pile into the next round's near queue and the next pile */
             const uint32_t thr_old = thr;
-            const uint32_t lowest = max(thr, fmin);
+            const uint32_t lowest = max(thr, fm);
             thr = lowest > NONE - a.delta ? NONE : lowest + a.delta;
             const uint32_t fq = fp == 2 ? 0 : fp + 1; /* pile that keeps the far items */
             if (blockIdx.x == 0 && tid == 0) {
@@ -263,97 +351,92 @@ __global__ void __launch_bounds__(BS) k_frontier(Args a) {
             const uint32_t *fin = sel3(fp, a.far0, a.far1, a.far2);
             for (uint64_t base = (uint64_t)blockIdx.x * BS; base < fc; base += gthreads) {
                 const uint64_t i = base + tid;
-                bool to_near = false, keep = false;
-                uint32_t v = 0, d = NONE;
                 if (i < fc) {
-                    v = __ldcg(fin + i);
-                    d = __ldcg(a.dist + v);
+                    const uint32_t v = __ldcg(fin + i);
+                    const uint32_t d = __ldcg(a.dist + v);
                     if (d >= thr) {
-                        keep = true;
+                        atomicMin(&C.fmin, d);
+                        stage_far(a, C, sf, v);
                     } else {
                         atomicAnd(a.farbits + (v >> 5), ~(1u << (v & 31)));
-                        if (d >= thr_old) to_near = atomicExch(a.stamp + v, round + 1) != round + 1;
+                        if (d >= thr_old && atomicExch(a.stamp + v, round + 1) != round + 1) {
+                            uint32_t b, dg;
+                            item_range(a, v, b, dg);
+                            if (dg) stage_near(a, C, sv, sb, sd, v, b, dg);
+                        }
                     }
                 }
-                push_near(a, v, to_near, nxt, r3n);
-                const uint32_t kmin = __reduce_min_sync(FULL, keep ? d : NONE);
-                if (kmin != NONE && lane_id() == __ffs(__ballot_sync(FULL, keep && d == kmin)) - 1)
-                    atomicMin(&ctl->far_min[fq], kmin);
-                push_far(a, v, keep, fq);
+                checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fq, BS);
+            }
+            checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fq, 1);
+            if (tid == 0 && C.fmin != NONE) {
+                atomicMin(&ctl->far_min[fq], C.fmin);
+                C.fmin = NONE;
             }
             if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
             fp = fq;
             continue;
         }
         for (;;) {
-            if (tid == 0) s_unit = atomicAdd(&ctl->work[r3], 1u);
-            __syncthreads();
-            const uint32_t unit = s_unit;
-            if (unit >= units) break;
-            if (unit < nchunks) {
-                /* a tile of BS frontier vertices, expanded by the whole CTA */
-                const uint32_t idx = unit * BS + tid;
-                uint32_t beg = 0, deg = 0, du = 0;
-                if (idx < qn) {
-                    const uint32_t v = __ldcg(qin + idx);
-                    beg = __ldg(a.off + v);
-                    deg = __ldg(a.off + v + 1) - beg;
-                    if (SSSP) du = __ldcg(a.dist + v);
+            if (tid == 0) {
+                const uint32_t k = atomicAdd(&ctl->work[r3], 1u);
+                C.unit = k;
+                if (k < units) {
+                    const uint32_t i0 = min(__ldcg(uf + k), nitems - 1);
+                    const uint32_t i1 = k + 1 < units ? min(__ldcg(uf + k + 1), nitems - 1) : nitems - 1;
+                    C.i0 = i0;
+                    C.cnt = i1 >= i0 ? min(i1 - i0 + 1, U + 1) : 1u;
                 }
-                uint32_t total;
-                const uint32_t pos = block_exclusive_scan(deg, s_ws, &total);
-                s_incl[tid] = pos + deg;
-                s_adj[tid] = beg - pos;
-                if (SSSP) s_du[tid] = du;
-                __syncthreads();
-                for (uint32_t base = 0; base < total; base += BS) {
-                    const uint32_t e = base + tid;
-                    const bool act = e < total;
-                    uint32_t v = 0, alt = 0;
-                    if (act) {
-                        uint32_t lo = 0, hi = BS - 1; /* first o with s_incl[o] > e */
-                        while (lo < hi) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (s_incl[mid] > e) hi = mid; else lo = mid + 1;
-                        }
-                        const uint32_t ei = e + s_adj[lo];
-                        v = __ldg(a.col + ei);
-                        alt = SSSP ? s_du[lo] + __ldg(a.wt + ei) : round + 1;
-                    }
-                    relax<SSSP>(a, act, v, alt, round, thr, fp, nxt, r3n);
-                }
-                if (tid == 0) relaxed += total;
-            } else {
-                /* one chunk of a huge vertex's edge list */
-                if (tid == 0) {
-                    const uint32_t c = unit - nchunks;
-                    uint32_t lo = 0, hi = hitems; /* last item whose first chunk <= c */
-                    while (hi - lo > 1) {
-                        const uint32_t mid = (lo + hi) >> 1;
-                        if (__ldcg(hqbin + mid) <= c) lo = mid; else hi = mid;
-                    }
-                    const uint32_t v = __ldcg(hqin + lo);
-                    const uint32_t b = __ldg(a.off + v), d = __ldg(a.off + v + 1) - b;
-                    const uint32_t start = (c - __ldcg(hqbin + lo)) * a.chunk_edges;
-                    s_hstart = b + start;
-                    s_hcnt = start < d ? min(a.chunk_edges, d - start) : 0u;
-                    s_hdu = SSSP ? __ldcg(a.dist + v) : 0;
-                }
-                __syncthreads();
-                const uint32_t hs = s_hstart, hc = s_hcnt, hdu = s_hdu;
-                for (uint32_t base = 0; base < hc; base += BS) {
-                    const uint32_t e = base + tid;
-                    const bool act = e < hc;
-                    uint32_t v = 0, alt = 0;
-                    if (act) {
-                        v = __ldg(a.col + hs + e);
-                        alt = SSSP ? hdu + __ldg(a.wt + hs + e) : round + 1;
-                    }
-                    relax<SSSP>(a, act, v, alt, round, thr, fp, nxt, r3n);
-                }
-                if (tid == 0) relaxed += hc;
             }
             __syncthreads();
+            const uint32_t k = C.unit;
+            if (k >= units) break;
+            const uint32_t i0 = C.i0, cnt = C.cnt;
+            const uint32_t ebase = k * U, eend = min(ebase + U, total);
+            for (uint32_t j = tid; j < cnt; j += BS) {
+                const uint32_t i = i0 + j;
+                t_o[j] = __ldcg(qo + i);
+                t_b[j] = __ldcg(qb + i);
+                if (SSSP) t_du[j] = __ldcg(a.dist + __ldcg(qv + i));
+            }
+            __syncthreads();
+            /* consecutive threads take consecutive edges of the unit */
+            for (uint32_t it = 0; it < a.iters; ++it) {
+                const uint32_t e = ebase + it * BS + tid;
+                if (e >= eend) continue;
+                uint32_t lo = 0, hi = cnt; /* last j with t_o[j] <= e */
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (t_o[mid] <= e) lo = mid; else hi = mid;
+                }
+                const uint32_t ei = t_b[lo] + (e - t_o[lo]);
+                if (ei >= a.m) { /* unreachable by construction; keeps reads in bounds */
+                    set_err(ctl, GGA_DEV_BAD_EDGE);
+                    continue;
+                }
+                const uint32_t v = __ldg(a.col + ei);
+                const uint32_t alt = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
+                bool nr, fr;
+                uint32_t fv;
+                relax_edge<SSSP>(a, v, alt, round, thr, nr, fr, fv);
+                if (nr) {
+                    uint32_t b, dg;
+                    item_range(a, v, b, dg);
+                    if (dg) stage_near(a, C, sv, sb, sd, v, b, dg); /* nothing to expand otherwise */
+                }
+                if (SSSP && fv != NONE) {
+                    atomicMin(&C.fmin, fv);
+                    if (fr) stage_far(a, C, sf, v);
+                }
+            }
+            if (tid == 0) relaxed += eend - ebase;
+            /* ends the unit: table reads done, staged counts stable */
+            checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fp, BS);
+        }
+        checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fp, 1);
+        if (SSSP && tid == 0 && C.fmin != NONE) {
+            atomicMin(&ctl->far_min[fp], C.fmin);
+            C.fmin = NONE;
         }
         if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
     }
@@ -362,25 +445,38 @@ __global__ void __launch_bounds__(BS) k_frontier(Args a) {
 }
 
 template <int BS, bool SSSP>
-int occupancy() {
-    static int occ = -1;
-    if (occ < 0) {
-        int v = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_frontier<BS, SSSP>, BS, 0) != cudaSuccess) v = 0;
-        occ = v;
+size_t dyn_smem(uint32_t unit, uint32_t scap) {
+    return ((size_t)(unit + 1) * (SSSP ? 3 : 2) + (size_t)scap * (SSSP ? 4 : 3)) * sizeof(uint32_t);
+}
+
+template <int BS, bool SSSP>
+int occupancy(size_t smem) {
+    static int occ[8];
+    static size_t occ_smem[8];
+    static int used = 0;
+    for (int i = 0; i < used; ++i)
+        if (occ_smem[i] == smem) return occ[i];
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_frontier<BS, SSSP>, BS, smem) != cudaSuccess) v = 0;
+    if (used < 8) {
+        occ[used] = v;
+        occ_smem[used] = smem;
+        ++used;
     }
-    return occ;
+    return v;
 }
 
 template <int BS, bool SSSP>
 gga_status launch(Args &a, const gga_params &p, int sms, cudaStream_t st) {
-    int occ = occupancy<BS, SSSP>();
-    if (occ <= 0) return gga_fail(GGA_ERR_CUDA, "frontier kernel: zero occupancy");
+    const size_t smem = dyn_smem<BS, SSSP>(a.unit, a.scap);
+    GGA_CK(cudaFuncSetAttribute(k_frontier<BS, SSSP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = occupancy<BS, SSSP>(smem);
+    if (occ <= 0) return gga_fail(GGA_ERR_CUDA, "frontier kernel: zero occupancy (unit %u)", a.unit);
     int per_sm = p.blocks_per_sm ? (int)p.blocks_per_sm : occ;
     if (per_sm > occ) per_sm = occ;
     a.nblocks = (uint32_t)(sms * per_sm);
     void *args[] = {&a};
-    GGA_CK(cudaLaunchCooperativeKernel((const void *)k_frontier<BS, SSSP>, dim3(a.nblocks), dim3(BS), args, 0, st));
+    GGA_CK(cudaLaunchCooperativeKernel((const void *)k_frontier<BS, SSSP>, dim3(a.nblocks), dim3(BS), args, smem, st));
     return GGA_OK;
 }
 
@@ -393,35 +489,39 @@ static gga_status alloc_u32(uint32_t **p, size_t n) {
 
 void frontier_scratch_free(FrontierScratch *s) {
     cudaFree(s->dist); cudaFree(s->bits); cudaFree(s->farbits); cudaFree(s->stamp);
-    cudaFree(s->q0); cudaFree(s->q1); cudaFree(s->hq0); cudaFree(s->hq1);
-    cudaFree(s->hqb0); cudaFree(s->hqb1); cudaFree(s->far0); cudaFree(s->far1); cudaFree(s->far2);
+    cudaFree(s->qv0); cudaFree(s->qv1); cudaFree(s->qo0); cudaFree(s->qo1); cudaFree(s->qb0); cudaFree(s->qb1);
+    cudaFree(s->uf0); cudaFree(s->uf1);
+    cudaFree(s->far0); cudaFree(s->far1); cudaFree(s->far2);
     cudaFree(s->out); cudaFree(s->ctl);
+    if (s->hctl) cudaFreeHost(s->hctl);
     memset(s, 0, sizeof *s);
 }
 
 gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m) {
-    (void)m;
-    if (s->cap >= n && s->ctl) return GGA_OK;
+    const uint32_t ucap = m / MIN_UNIT + 4;
+    if (s->cap >= n && s->ucap >= ucap && s->ctl) return GGA_OK;
     frontier_scratch_free(s);
     const uint32_t cap = n < 1024 ? 1024 : n;
     const size_t words = (cap + 31) / 32 + 1;
     gga_status st;
     if ((st = alloc_u32(&s->dist, cap)) || (st = alloc_u32(&s->bits, words)) ||
         (st = alloc_u32(&s->farbits, words)) || (st = alloc_u32(&s->stamp, cap)) ||
-        (st = alloc_u32(&s->q0, cap)) || (st = alloc_u32(&s->q1, cap)) || (st = alloc_u32(&s->hq0, cap)) ||
-        (st = alloc_u32(&s->hq1, cap)) || (st = alloc_u32(&s->hqb0, cap)) || (st = alloc_u32(&s->hqb1, cap)) ||
+        (st = alloc_u32(&s->qv0, cap)) || (st = alloc_u32(&s->qv1, cap)) || (st = alloc_u32(&s->qo0, cap)) ||
+        (st = alloc_u32(&s->qo1, cap)) || (st = alloc_u32(&s->qb0, cap)) || (st = alloc_u32(&s->qb1, cap)) ||
+        (st = alloc_u32(&s->uf0, ucap)) || (st = alloc_u32(&s->uf1, ucap)) ||
         (st = alloc_u32(&s->far0, cap)) || (st = alloc_u32(&s->far1, cap)) || (st = alloc_u32(&s->far2, cap)) ||
         (st = alloc_u32(&s->out, cap))) {
         frontier_scratch_free(s);
         return st;
     }
     cudaError_t e = cudaMalloc((void **)&s->ctl, sizeof(FrontierCtl));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&s->hctl, sizeof(FrontierCtl));
     if (e != cudaSuccess) {
         frontier_scratch_free(s);
         return gga_fail(GGA_ERR_CUDA, "frontier control block: %s", cudaGetErrorString(e));
     }
     s->cap = cap;
-    s->hcap = cap;
+    s->ucap = ucap;
     return GGA_OK;
 }
 
@@ -433,18 +533,29 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     a.off = view.off; a.col = view.col; a.wt = view.wt; a.cc = view.cc;
     a.first = first;
     a.n = view.n;
+    a.m = view.m;
     a.dist = s->dist; a.bits = s->bits; a.farbits = s->farbits; a.stamp = s->stamp;
-    a.q0 = s->q0; a.q1 = s->q1; a.hq0 = s->hq0; a.hq1 = s->hq1; a.hqb0 = s->hqb0; a.hqb1 = s->hqb1;
+    a.qv0 = s->qv0; a.qv1 = s->qv1; a.qo0 = s->qo0; a.qo1 = s->qo1; a.qb0 = s->qb0; a.qb1 = s->qb1;
+    a.uf0 = s->uf0; a.uf1 = s->uf1;
     a.far0 = s->far0; a.far1 = s->far1; a.far2 = s->far2;
     a.ctl = s->ctl;
     a.cap = s->cap;
-    a.hcap = s->hcap;
+    a.ucap = s->ucap;
     a.src = src;
-    a.huge_degree = p.huge_degree ? p.huge_degree : 4096;
-    a.delta = p.sssp_delta;
-    a.timeout_ns = 4000000000ull;
     const uint32_t bs = p.block_threads ? p.block_threads : 256;
-    a.chunk_edges = bs * 16;
+    a.iters = p.unit_iters ? p.unit_iters : 4;
+    if (a.iters < 2 || a.iters > 16)
+        return gga_fail(GGA_ERR_INVALID_ARG, "unit_iters must be in [2, 16] (got %u)", a.iters);
+    a.unit = bs * a.iters;
+    if (a.unit < MIN_UNIT || a.unit > MAX_UNIT)
+        return gga_fail(GGA_ERR_INVALID_ARG, "block_threads x unit_iters = %u edges per unit, need %u..%u", a.unit,
+                        MIN_UNIT, MAX_UNIT);
+    a.scap = bs * (a.iters + 1);
+    a.delta = p.sssp_delta;
+    /* BFS needs at most n levels; near-far SSSP at most a level per
+     * improvement, which the bound below leaves ample room for */
+    a.max_rounds = view.n > 0x3fffffffu ? 0xffffffffu : 4u * view.n + 4096u;
+    a.timeout_ns = 4000000000ull;
     GGA_CK(cudaMemsetAsync(s->ctl, 0, sizeof(FrontierCtl), st));
     if (ev0) GGA_CK(cudaEventRecord(ev0, st));
     gga_status r;
@@ -456,12 +567,22 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     }
     if (r) return r;
     if (ev1) GGA_CK(cudaEventRecord(ev1, st));
-    FrontierCtl h;
-    GGA_CK(cudaMemcpyAsync(&h, s->ctl, sizeof h, cudaMemcpyDeviceToHost, st));
-    GGA_CK(cudaStreamSynchronize(st));
+    GGA_CK(cudaMemcpyAsync(s->hctl, s->ctl, sizeof(FrontierCtl), cudaMemcpyDeviceToHost, st));
+    gga_status w = dev_wait(st, 60.0);
+    if (w) return w;
+    const FrontierCtl h = *s->hctl;
     if (h.err == GGA_DEV_TIMEOUT)
         return gga_fail(GGA_ERR_TIMEOUT, "frontier grid barrier timed out after %u rounds", h.rounds);
     if (h.err == GGA_DEV_OVERFLOW) return gga_fail(GGA_ERR_CUDA, "frontier queue overflow (internal error)");
+    if (h.err == GGA_DEV_ROUND_LIMIT) return gga_fail(GGA_ERR_CUDA, "frontier round limit reached (internal error)");
+    if (h.err == GGA_DEV_OVERFLOW_UNITS) return gga_fail(GGA_ERR_CUDA, "frontier unit table overflow (internal error)");
+    if (h.err == GGA_DEV_OVERFLOW_FAR) return gga_fail(GGA_ERR_CUDA, "frontier far pile overflow (internal error)");
+    if (h.err == GGA_DEV_BAD_EDGE)
+        return gga_fail(GGA_ERR_CUDA,
+                        "frontier unit mapping self-check failed: round %u unit %u e %u jj %u cnt %u i0 %u t_o[jj] %u "
+                        "t_b[jj] %u total %u nitems %u t_o[0] %u t_o[jj+1] %u units %u uf[k] %u uf[k+1] %u ei %u",
+                        h.diag[0], h.diag[1], h.diag[2], h.diag[3], h.diag[4], h.diag[5], h.diag[6], h.diag[7],
+                        h.diag[8], h.diag[9], h.diag[10], h.diag[11], h.diag[12], h.diag[13], h.diag[14], h.diag[15]);
     if (h.err != GGA_DEV_OK) return gga_fail(GGA_ERR_CUDA, "frontier kernel error %u", h.err);
     if (res) {
         res->rounds = h.rounds;

@@ -9,30 +9,32 @@ struct FrontierCtl {
     GridBarrier bar;
     uint32_t err;
     uint32_t rounds;
-    uint32_t qcount[3];           /* near-queue counts, rotating by round */
+    unsigned long long qctr[3];   /* near queue: (entries << 32) | edges, rotating by round */
     uint32_t work[3];             /* work-unit tickets, rotating by round */
-    unsigned long long huge[3];   /* (items << 32) | edge chunks, rotating */
     uint32_t far_count[3];        /* three far piles rotate across far passes */
     uint32_t far_min[3];
     uint32_t far_phases;
     uint32_t overflow_at;
     unsigned long long edges_relaxed;
-    unsigned long long pad[4];
+    uint32_t diag[16];            /* first failed self-check: where and what */
 };
 
 /* Per-context device scratch of the frontier engine, sized by vertices. */
 struct FrontierScratch {
     uint32_t cap;        /* vertex capacity */
-    uint32_t hcap;       /* huge-queue capacity */
+    uint32_t ucap;       /* unit-boundary capacity */
     uint32_t *dist;      /* cap */
     uint32_t *bits;      /* cap/32: BFS visited / SSSP unused */
     uint32_t *farbits;   /* cap/32: SSSP "in far pile" */
     uint32_t *stamp;     /* cap: SSSP last round a vertex was queued */
-    uint32_t *q0, *q1;   /* near queues */
-    uint32_t *hq0, *hq1, *hqb0, *hqb1; /* huge items and their first chunk */
+    uint32_t *qv0, *qv1; /* near queues: vertex */
+    uint32_t *qo0, *qo1; /* exclusive edge offset of each entry in the round */
+    uint32_t *qb0, *qb1; /* first edge of each entry in the CSR */
+    uint32_t *uf0, *uf1; /* unit k's first entry */
     uint32_t *far0, *far1, *far2;
     uint32_t *out;       /* cap: gathered original-order output */
     FrontierCtl *ctl;
+    FrontierCtl *hctl;   /* pinned host mirror (keeps the read-back asynchronous) */
 };
 
 struct FrontierResult {

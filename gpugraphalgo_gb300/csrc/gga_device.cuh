@@ -55,7 +55,11 @@ enum : uint32_t {
     GGA_DEV_OK = 0,
     GGA_DEV_TIMEOUT = 1,
     GGA_DEV_OVERFLOW = 2,
-    GGA_DEV_SPLIT_RULE = 3
+    GGA_DEV_SPLIT_RULE = 3,
+    GGA_DEV_OVERFLOW_UNITS = 4,
+    GGA_DEV_OVERFLOW_FAR = 5,
+    GGA_DEV_BAD_EDGE = 6,
+    GGA_DEV_ROUND_LIMIT = 7
 };
 
 /* ---- small device helpers ---------------------------------------------- */
@@ -90,44 +94,55 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-/* Bounded grid barrier for persistent cooperative launches.  Sense is a
- * generation counter; a block that waits longer than timeout_ns (or sees the
- * error word set) records GGA_DEV_TIMEOUT and returns false instead of
- * spinning on.  Every block must call it the same number of times. */
+/* Bounded grid barrier for persistent cooperative launches.  Arrivals add
+ * to one monotonic counter with acquire-release atomics; barrier number k is
+ * complete once the counter reaches k * nblocks (nothing is ever reset, so
+ * no plain store races with an arrival).  A block that waits longer than
+ * timeout_ns (or sees the error word set) records GGA_DEV_TIMEOUT and returns
+ * false instead of spinning on.  The verdict is broadcast through shared
+ * memory so all threads of a block agree.  Every block must call it the
+ * same number of times. */
 struct GridBarrier {
     uint32_t count;
-    uint32_t gen;
+    uint32_t pad;
 };
+
+__device__ __forceinline__ uint32_t atom_add_acq_rel_u32(uint32_t *p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
 
 __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err, uint32_t nblocks,
                                              uint32_t &gen_local, uint64_t timeout_ns) {
+    __shared__ uint32_t s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t g = gen_local;
+        const uint32_t target = (gen_local + 1) * nblocks;
         __threadfence();
-        uint32_t prev = atomicAdd(&bar->count, 1u);
-        if (prev == nblocks - 1) {
-            bar->count = 0;
-            st_release_u32(&bar->gen, g + 1);
-        } else {
-            uint64_t t0 = global_timer_ns();
-            uint32_t spins = 0;
-            while (ld_acquire_u32(&bar->gen) == g) {
-                if ((++spins & 63u) == 0) {
-                    if (ld_relaxed_u32(err) != GGA_DEV_OK) break;
-                    if (global_timer_ns() - t0 > timeout_ns) {
-                        atomicCAS(err, GGA_DEV_OK, GGA_DEV_TIMEOUT);
-                        break;
-                    }
+        atom_add_acq_rel_u32(&bar->count, 1u);
+        uint64_t t0 = 0;
+        uint32_t spins = 0;
+        while (ld_acquire_u32(&bar->count) < target) {
+            if ((++spins & 63u) == 0) {
+                if (ld_relaxed_u32(err) != GGA_DEV_OK) break;
+                const uint64_t now = global_timer_ns();
+                if (t0 == 0) t0 = now;
+                else if (now - t0 > timeout_ns) {
+                    atomicCAS(err, GGA_DEV_OK, GGA_DEV_TIMEOUT);
+                    break;
                 }
-                __nanosleep(20);
             }
+            __nanosleep(32);
         }
         __threadfence();
-        gen_local = g + 1;
+        gen_local += 1;
+        s_ok = ld_relaxed_u32(err) == GGA_DEV_OK;
     }
     __syncthreads();
-    return ld_relaxed_u32(err) == GGA_DEV_OK;
+    const bool ok = s_ok != 0;
+    __syncthreads(); /* s_ok is rewritten by the next barrier */
+    return ok;
 }
 
 /* Exclusive block scan of one uint32 per thread (blockDim.x a multiple of
@@ -166,6 +181,10 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t *w
 extern "C++" {
 #endif
 /* device_graph.cu */
+/* Waits for `st` like cudaStreamSynchronize, but gives up after limit_s
+ * seconds with GGA_ERR_TIMEOUT (a kernel that never finishes then surfaces as
+ * an error; only ending the process frees the device). */
+gga_status dev_wait(cudaStream_t st, double limit_s);
 gga_status dev_graph_ensure(gga_graph *g, int device, cudaStream_t st);
 DevGraph *dev_graph_of(gga_graph *g);
 gga_status dev_exclusive_scan(const uint32_t *in, uint32_t *out, uint32_t count, cudaStream_t st);

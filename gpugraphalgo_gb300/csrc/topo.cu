@@ -237,7 +237,8 @@ gga_status topo_run(const DevGraph *d, bool split, gga_variant variant, bool sss
         res->launches++;
         GGA_CK(cudaGetLastError());
         GGA_CK(cudaMemcpyAsync(hflag, dflag, 4 * sizeof(uint32_t) + sizeof(CdpState), cudaMemcpyDeviceToHost, st));
-        GGA_CK(cudaStreamSynchronize(st));
+        gga_status w = dev_wait(st, 60.0);
+        if (w) return w;
         cudaEventElapsedTime(&t, ev[0], ev[1]);
         res->ktime += t;
         if (children) {

@@ -81,14 +81,20 @@ def test_split_graph_all_variants_match_reference(golden, ctx):
 
 
 @pytest.mark.parametrize("bs", [256, 512, 1024])
-@pytest.mark.parametrize("huge", [1, 7, 4096])
+@pytest.mark.parametrize("iters", [2, 4, 8])
 @pytest.mark.parametrize("delta", [0, 1, 37, 100000])
-def test_frontier_parameters_do_not_change_answers(golden, ctx, bs, huge, delta):
+def test_frontier_parameters_do_not_change_answers(golden, ctx, bs, iters, delta):
     meta, arrays = golden
     name = "c1_rmat14"
     e = meta["graphs"][name]
     g = build_golden_graph(name, e, arrays)
-    ctx.set_params(block_threads=bs, huge_degree=huge, sssp_delta=delta, use_split=1)
+    ctx.set_params(block_threads=bs, unit_iters=iters, sssp_delta=delta, use_split=1)
+    if bs * iters > 4096:  # a unit must fit the CTA's shared memory
+        with pytest.raises(gga.GGAError) as ex:
+            ctx.solve(g, "bfs", 0, "frontier")
+        assert ex.value.status == gga.ERR_INVALID_ARG
+        ctx.reset_params()
+        return
     try:
         for key, rec in e["dist"].items():
             algo, src = key.split("/")
