@@ -200,7 +200,7 @@ gga_params ctx_default_params(const gga_graph *g) {
     gga_params p;
     memset(&p, 0, sizeof p);
     p.block_threads = 256;
-    p.unit_iters = 4;
+    p.unit_iters = 8;
     uint64_t wsum = 0;
     const uint32_t stride = g->m > (1u << 20) ? g->m >> 20 : 1;
     uint32_t cnt = 0;

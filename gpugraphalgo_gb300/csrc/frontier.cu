@@ -543,7 +543,7 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     a.ucap = s->ucap;
     a.src = src;
     const uint32_t bs = p.block_threads ? p.block_threads : 256;
-    a.iters = p.unit_iters ? p.unit_iters : 4;
+    a.iters = p.unit_iters ? p.unit_iters : 8;
     if (a.iters < 2 || a.iters > 16)
         return gga_fail(GGA_ERR_INVALID_ARG, "unit_iters must be in [2, 16] (got %u)", a.iters);
     a.unit = bs * a.iters;
