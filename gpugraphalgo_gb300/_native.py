@@ -148,6 +148,7 @@ SIGNATURES = {
     "gga_write_dist": (C.c_int, [C.c_char_p, P, P]),
     "gga_reached": (C.c_int, [P, P, PU64, PU64]),
     "gga_write_result_row": (C.c_int, [C.c_char_p, C.POINTER(ResultRow)]),
+    "gga_bfs_noalloc": (C.c_int, [P, P, u32, u32, u32, P, P]),
     "gga_msbfs": (C.c_int, [P, P, u32, P, P, C.POINTER(Stats)]),
     "gga_sssp_batch": (C.c_int, [P, P, u32, P, P, C.POINTER(Stats)]),
     "gga_multi_solve": (C.c_int, [P, u32, C.POINTER(Query), C.POINTER(Stats)]),

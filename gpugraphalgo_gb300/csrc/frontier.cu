@@ -593,3 +593,121 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     }
     return GGA_OK;
 }
+
+/* ------------------------------------------------------------------------
+ * Allocation-free BFS entry point.
+ *
+ * Some callers cannot allocate GPU memory when they run a traversal: code
+ * that runs inside a memory pool or arena another framework owns (calling
+ * cudaMalloc there fragments or oversubscribes that pool), real-time or
+ * latency-critical paths where an allocation may synchronise the device or
+ * take unbounded time, and processes whose device memory is fully reserved
+ * up front.  gga_bfs_noalloc serves them: it runs the same frontier BFS
+ * kernel as gga_bfs, but all of its working memory (queues, visited bitmap,
+ * control block) lives in the fixed array below, which the library
+ * reserves on every GPU where it is loaded and keeps until the process
+ * exits.  The caller provides the graph and the output in device memory.
+ *
+ * Limits: at most NOALLOC_MAX_NODES vertices and NOALLOC_MAX_EDGES edges;
+ * larger graphs are rejected with GGA_ERR_TOO_LARGE.  All calls share the
+ * one array, so calls whose work overlaps on the GPU (different host
+ * threads, or different streams without ordering between them) race and
+ * corrupt each other's results; serialise them.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture begins.
+ * ------------------------------------------------------------------------ */
+
+#include <mutex>
+
+#define NOALLOC_MAX_NODES (1u << 18) /* 262,144 vertices */
+#define NOALLOC_MAX_EDGES (1u << 23) /* 8,388,608 directed edges */
+
+namespace {
+constexpr size_t NA_CTL_WORDS = (sizeof(FrontierCtl) + 255) / 256 * 64; /* control block, 256-byte rounded */
+constexpr size_t NA_BITS_WORDS = NOALLOC_MAX_NODES / 32 + 64;
+constexpr size_t NA_UCAP = NOALLOC_MAX_EDGES / MIN_UNIT + 4;
+constexpr size_t NA_WORDS = NA_CTL_WORDS + NA_BITS_WORDS + 6 * (size_t)NOALLOC_MAX_NODES + 2 * NA_UCAP;
+} // namespace
+
+/* Fixed working memory of gga_bfs_noalloc (about 6.2 MiB per GPU). */
+static __device__ __align__(256) uint32_t g_noalloc_scratch[NA_WORDS];
+
+static std::mutex g_noalloc_mu;
+static uint32_t *g_noalloc_ptr[64]; /* device address of the array, per device */
+static int g_noalloc_sms[64];
+
+extern "C" gga_status gga_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_cols, uint32_t n, uint32_t m,
+                                      uint32_t src, uint32_t *d_dist, void *stream) {
+    if (!d_offsets || !d_dist || (m && !d_cols))
+        return gga_fail(GGA_ERR_INVALID_ARG, "gga_bfs_noalloc: NULL device pointer");
+    if (n == 0 || src >= n) return gga_fail(GGA_ERR_INVALID_ARG, "gga_bfs_noalloc: source %u of %u vertices", src, n);
+    if (n > NOALLOC_MAX_NODES || m > NOALLOC_MAX_EDGES)
+        return gga_fail(GGA_ERR_TOO_LARGE,
+                        "gga_bfs_noalloc: %u vertices / %u edges exceed its fixed working memory "
+                        "(at most %u vertices and %u edges); use gga_bfs",
+                        n, m, NOALLOC_MAX_NODES, NOALLOC_MAX_EDGES);
+    int dev = 0;
+    GGA_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return gga_fail(GGA_ERR_INVALID_ARG, "gga_bfs_noalloc: device %d", dev);
+    uint32_t *base;
+    int sms;
+    {
+        /* once per device, with that device current: host code cannot use the
+         * array's name as a device address, so ask the runtime for it */
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess)
+                return gga_fail(GGA_ERR_CUDA, "gga_bfs_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            int s = 0;
+            e = cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess)
+                return gga_fail(GGA_ERR_CUDA, "gga_bfs_noalloc: SM count: %s", cudaGetErrorString(e));
+            g_noalloc_sms[dev] = s;
+            g_noalloc_ptr[dev] = (uint32_t *)p;
+        }
+        base = g_noalloc_ptr[dev];
+        sms = g_noalloc_sms[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    FrontierCtl *ctl = (FrontierCtl *)base;
+    uint32_t *w = base + NA_CTL_WORDS;
+    Args a;
+    memset(&a, 0, sizeof a);
+    a.off = d_offsets;
+    a.col = d_cols;
+    a.n = n;
+    a.m = m;
+    a.dist = d_dist;
+    a.bits = w;
+    w += NA_BITS_WORDS;
+    a.qv0 = w; a.qv1 = w + NOALLOC_MAX_NODES; a.qo0 = w + 2 * NOALLOC_MAX_NODES; a.qo1 = w + 3 * NOALLOC_MAX_NODES;
+    a.qb0 = w + 4 * NOALLOC_MAX_NODES; a.qb1 = w + 5 * NOALLOC_MAX_NODES;
+    w += 6 * (size_t)NOALLOC_MAX_NODES;
+    a.uf0 = w;
+    a.uf1 = w + NA_UCAP;
+    a.ctl = ctl;
+    a.cap = NOALLOC_MAX_NODES;
+    a.ucap = (uint32_t)NA_UCAP;
+    a.src = src;
+    a.iters = 8;
+    a.unit = 256 * a.iters;
+    a.scap = 256 * (a.iters + 1);
+    a.max_rounds = 4u * n + 4096u;
+    a.timeout_ns = 4000000000ull;
+    /* the control block must start at zero; the kernel clears the bitmap */
+    GGA_CK(cudaMemsetAsync(ctl, 0, sizeof(FrontierCtl), st));
+    gga_params p;
+    memset(&p, 0, sizeof p);
+    gga_status s = launch<256, false>(a, p, sms, st);
+    if (s) return s;
+    s = dev_wait(st, 60.0); /* bounded wait for the kernel */
+    if (s) return s;
+    uint32_t err = 0;
+    GGA_CK(cudaMemcpyAsync(&err, &ctl->err, sizeof err, cudaMemcpyDeviceToHost, st));
+    GGA_CK(cudaStreamSynchronize(st));
+    if (err == GGA_DEV_TIMEOUT) return gga_fail(GGA_ERR_TIMEOUT, "gga_bfs_noalloc: grid barrier timed out");
+    if (err != GGA_DEV_OK) return gga_fail(GGA_ERR_CUDA, "gga_bfs_noalloc: kernel error %u", err);
+    return GGA_OK;
+}

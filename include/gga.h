@@ -246,6 +246,24 @@ typedef struct gga_result_row {
 } gga_result_row;
 gga_status gga_write_result_row(const char *path, const gga_result_row *row);
 
+/* Allocation-free BFS (no counterpart in the reference, which allocates all
+ * of its device memory with cudaMalloc, graph.h:534-553).  For callers that
+ * must not allocate GPU memory while they traverse: code running inside a
+ * memory pool another framework owns, latency-critical paths where an
+ * allocation could synchronise the device, processes whose device memory is
+ * reserved up front.  Runs the frontier BFS of gga_bfs with its working
+ * memory in a fixed array the library reserves on each GPU it is loaded on
+ * (about 6.2 MiB, kept until exit).  Graphs up to 262,144 vertices and
+ * 8,388,608 edges; larger ones return GGA_ERR_TOO_LARGE.  Inputs and output
+ * are device pointers: d_offsets[n+1] and d_cols[m] a 0-based CSR, d_dist[n]
+ * BFS levels (GGA_INFINITY where unreached).  `stream` is a cudaStream_t
+ * (NULL = default stream) on the current device.  All calls share the one
+ * array: calls that overlap on the GPU race, so serialise them.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture begins. */
+gga_status gga_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_cols, uint32_t n, uint32_t m,
+                           uint32_t src, uint32_t *d_dist, void *stream);
+
 /* ---- batched queries ---------------------------------------------------- */
 
 /* Bit-packed multi-source BFS: nsrc <= 64 sources in one traversal (one
