@@ -201,11 +201,7 @@ gga_params ctx_default_params(const gga_graph *g) {
     memset(&p, 0, sizeof p);
     p.block_threads = 256;
     p.unit_iters = 8;
-    uint64_t wsum = 0;
-    const uint32_t stride = g->m > (1u << 20) ? g->m >> 20 : 1;
-    uint32_t cnt = 0;
-    for (uint32_t e = 0; e < g->m; e += stride, ++cnt) wsum += g->wt[e];
-    const double wavg = cnt ? (double)wsum / cnt : 1.0;
+    const double wavg = g->wavg > 0 ? g->wavg : 1.0; /* computed once when the graph is built */
     const double davg = g->n ? (double)g->m / g->n : 1.0;
     /* bucket width ~ a few average weights over the average degree */
     double delta = wavg * 8.0 / (davg > 1.0 ? davg : 1.0);

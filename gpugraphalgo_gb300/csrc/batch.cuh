@@ -1,0 +1,84 @@
+/*
+ * Batch engine interface (batch.cu): many queries in one persistent launch.
+ */
+#pragma once
+#include <vector>
+
+#include "ctx.cuh"
+
+/* One query as the batch kernel sees it (device memory). */
+struct MqQuery {
+    const uint32_t *off, *col, *wt; /* the graph's unsplit CSR (device) */
+    uint32_t *dist;                 /* n distances / levels */
+    uint32_t *aux;                  /* BFS: visited bitmap (n/32 words); SSSP: round stamps (n) */
+    uint32_t n, m;
+    uint32_t algo;        /* gga_algo */
+    uint32_t src;
+    uint32_t start_round; /* round in which the source is expanded */
+    uint32_t pad[3];
+};
+
+/* Control block of the batch kernel; persists across superstep launches
+ * (only the barrier is reset before each launch). */
+struct MqCtl {
+    GridBarrier bar;
+    uint32_t err;
+    uint32_t round;       /* next round to run */
+    uint32_t rounds_done; /* rounds run so far */
+    uint32_t pad0;
+    unsigned long long qctr[3]; /* (entries << 32) | edges, rotating by round */
+    uint32_t work[3];
+    uint32_t pad1;
+    unsigned long long edges_relaxed;
+};
+
+/* Device buffers of one batch engine. */
+struct MqEngine {
+    int device = -1;
+    uint32_t cap = 0;  /* queue entries (>= sum of admitted queries' n) */
+    uint32_t ucap = 0; /* unit boundaries (>= sum of m / unit + 4) */
+    uint32_t qcap = 0; /* query-table slots */
+    uint32_t *qq[2] = {}, *qv[2] = {}, *qo[2] = {}, *qb[2] = {}, *uf[2] = {};
+    MqQuery *qt = nullptr;    /* device query table */
+    MqQuery *qstage = nullptr; /* device staging for admitted records (qcap) */
+    uint32_t *list = nullptr; /* device index list for init / inject (qcap) */
+    uint32_t *active = nullptr; /* device per-query entry counts (qcap) */
+    MqCtl *ctl = nullptr;
+    MqCtl *hctl = nullptr;    /* pinned mirror */
+    uint32_t *hactive = nullptr; /* pinned mirror of active */
+    int nblocks = 0;
+    uint32_t rounds_done = 0;          /* rounds run since the last reset */
+    unsigned long long edges_relaxed = 0;
+};
+
+gga_status mq_engine_reserve(MqEngine *e, int device, uint32_t cap, uint64_t edges, uint32_t qcap);
+void mq_engine_free(MqEngine *e);
+/* Zeroes the control block (round 0, empty queues). */
+gga_status mq_engine_reset(MqEngine *e, cudaStream_t st);
+/* Uploads the n query records `host_q` into table slots `slots`, initialises
+ * their distance / visited state and injects their sources into the queue of
+ * the next round. */
+gga_status mq_engine_admit(MqEngine *e, const MqQuery *host_q, const uint32_t *slots, uint32_t n, cudaStream_t st);
+/* Runs at most max_rounds rounds (UINT32_MAX: until the queue drains) and
+ * waits for them; *rounds_run receives the rounds this launch ran. */
+gga_status mq_engine_run(MqEngine *e, uint32_t max_rounds, cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1,
+                         uint32_t *rounds_run, float *ms);
+/* Fills e->hactive[slot] with the queue entries each slot still has. */
+gga_status mq_engine_count(MqEngine *e, uint32_t nslots, cudaStream_t st);
+
+struct MsbfsScratch;
+
+/* Batch state owned by a context (created on first batched call). */
+struct BatchScratch {
+    MqEngine eng;
+    uint32_t *pool = nullptr; /* per-query dist + visited / stamp words */
+    size_t pool_words = 0;
+    MsbfsScratch *ms = nullptr;
+};
+
+BatchScratch *ctx_batch(gga_ctx *c);
+gga_status batch_pool_reserve(BatchScratch *b, size_t words);
+void msbfs_scratch_free(MsbfsScratch *m);
+/* Words of device state one query needs (dist + visited bits or stamps),
+ * each part rounded up to 64 words. */
+size_t mq_state_words(uint32_t n, uint32_t algo);

@@ -43,6 +43,7 @@ namespace {
 constexpr uint32_t NONE = 0xffffffffu;
 constexpr uint32_t MIN_UNIT = 512;  /* smallest edges-per-unit the buffers are sized for */
 constexpr uint32_t MAX_UNIT = 4096; /* largest edges-per-unit (shared-memory bound) */
+constexpr uint32_t STAGE_BATCH = 4; /* edge batches per thread between staging checkpoints */
 
 struct Args {
     const uint32_t *off, *col, *wt, *cc;
@@ -57,7 +58,7 @@ struct Args {
     uint32_t src;
     uint32_t unit;  /* edges per unit = BS * iters */
     uint32_t iters; /* CTA-wide iterations per unit */
-    uint32_t scap;  /* staging slots per CTA = BS * (iters + 1) */
+    uint32_t scap;  /* staging slots per CTA (>= BS * (STAGE_BATCH + 1)) */
     uint32_t delta;
     uint32_t nblocks;
     uint32_t max_rounds;
@@ -204,14 +205,16 @@ __device__ __forceinline__ void checkpoint(const Args &a, Ctrl &C, uint32_t *sv,
  * M_my_drelax does, cudaKernels.h:323-330); reports whether v joins the
  * near queue or the far pile (farval = its new distance). */
 template <bool SSSP>
-__device__ __forceinline__ void relax_edge(const Args &a, uint32_t v, uint32_t alt, uint32_t round, uint32_t thr,
-                                           bool &near, bool &far, uint32_t &farval) {
+__device__ __forceinline__ void relax_edge(const Args &a, uint32_t v, uint32_t alt, uint32_t probe, uint32_t round,
+                                           uint32_t thr, bool &near, bool &far, uint32_t &farval) {
+    /* probe: a recent read of the visited word (BFS) or of dist[v] (SSSP);
+     * it may be stale but never lower than the truth, so it only filters */
     near = false;
     far = false;
     farval = NONE;
     if (!SSSP) {
         const uint32_t bit = 1u << (v & 31);
-        if (!(__ldcg(a.bits + (v >> 5)) & bit)) {
+        if (!(probe & bit)) {
             const uint32_t old = atomicOr(a.bits + (v >> 5), bit);
             if (!(old & bit)) {
                 a.dist[v] = alt;
@@ -222,7 +225,7 @@ __device__ __forceinline__ void relax_edge(const Args &a, uint32_t v, uint32_t a
                 near = true;
             }
         }
-    } else if (alt < __ldcg(a.dist + v)) {
+    } else if (alt < probe) {
         const uint32_t old = atomicMin(a.dist + v, alt);
         if (alt < old) {
             if (a.cc) {
@@ -400,33 +403,55 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
                 if (SSSP) t_du[j] = __ldcg(a.dist + __ldcg(qv + i));
             }
             __syncthreads();
-            /* consecutive threads take consecutive edges of the unit */
-            for (uint32_t it = 0; it < a.iters; ++it) {
-                const uint32_t e = ebase + it * BS + tid;
-                if (e >= eend) continue;
-                uint32_t lo = 0, hi = cnt; /* last j with t_o[j] <= e */
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (t_o[mid] <= e) lo = mid; else hi = mid;
+            /* Consecutive threads take consecutive edges of the unit.  Each
+             * thread handles PB edges at a time in three passes (edge loads,
+             * then distance/bitmap probes, then updates), so PB independent
+             * memory chains are in flight per thread instead of one. */
+            constexpr uint32_t PB = STAGE_BATCH;
+            for (uint32_t it0 = 0; it0 < a.iters; it0 += PB) {
+                if (it0) checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fp, BS);
+                uint32_t v[PB], alt[PB], probe[PB];
+                bool act[PB];
+#pragma unroll
+                for (uint32_t q = 0; q < PB; ++q) {
+                    const uint32_t e = ebase + (it0 + q) * BS + tid;
+                    act[q] = it0 + q < a.iters && e < eend;
+                    v[q] = 0;
+                    alt[q] = 0;
+                    if (act[q]) {
+                        uint32_t lo = 0, hi = cnt; /* last j with t_o[j] <= e */
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (t_o[mid] <= e) lo = mid; else hi = mid;
+                        }
+                        const uint32_t ei = t_b[lo] + (e - t_o[lo]);
+                        if (ei < a.m) {
+                            v[q] = __ldg(a.col + ei);
+                            alt[q] = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
+                        } else { /* unreachable by construction; keeps reads in bounds */
+                            set_err(ctl, GGA_DEV_BAD_EDGE);
+                            act[q] = false;
+                        }
+                    }
                 }
-                const uint32_t ei = t_b[lo] + (e - t_o[lo]);
-                if (ei >= a.m) { /* unreachable by construction; keeps reads in bounds */
-                    set_err(ctl, GGA_DEV_BAD_EDGE);
-                    continue;
-                }
-                const uint32_t v = __ldg(a.col + ei);
-                const uint32_t alt = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
-                bool nr, fr;
-                uint32_t fv;
-                relax_edge<SSSP>(a, v, alt, round, thr, nr, fr, fv);
-                if (nr) {
-                    uint32_t b, dg;
-                    item_range(a, v, b, dg);
-                    if (dg) stage_near(a, C, sv, sb, sd, v, b, dg); /* nothing to expand otherwise */
-                }
-                if (SSSP && fv != NONE) {
-                    atomicMin(&C.fmin, fv);
-                    if (fr) stage_far(a, C, sf, v);
+#pragma unroll
+                for (uint32_t q = 0; q < PB; ++q)
+                    probe[q] = act[q] ? (SSSP ? __ldcg(a.dist + v[q]) : __ldcg(a.bits + (v[q] >> 5))) : 0u;
+#pragma unroll
+                for (uint32_t q = 0; q < PB; ++q) {
+                    if (!act[q]) continue;
+                    bool nr, fr;
+                    uint32_t fv;
+                    relax_edge<SSSP>(a, v[q], alt[q], probe[q], round, thr, nr, fr, fv);
+                    if (nr) {
+                        uint32_t b, dg;
+                        item_range(a, v[q], b, dg);
+                        if (dg) stage_near(a, C, sv, sb, sd, v[q], b, dg); /* nothing to expand otherwise */
+                    }
+                    if (SSSP && fv != NONE) {
+                        atomicMin(&C.fmin, fv);
+                        if (fr) stage_far(a, C, sf, v[q]);
+                    }
                 }
             }
             if (tid == 0) relaxed += eend - ebase;
@@ -550,7 +575,7 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     if (a.unit < MIN_UNIT || a.unit > MAX_UNIT)
         return gga_fail(GGA_ERR_INVALID_ARG, "block_threads x unit_iters = %u edges per unit, need %u..%u", a.unit,
                         MIN_UNIT, MAX_UNIT);
-    a.scap = bs * (a.iters + 1);
+    a.scap = bs * (STAGE_BATCH + 1); /* < BS staged after a checkpoint, + one batch */
     a.delta = p.sssp_delta;
     /* BFS needs at most n levels; near-far SSSP at most a level per
      * improvement, which the bound below leaves ample room for */

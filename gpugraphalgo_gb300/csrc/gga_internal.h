@@ -29,6 +29,7 @@ struct gga_graph {
     uint32_t *wt;   /* m */
     uint32_t maxdeg;
     uint32_t maxw;
+    double wavg;    /* mean edge weight (1 for an edgeless graph) */
     int symmetric;
 
     /* node split (graph.h:415-522); arrays live on the device */

@@ -102,10 +102,14 @@ void gga_graph_refresh_stats(gga_graph *g) {
         uint32_t d = g->off[u + 1] - g->off[u];
         if (d > md) md = d;
     }
-    for (uint32_t e = 0; e < g->m; ++e)
+    uint64_t ws = 0;
+    for (uint32_t e = 0; e < g->m; ++e) {
         if (g->wt[e] > mw) mw = g->wt[e];
+        ws += g->wt[e];
+    }
     g->maxdeg = md;
     g->maxw = mw;
+    g->wavg = g->m ? (double)ws / g->m : 1.0;
 }
 
 void gga_graph_free(gga_graph *g) {

@@ -1,0 +1,464 @@
+/*
+ * Bit-packed multi-source BFS: up to 64 BFS traversals of one graph in one
+ * persistent cooperative launch.
+ *
+ * Each vertex holds two 64-bit masks, one bit per source: `seen` (sources that
+ * have reached it) and `nxt` (sources reaching it in the level being built).
+ * A level is two grid-wide phases separated by grid barriers:
+ *
+ *   settle(L): every candidate vertex v (nxt[v] became non-zero during the
+ *     previous expand) takes its new bits f = nxt[v] & ~seen[v], records level
+ *     L for each set bit (dist[s * n + v] = L, source-major), folds f into
+ *     seen[v] and, if it has out-edges, is appended to the expansion list with
+ *     its frontier mask f and an exclusive edge offset (warp-aggregated 64-bit
+ *     atomicAdd of (entries << 32 | edges), so entry index and edge offset
+ *     grow together).
+ *   expand(L): the expansion list's edges are cut into fixed units of
+ *     MB_UNIT edges; CTAs take units by ticket, load the unit's entries into
+ *     shared memory and give one edge to each thread: for the edge (u, v) the
+ *     new sources are f_u & ~seen[v]; they are OR-ed into nxt[v] and the thread
+ *     whose OR found nxt[v] == 0 appends v to the next candidate list (staged
+ *     in shared memory, published at block-uniform checkpoints).
+ *
+ * One edge read serves every source whose frontier contains u, so a vertex
+ * reached by all 64 sources in the same level is expanded once instead of 64
+ * times.  Levels equal those of 64 single-source BFS runs (the reference's
+ * BFS levels, K/graph.h:115-149 serial and K/cudaKernels.h:285-344 device),
+ * on the unsplit graph: splitting a vertex does not change any level.
+ */
+#include <algorithm>
+#include <string.h>
+#include <vector>
+
+#include "batch.cuh"
+
+namespace {
+
+constexpr uint32_t MB_BS = 256;
+constexpr uint32_t MB_ITERS = 8;
+constexpr uint32_t MB_UNIT = MB_BS * MB_ITERS;
+constexpr uint32_t MB_BATCH = 4;
+constexpr uint32_t MB_SCAP = MB_BS * (MB_BATCH + 1);
+constexpr unsigned FULL = 0xffffffffu;
+
+struct MsCtl {
+    GridBarrier bar;
+    uint32_t err;
+    uint32_t levels;
+    uint32_t cand[2];               /* candidate counts, by level parity */
+    unsigned long long xctr[2];     /* (entries << 32) | edges of the expansion list, by parity */
+    uint32_t work[2];               /* unit tickets, by parity */
+    unsigned long long edges_relaxed;
+};
+
+struct MsArgs {
+    const uint32_t *off, *col;
+    uint32_t n, m;
+    unsigned long long *seen, *nxt; /* n each */
+    uint32_t *cand;                 /* n */
+    uint32_t *xv, *xo, *xb;         /* n each: vertex, edge offset, first edge */
+    unsigned long long *xf;         /* n: frontier mask of the entry */
+    uint32_t *uf;                   /* ucap: first entry of each unit */
+    uint32_t *dist;                 /* nsrc * n, source-major */
+    MsCtl *ctl;
+    uint32_t ucap, nblocks, max_levels;
+    unsigned long long timeout_ns;
+};
+
+struct MsCtrl {
+    uint32_t nn, base, unit, i0, cnt, ncand, nitems, total;
+};
+
+__device__ __forceinline__ void ms_err(MsCtl *c, uint32_t code) { atomicCAS(&c->err, GGA_DEV_OK, code); }
+
+__device__ __forceinline__ void ms_checkpoint(const MsArgs &a, MsCtrl &C, uint32_t *sc, uint32_t np,
+                                              uint32_t limit) {
+    __syncthreads();
+    const uint32_t nn = C.nn;
+    __syncthreads();
+    if (nn < limit || nn == 0) return;
+    if (threadIdx.x == 0) C.base = atomicAdd(&a.ctl->cand[np], nn);
+    __syncthreads();
+    const uint32_t base = C.base;
+    for (uint32_t j = threadIdx.x; j < nn; j += MB_BS) {
+        if (base + j < a.n) a.cand[base + j] = sc[j];
+        else ms_err(a.ctl, GGA_DEV_OVERFLOW);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) C.nn = 0;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
+    extern __shared__ unsigned long long dyn64[];
+    __shared__ MsCtrl C;
+    unsigned long long *t_f = dyn64;
+    uint32_t *t_o = (uint32_t *)(t_f + MB_UNIT + 1);
+    uint32_t *t_b = t_o + MB_UNIT + 1;
+    uint32_t *sc = t_b + MB_UNIT + 1;
+    MsCtl *ctl = a.ctl;
+    const uint32_t tid = threadIdx.x, lane = tid & 31;
+    const uint64_t gthreads = (uint64_t)gridDim.x * MB_BS;
+    uint32_t gen = 0;
+    unsigned long long relaxed = 0;
+    if (tid == 0) C.nn = 0;
+    __syncthreads();
+    uint32_t L = 0;
+    for (;; ++L) {
+        const uint32_t p = L & 1, np = p ^ 1;
+        /* ---------------- settle(L) */
+        if (tid == 0) C.ncand = min(ld_relaxed_u32(&ctl->cand[p]), a.n);
+        __syncthreads();
+        const uint32_t ncand = C.ncand;
+        __syncthreads();
+        if (ncand == 0) break; /* same decision in every block */
+        if (L >= a.max_levels) {
+            if (blockIdx.x == 0 && tid == 0) ms_err(ctl, GGA_DEV_ROUND_LIMIT);
+            break;
+        }
+        if (blockIdx.x == 0 && tid == 0) ctl->work[p] = 0;
+        /* warp-uniform trip count: every lane of a warp runs each iteration */
+        for (uint64_t base = (uint64_t)blockIdx.x * MB_BS + (tid & ~31u); base < ncand; base += gthreads) {
+            const uint64_t i = base + lane;
+            uint32_t v = 0, b = 0, d = 0;
+            unsigned long long f = 0;
+            if (i < ncand) {
+                v = __ldcg(a.cand + i);
+                const unsigned long long s0 = __ldcg(a.seen + v);
+                f = __ldcg(a.nxt + v) & ~s0;
+                a.nxt[v] = 0;
+                a.seen[v] = s0 | f;
+                for (unsigned long long mm = f; mm; mm &= mm - 1) {
+                    const uint32_t s = (uint32_t)__ffsll((long long)mm) - 1;
+                    a.dist[(size_t)s * a.n + v] = L;
+                }
+                b = __ldg(a.off + v);
+                d = f ? __ldg(a.off + v + 1) - b : 0u;
+            }
+            const unsigned has = __ballot_sync(FULL, d > 0);
+            uint32_t incl = d;
+#pragma unroll
+            for (int k = 1; k < 32; k <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, incl, k);
+                if (lane >= (uint32_t)k) incl += y;
+            }
+            const uint32_t wtot = __shfl_sync(FULL, incl, 31);
+            unsigned long long old = 0;
+            if (lane == 0 && has)
+                old = atomicAdd(&ctl->xctr[p], ((unsigned long long)__popc(has) << 32) | (unsigned long long)wtot);
+            old = __shfl_sync(FULL, old, 0);
+            if (d > 0) {
+                const uint32_t idx = (uint32_t)(old >> 32) + (uint32_t)__popc(has & lanemask_lt());
+                const uint32_t o = (uint32_t)old + incl - d;
+                if (idx < a.n) {
+                    a.xv[idx] = v;
+                    a.xo[idx] = o;
+                    a.xb[idx] = b;
+                    a.xf[idx] = f;
+                    for (uint64_t k = ((uint64_t)o + MB_UNIT - 1) / MB_UNIT; k * MB_UNIT < (uint64_t)o + d; ++k) {
+                        if (k < a.ucap) a.uf[k] = idx;
+                        else ms_err(ctl, GGA_DEV_OVERFLOW_UNITS);
+                    }
+                } else {
+                    ms_err(ctl, GGA_DEV_OVERFLOW);
+                }
+            }
+        }
+        if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+
+        /* ---------------- expand(L) */
+        if (tid == 0) {
+            const unsigned long long qc = ld_relaxed_u64(&ctl->xctr[p]);
+            const uint32_t ni = min((uint32_t)(qc >> 32), a.n);
+            C.nitems = ni;
+            C.total = ni ? (uint32_t)qc : 0u;
+        }
+        __syncthreads();
+        const uint32_t nitems = C.nitems, total = C.total;
+        const uint32_t units = min((uint32_t)(((uint64_t)total + MB_UNIT - 1) / MB_UNIT), a.ucap);
+        __syncthreads();
+        if (blockIdx.x == 0 && tid == 0) {
+            ctl->cand[p] = 0;  /* read at the start of settle(L), appended in expand(L+1) */
+            ctl->xctr[np] = 0; /* read in expand(L-1), appended in settle(L+1) */
+        }
+        for (;;) {
+            if (tid == 0) {
+                const uint32_t k = atomicAdd(&ctl->work[p], 1u);
+                C.unit = k;
+                if (k < units) {
+                    const uint32_t i0 = min(__ldcg(a.uf + k), nitems - 1);
+                    const uint32_t i1 = k + 1 < units ? min(__ldcg(a.uf + k + 1), nitems - 1) : nitems - 1;
+                    C.i0 = i0;
+                    C.cnt = i1 >= i0 ? min(i1 - i0 + 1, MB_UNIT + 1) : 1u;
+                }
+            }
+            __syncthreads();
+            const uint32_t k = C.unit;
+            if (k >= units) break;
+            const uint32_t i0 = C.i0, cnt = C.cnt;
+            const uint32_t ebase = k * MB_UNIT, eend = min(ebase + MB_UNIT, total);
+            for (uint32_t j = tid; j < cnt; j += MB_BS) {
+                t_o[j] = __ldcg(a.xo + i0 + j);
+                t_b[j] = __ldcg(a.xb + i0 + j);
+                t_f[j] = __ldcg(a.xf + i0 + j);
+            }
+            __syncthreads();
+            for (uint32_t it0 = 0; it0 < MB_ITERS; it0 += MB_BATCH) {
+                if (it0) ms_checkpoint(a, C, sc, np, MB_BS);
+#pragma unroll
+                for (uint32_t s = 0; s < MB_BATCH; ++s) {
+                    const uint32_t e = ebase + (it0 + s) * MB_BS + tid;
+                    if (e >= eend) continue;
+                    uint32_t lo = 0, hi = cnt;
+                    while (hi - lo > 1) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (t_o[mid] <= e) lo = mid; else hi = mid;
+                    }
+                    const uint32_t ei = t_b[lo] + (e - t_o[lo]);
+                    if (ei >= a.m) {
+                        ms_err(ctl, GGA_DEV_BAD_EDGE);
+                        continue;
+                    }
+                    const uint32_t v = __ldg(a.col + ei);
+                    const unsigned long long nb = t_f[lo] & ~__ldcg(a.seen + v);
+                    if (nb && (nb & ~__ldcg(a.nxt + v))) {
+                        if (atomicOr(a.nxt + v, nb) == 0) {
+                            const uint32_t slot = atomicAdd(&C.nn, 1u);
+                            if (slot < MB_SCAP) sc[slot] = v;
+                            else ms_err(ctl, GGA_DEV_OVERFLOW);
+                        }
+                    }
+                }
+            }
+            if (tid == 0) relaxed += eend - ebase;
+            ms_checkpoint(a, C, sc, np, MB_BS);
+        }
+        ms_checkpoint(a, C, sc, np, 1);
+        if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+    }
+    if (tid == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);
+    if (blockIdx.x == 0 && tid == 0) ctl->levels = L;
+}
+
+__global__ void k_ms_fill(uint32_t *p, size_t count, uint32_t value) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = value;
+}
+
+/* Level-0 candidates: each distinct source vertex once, carrying the bits of
+ * every source index that names it. */
+__global__ void k_ms_sources(MsArgs a, const uint32_t *srcs, uint32_t nsrc) {
+    const uint32_t s = threadIdx.x;
+    if (s >= nsrc) return;
+    const uint32_t v = srcs[s];
+    if (atomicOr(a.nxt + v, 1ull << s) == 0) {
+        const uint32_t idx = atomicAdd(&a.ctl->cand[0], 1u);
+        a.cand[idx] = v;
+    }
+}
+
+/* vertices_reached / edges_reached summed over the sources: popcount(seen). */
+__global__ void k_ms_reached(const unsigned long long *seen, const uint32_t *off, uint32_t n,
+                             unsigned long long *acc) {
+    unsigned long long vr = 0, er = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)__popcll(seen[v]);
+        vr += c;
+        er += (unsigned long long)c * (off[v + 1] - off[v]);
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        vr += __shfl_down_sync(FULL, vr, d);
+        er += __shfl_down_sync(FULL, er, d);
+    }
+    if ((threadIdx.x & 31) == 0 && (vr || er)) {
+        atomicAdd(acc, vr);
+        atomicAdd(acc + 1, er);
+    }
+}
+
+size_t ms_smem() { return (size_t)(MB_UNIT + 1) * 16 + (size_t)MB_SCAP * 4; }
+
+} // namespace
+
+struct MsbfsScratch {
+    int device = -1;
+    uint32_t ncap = 0, ucap = 0;
+    size_t dcap = 0;
+    unsigned long long *seen = nullptr, *nxt = nullptr, *xf = nullptr;
+    uint32_t *cand = nullptr, *xv = nullptr, *xo = nullptr, *xb = nullptr, *uf = nullptr;
+    uint32_t *dist = nullptr, *srcs = nullptr;
+    MsCtl *ctl = nullptr, *hctl = nullptr;
+    int nblocks = 0;
+};
+
+void msbfs_scratch_free(MsbfsScratch *m) {
+    if (!m) return;
+    cudaFree(m->seen);
+    cudaFree(m->nxt);
+    cudaFree(m->xf);
+    cudaFree(m->cand);
+    cudaFree(m->xv);
+    cudaFree(m->xo);
+    cudaFree(m->xb);
+    cudaFree(m->uf);
+    cudaFree(m->dist);
+    cudaFree(m->srcs);
+    cudaFree(m->ctl);
+    cudaFreeHost(m->hctl);
+    delete m;
+}
+
+static gga_status ms_reserve(MsbfsScratch *m, uint32_t n, uint32_t edges, size_t dist_words) {
+    cudaError_t e = cudaSuccess;
+    if (m->ncap < n) {
+        cudaFree(m->seen); cudaFree(m->nxt); cudaFree(m->xf);
+        cudaFree(m->cand); cudaFree(m->xv); cudaFree(m->xo); cudaFree(m->xb);
+        m->seen = m->nxt = m->xf = nullptr;
+        m->cand = m->xv = m->xo = m->xb = nullptr;
+        m->ncap = 0;
+        e = cudaMalloc((void **)&m->seen, (size_t)n * 8);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&m->nxt, (size_t)n * 8);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&m->xf, (size_t)n * 8);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&m->cand, (size_t)n * 4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&m->xv, (size_t)n * 4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&m->xo, (size_t)n * 4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&m->xb, (size_t)n * 4);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return gga_fail(GGA_ERR_CUDA, "msbfs scratch (%u vertices): %s", n, cudaGetErrorString(e));
+        }
+        m->ncap = n;
+    }
+    const uint32_t ucap = edges / MB_UNIT + 4;
+    if (m->ucap < ucap) {
+        cudaFree(m->uf);
+        m->uf = nullptr;
+        m->ucap = 0;
+        GGA_CK(cudaMalloc((void **)&m->uf, (size_t)ucap * 4));
+        m->ucap = ucap;
+    }
+    if (m->dcap < dist_words) {
+        cudaFree(m->dist);
+        m->dist = nullptr;
+        m->dcap = 0;
+        e = cudaMalloc((void **)&m->dist, dist_words * 4);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return gga_fail(GGA_ERR_CUDA, "msbfs levels (%zu MiB): %s", (dist_words * 4) >> 20,
+                            cudaGetErrorString(e));
+        }
+        m->dcap = dist_words;
+    }
+    if (!m->ctl) {
+        GGA_CK(cudaMalloc((void **)&m->ctl, sizeof(MsCtl)));
+        GGA_CK(cudaMallocHost((void **)&m->hctl, sizeof(MsCtl)));
+        GGA_CK(cudaMalloc((void **)&m->srcs, 64 * sizeof(uint32_t)));
+    }
+    if (!m->nblocks) {
+        const size_t smem = ms_smem();
+        GGA_CK(cudaFuncSetAttribute(k_msbfs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int occ = 0, sms = 0;
+        GGA_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_msbfs, MB_BS, smem));
+        GGA_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device));
+        if (occ <= 0) return gga_fail(GGA_ERR_CUDA, "msbfs kernel: zero occupancy");
+        m->nblocks = occ * sms;
+    }
+    return GGA_OK;
+}
+
+gga_status gga_msbfs(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *srcs, uint32_t *dist_out,
+                     gga_stats *stats) {
+    const double t0 = gga_now_ms();
+    if (!c || !g || !srcs || !dist_out) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    if (nsrc == 0 || nsrc > 64) return gga_fail(GGA_ERR_INVALID_ARG, "nsrc %u (1..64)", nsrc);
+    for (uint32_t i = 0; i < nsrc; ++i)
+        if (srcs[i] >= g->n) return gga_fail(GGA_ERR_INVALID_ARG, "source %u >= %u vertices", srcs[i], g->n);
+    std::lock_guard<std::mutex> lk(c->mu);
+    gga_status s;
+    if ((s = ctx_activate(c))) return s;
+    if ((s = dev_graph_ensure(g, c->device, c->st))) return s;
+    const DevGraph *d = dev_graph_of(g);
+    BatchScratch *b = ctx_batch(c);
+    if (!b) return gga_fail(GGA_ERR_NO_MEMORY, "batch scratch");
+    if (!b->ms) {
+        b->ms = new (std::nothrow) MsbfsScratch();
+        if (!b->ms) return gga_fail(GGA_ERR_NO_MEMORY, "msbfs scratch");
+        b->ms->device = c->device;
+    }
+    MsbfsScratch *m = b->ms;
+    const bool dev_out = ptr_is_device(dist_out);
+    const size_t words = (size_t)nsrc * d->n;
+    if ((s = ms_reserve(m, d->n, d->m, dev_out ? 0 : words))) return s;
+    uint32_t *levels = dev_out ? dist_out : m->dist;
+
+    MsArgs a;
+    memset(&a, 0, sizeof a);
+    a.off = d->off;
+    a.col = d->col;
+    a.n = d->n;
+    a.m = d->m;
+    a.seen = m->seen;
+    a.nxt = m->nxt;
+    a.cand = m->cand;
+    a.xv = m->xv;
+    a.xo = m->xo;
+    a.xb = m->xb;
+    a.xf = m->xf;
+    a.uf = m->uf;
+    a.dist = levels;
+    a.ctl = m->ctl;
+    a.ucap = m->ucap;
+    a.nblocks = (uint32_t)m->nblocks;
+    a.max_levels = d->n + 1;
+    a.timeout_ns = 4000000000ull;
+
+    GGA_CK(cudaMemsetAsync(m->ctl, 0, sizeof(MsCtl), c->st));
+    GGA_CK(cudaMemsetAsync(m->seen, 0, (size_t)d->n * 8, c->st));
+    GGA_CK(cudaMemsetAsync(m->nxt, 0, (size_t)d->n * 8, c->st));
+    GGA_CK(cudaMemcpyAsync(m->srcs, srcs, nsrc * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
+    k_ms_fill<<<ctx_grid(c, words, 256), 256, 0, c->st>>>(levels, words, GGA_INFINITY);
+    k_ms_sources<<<1, 64, 0, c->st>>>(a, m->srcs, nsrc);
+    GGA_CK(cudaGetLastError());
+    GGA_CK(cudaEventRecord(c->ev[0], c->st));
+    void *args[] = {&a};
+    GGA_CK(cudaLaunchCooperativeKernel((const void *)k_msbfs, dim3(a.nblocks), dim3(MB_BS), args, ms_smem(), c->st));
+    GGA_CK(cudaEventRecord(c->ev[1], c->st));
+    GGA_CK(cudaMemcpyAsync(m->hctl, m->ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, c->st));
+    uint32_t launches = 4;
+    if (!dev_out) GGA_CK(cudaMemcpyAsync(dist_out, levels, words * 4, cudaMemcpyDeviceToHost, c->st));
+    if (stats) {
+        unsigned long long *acc = (unsigned long long *)(c->dflag + 32);
+        GGA_CK(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), c->st));
+        k_ms_reached<<<ctx_grid(c, d->n, 256), 256, 0, c->st>>>(m->seen, d->off, d->n, acc);
+        GGA_CK(cudaGetLastError());
+        GGA_CK(cudaMemcpyAsync(c->hflag + 32, acc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+        launches++;
+    }
+    if ((s = dev_wait(c->st, 60.0))) return s;
+    const MsCtl &h = *m->hctl;
+    switch (h.err) {
+    case GGA_DEV_OK: break;
+    case GGA_DEV_TIMEOUT: return gga_fail(GGA_ERR_TIMEOUT, "msbfs grid barrier timed out");
+    case GGA_DEV_OVERFLOW: return gga_fail(GGA_ERR_CUDA, "msbfs list overflow (internal error)");
+    case GGA_DEV_OVERFLOW_UNITS: return gga_fail(GGA_ERR_CUDA, "msbfs unit table overflow (internal error)");
+    case GGA_DEV_BAD_EDGE: return gga_fail(GGA_ERR_CUDA, "msbfs edge index out of range (internal error)");
+    case GGA_DEV_ROUND_LIMIT: return gga_fail(GGA_ERR_CUDA, "msbfs level limit reached (internal error)");
+    default: return gga_fail(GGA_ERR_CUDA, "msbfs kernel error %u", h.err);
+    }
+    if (stats) {
+        gga_stats st;
+        memset(&st, 0, sizeof st);
+        float ms = 0;
+        GGA_CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+        const unsigned long long *hr = (const unsigned long long *)(c->hflag + 32);
+        st.iterations = h.levels;
+        st.kernel_launches = launches;
+        st.edges_relaxed = h.edges_relaxed;
+        st.vertices_reached = hr[0];
+        st.edges_reached = hr[1];
+        st.kernel_ms = ms;
+        st.total_ms = gga_now_ms() - t0;
+        *stats = st;
+    }
+    return GGA_OK;
+}

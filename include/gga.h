@@ -32,7 +32,7 @@ extern "C" {
 
 #define GGA_INFINITY 1000000000u /* MYINFINITY, bfs_sssp.cu:53 / graph.h:96 */
 #define GGA_MSBFS_MAX_SOURCES 64 /* one uint64 lane word per vertex */
-#define GGA_SSSP_BATCH_MAX_SOURCES 32 /* one warp lane per source */
+#define GGA_SSSP_BATCH_MAX_SOURCES 32
 /* Largest edge weight for which dist + weight cannot wrap in uint32 while
  * dist <= GGA_INFINITY; heavier weights are rejected (the reference's unsigned
  * arithmetic would wrap, bfs_sssp.cu/cudaKernels.h:323). */
@@ -267,11 +267,15 @@ gga_status gga_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_cols, ui
 /* ---- batched queries ---------------------------------------------------- */
 
 /* Bit-packed multi-source BFS: nsrc <= 64 sources in one traversal (one
- * uint64 lane word per vertex).  dist_out: nsrc x nodes_orig, source-major. */
+ * uint64 mask per vertex; an edge read serves every source whose frontier
+ * holds its tail).  Levels equal nsrc single-source gga_bfs runs on the
+ * unsplit graph.  dist_out: nsrc x nodes_orig, source-major, host or device.
+ * stats: iterations = levels, vertices/edges_reached summed over sources. */
 gga_status gga_msbfs(gga_ctx *ctx, gga_graph *g, uint32_t nsrc, const uint32_t *srcs,
                      uint32_t *dist_out, gga_stats *stats);
-/* Batched SSSP: nsrc <= 32 sources, one warp lane per source.
- * dist_out: nsrc x nodes_orig, source-major. */
+/* Batched SSSP: nsrc <= 32 sources of one graph in one launch of the batch
+ * engine (as gga_multi_solve).  dist_out: nsrc x nodes_orig, source-major,
+ * host or device. */
 gga_status gga_sssp_batch(gga_ctx *ctx, gga_graph *g, uint32_t nsrc, const uint32_t *srcs,
                           uint32_t *dist_out, gga_stats *stats);
 
@@ -282,7 +286,11 @@ typedef struct gga_query {
     uint32_t src;
     uint32_t *dist_out; /* host or device, nodes_orig entries */
 } gga_query;
-/* Runs nq queries over any mix of graphs in one persistent launch. */
+/* Runs nq queries over any mix of graphs in one persistent launch: queue
+ * entries carry their query, so edge-balanced work units are cut from all
+ * queries' frontiers at once and a round costs one grid barrier for the
+ * whole batch.  Each result equals the single-source answer (unsplit CSR).
+ * stats: iterations = rounds, vertices/edges_reached summed over queries. */
 gga_status gga_multi_solve(gga_ctx *ctx, uint32_t nq, const gga_query *queries, gga_stats *stats);
 
 /* ---- serving ------------------------------------------------------------ */
@@ -295,9 +303,13 @@ typedef struct gga_server_stats {
     uint64_t state_bytes_peak; /* peak per-query device state admitted */
 } gga_server_stats;
 
-/* Starts a request loop over resident graphs; per-query device state
- * (distances, frontiers) is admitted against mem_cap_bytes; at most
- * max_slots queries share the device at once. */
+/* Starts a request loop (own thread and stream) over resident graphs:
+ * continuous batching on the batch engine in supersteps of a few rounds;
+ * finished queries retire and waiting ones join between supersteps.  All
+ * device memory (queues, per-query distances and visited/stamp words) is
+ * reserved here from mem_cap_bytes; a query whose state can never fit is
+ * rejected with GGA_ERR_ADMISSION at submit, others wait for room.  At most
+ * max_slots queries are in flight at once. */
 gga_status gga_server_create(gga_ctx *ctx, uint32_t ngraphs, gga_graph *const *graphs,
                              uint64_t mem_cap_bytes, uint32_t max_slots, gga_server **out);
 /* Queues a query; returns at once with a ticket.  dist_out (host) must stay
@@ -305,10 +317,13 @@ gga_status gga_server_create(gga_ctx *ctx, uint32_t ngraphs, gga_graph *const *g
 gga_status gga_server_submit(gga_server *s, uint32_t graph_index, gga_algo algo, uint32_t src,
                              uint32_t *dist_out, uint64_t *ticket);
 /* Waits up to timeout_ms (0 = poll) for a ticket; latency_us = completion -
- * submission.  GGA_ERR_NOT_READY if still running. */
+ * submission.  GGA_ERR_NOT_READY if still running.  A ticket is consumed by
+ * the wait that returns its result. */
 gga_status gga_server_wait(gga_server *s, uint64_t ticket, uint32_t timeout_ms,
                            double *latency_us);
 gga_status gga_server_get_stats(gga_server *s, gga_server_stats *st);
+/* Stops the loop after the current superstep; queries still queued or in
+ * flight are dropped (their buffers are not written after this returns). */
 void gga_server_destroy(gga_server *s);
 
 #ifdef __cplusplus
