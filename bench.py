@@ -62,6 +62,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--autotune-trials", type=int, default=1)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-query and serving sections")
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="offered-load duration per Poisson rate")
     return ap.parse_args()
 
 
@@ -247,6 +249,185 @@ def run_reference(args, dist: Dist):
     }
 
 
+# ------------------------------------------------------------ batching / serving
+
+def _timed(fn, reps):
+    best = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        r = fn()
+        best.append(time.perf_counter() - t0)
+    return r, statistics.median(best)
+
+
+def batch_section(gga, ctx):
+    """Batched queries in one launch against the same queries one at a time.
+
+    Both sides copy every distance vector to host memory (the user-facing
+    call); kernel-only rates come from the library's CUDA events."""
+    res = {}
+    g = gga.Graph.rmat(20, 16, 0.57, 0.19, 0.19, seed=4, wmin=1, wmax=255)
+    g.cudaCopy(ctx)
+    rng = np.random.default_rng(4)
+    cand = np.nonzero(g.degrees() > 0)[0]
+    s64 = [int(x) for x in rng.choice(cand, 64, replace=False)]
+    s32 = s64[:32]
+
+    def singles(qs):
+        outs, kms = [], 0.0
+        t0 = time.perf_counter()
+        for gg, algo, s in qs:
+            o, st = ctx.solve(gg, algo, s, stats=True)
+            outs.append(o)
+            kms += st["kernel_ms"]
+        return outs, time.perf_counter() - t0, kms
+
+    def record(name, nq, batch_out, bst, bwall, single_outs, swall, skms, er):
+        same = all(np.array_equal(a, b) for a, b in zip(batch_out, single_outs))
+        res[name] = {"queries": nq, "identical_to_single": bool(same),
+                     "batch_qps": nq / bwall, "one_at_a_time_qps": nq / swall, "speedup": swall / bwall,
+                     "batch_kernel_ms": bst["kernel_ms"], "one_at_a_time_kernel_ms": skms,
+                     "kernel_speedup": skms / bst["kernel_ms"] if bst["kernel_ms"] else None,
+                     "batch_ms": bwall * 1e3, "gteps_kernel": er / (bst["kernel_ms"] * 1e-3) / 1e9 if bst["kernel_ms"] else None,
+                     "rounds": bst["iterations"], "edges_relaxed": bst["edges_relaxed"], "edges_reached": er}
+
+    ctx.msbfs(g, s64)
+    (bo, bst), bw = _timed(lambda: ctx.msbfs(g, s64, stats=True), 3)
+    so, sw, sk = singles([(g, "bfs", s) for s in s64])
+    record("msbfs64_rmat20", 64, list(bo), bst, bw, so, sw, sk, bst["edges_reached"])
+
+    ctx.sssp_batch(g, s32)
+    (bo, bst), bw = _timed(lambda: ctx.sssp_batch(g, s32, stats=True), 3)
+    so, sw, sk = singles([(g, "sssp", s) for s in s32])
+    record("sssp32_rmat20", 32, list(bo), bst, bw, so, sw, sk, bst["edges_reached"])
+
+    gs = [gga.Graph.rmat(sc, 16, 0.57, 0.19, 0.19, seed=10 + i, wmin=1, wmax=255) for i, sc in enumerate(range(12, 21))]
+    gs += [gga.Graph.grid(w, w, 0.05, 0.001, seed=19 + i, wmin=1, wmax=1000)
+           for i, w in enumerate((256, 512, 768, 1024, 1280, 1536, 2048))]
+    qs = []
+    for j, gg in enumerate(gs):
+        gg.cudaCopy(ctx)
+        r = np.random.default_rng(100 + j)
+        for s in r.choice(np.nonzero(gg.degrees() > 0)[0], 8, replace=False):
+            qs += [(gg, "bfs", int(s)), (gg, "sssp", int(s))]
+    ctx.multi_solve(qs)
+    (bo, bst), bw = _timed(lambda: ctx.multi_solve(qs, stats=True), 3)
+    so, sw, sk = singles(qs)
+    record("mixed16x8_bfs+sssp", len(qs), bo, bst, bw, so, sw, sk, bst["edges_reached"])
+    res["mixed16x8_bfs+sssp"]["graphs"] = "R-MAT 12..20 ef16 seeds 10-18, grids 256..2048 seeds 19-25"
+    return res
+
+
+def serving_section(gga, ctx, seconds: float, device: int):
+    """Open-loop Poisson query streams against the continuous-batching server."""
+    import torch
+
+    specs = [("rmat", 16, 30), ("rmat", 18, 31), ("rmat", 20, 32), ("rmat", 21, 33),
+             ("grid", 512, 34), ("grid", 1024, 35), ("grid", 1536, 36), ("grid", 2048, 37)]
+    graphs = []
+    for kind, size, seed in specs:
+        if kind == "rmat":
+            gg = gga.Graph.rmat(size, 16, 0.57, 0.19, 0.19, seed=seed, wmin=1, wmax=255)
+        else:
+            gg = gga.Graph.grid(size, size, 0.05, 0.001, seed=seed, wmin=1, wmax=1000)
+        gg.cudaCopy(ctx)
+        graphs.append(gg)
+    ns = [gg.n for gg in graphs]
+    W = 512
+    ring = torch.empty((W, max(ns)), dtype=torch.int32, device=f"cuda:{device}")
+    rng = np.random.default_rng(77)
+
+    def draw(k):
+        gi = rng.integers(0, len(graphs), k)
+        al = np.where(rng.random(k) < 0.7, "bfs", "sssp")
+        src = [int(rng.integers(0, ns[i])) for i in gi]
+        return list(zip(gi.tolist(), al.tolist(), src))
+
+    # sequential plain launches, one query at a time, same mix, device outputs
+    seq = draw(300)
+    for gi, al, s in seq[:20]:
+        ctx.solve(graphs[gi], al, s, out=ring[0][: ns[gi]])
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for k, (gi, al, s) in enumerate(seq):
+        ctx.solve(graphs[gi], al, s, out=ring[k % W][: ns[gi]])
+    ctx.synchronize()
+    seq_qps = len(seq) / (time.perf_counter() - t0)
+
+    srv = gga.Server(ctx, graphs, mem_cap_bytes=60 << 30, max_slots=256)
+    old_switch = sys.getswitchinterval()
+    sys.setswitchinterval(0.0002)  # the submitting and the waiting thread share the GIL
+    out = {"graphs": "R-MAT 16/18/20/21 ef16 seeds 30-33, grids 512/1024/1536/2048 seeds 34-37 (5% deleted, w 1..1000)",
+           "mix": "70% BFS / 30% SSSP, uniform graph and source", "mem_cap_bytes": 60 << 30, "max_slots": 256,
+           "superstep_rounds": 8, "sequential_qps": seq_qps, "rates": []}
+    try:
+        # exactness: served answers equal single-query answers
+        chk = draw(24)
+        tk = [srv.submit(gi, al, s) for gi, al, s in chk]
+        mism = 0
+        for (gi, al, s), t in zip(chk, tk):
+            got, _ = srv.wait(t)
+            mism += int(not np.array_equal(got, ctx.solve(graphs[gi], al, s)))
+        out["identical_to_single"] = mism == 0
+        for rate in (1000, 5000, 20000, 50000):
+            nq = max(50, int(rate * seconds))
+            qs = draw(nq)
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, nq))
+            free = list(range(W))
+            lock = threading.Condition()
+            pending = []  # (ticket, slot, scheduled arrival, submit time)
+            lat = []
+            done_t = [0.0]
+
+            def consumer():
+                k = 0
+                while k < nq:
+                    with lock:
+                        while not pending:
+                            lock.wait()
+                        t, slot, arr, sub = pending.pop(0)
+                    _, l_us = srv.wait(t, 120000)
+                    fin = sub + l_us * 1e-6
+                    lat.append(fin - arr)
+                    done_t[0] = max(done_t[0], fin)
+                    with lock:
+                        free.append(slot)
+                        lock.notify_all()
+                    k += 1
+
+            th = threading.Thread(target=consumer)
+            th.start()
+            throttled = 0
+            base = time.perf_counter()
+            for (gi, al, s), a in zip(qs, arrivals):
+                when = base + a
+                while time.perf_counter() < when:
+                    pass
+                with lock:
+                    if not free:
+                        throttled += 1
+                        while not free:
+                            lock.wait()
+                    slot = free.pop()
+                sub = time.perf_counter()
+                t = srv.submit(gi, al, s, out=ring[slot][: ns[gi]])
+                with lock:
+                    pending.append((t, slot, when, sub))
+                    lock.notify_all()
+            th.join()
+            span = done_t[0] - base
+            lat_ms = np.array(lat) * 1e3
+            out["rates"].append({"offered_qps": rate, "queries": nq, "achieved_qps": nq / span,
+                                 "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+                                 "throttled_submits": throttled, "window": W})
+        out["stats"] = srv.stats()
+        out["peak_qps_vs_sequential"] = max(r["achieved_qps"] for r in out["rates"]) / seq_qps
+    finally:
+        sys.setswitchinterval(old_switch)
+        srv.close()
+    return out
+
+
 def run_gga(args, dist: Dist):
     import gpugraphalgo_gb300 as gga
 
@@ -382,6 +563,16 @@ def run_gga(args, dist: Dist):
                       "d2h_bytes_per_step": 4 * info["nodes_orig"] * 2 * len(srcs),
                       "steps": e2e_steps}
         g.cudaCopy(ctx)
+
+    if not args.no_batch and dist.rank == 0:
+        try:
+            out["batched"] = batch_section(gga, ctx)
+        except Exception as e:  # reported, not fatal
+            out["batched"] = {"error": repr(e)}
+        try:
+            out["serving"] = serving_section(gga, ctx, args.serve_seconds, dist.local_rank)
+        except Exception as e:
+            out["serving"] = {"error": repr(e)}
 
     if dist.rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

@@ -341,6 +341,24 @@ class Context:
     def sssp(self, graph: Graph, src: int, variant="auto", **kw):
         return self.solve(graph, SSSP, src, variant, **kw)
 
+    def trace(self, enable: bool = True):
+        """Record per-round frontier records and per-CTA busy kilocycles of the
+        following frontier-engine solves (cudaKernels.h:1-70's clock64
+        histogram and convergence.h's per-iteration log, on device counters)."""
+        _check(N.load().gga_trace_enable(self._h, 1 if enable else 0), "trace_enable")
+
+    def last_trace(self) -> dict:
+        nr, nb = C.c_uint32(), C.c_uint32()
+        _check(N.load().gga_trace_get(self._h, None, 0, C.byref(nr), None, 0, C.byref(nb)), "trace_get")
+        rounds = (N.RoundTrace * max(1, nr.value))()
+        cta = np.zeros(max(1, nb.value), np.uint32)
+        _check(N.load().gga_trace_get(self._h, rounds, nr.value, C.byref(nr),
+                                      cta.ctypes.data_as(C.POINTER(C.c_uint32)), nb.value, C.byref(nb)), "trace_get")
+        kinds = ("near", "bottom_up", "far", "heavy")
+        return {"rounds": [{"kind": kinds[r.kind] if r.kind < 4 else r.kind, "items": r.items, "edges": r.edges,
+                            "far_items": r.far_items} for r in rounds[: nr.value]],
+                "cta_kcycles": cta[: nb.value]}
+
     def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False):
         s = np.ascontiguousarray(srcs, dtype=np.uint32)
         out = np.empty((len(s), graph.n), np.uint32)
@@ -379,10 +397,14 @@ class Server:
         _check(N.load().gga_server_create(ctx.handle, len(graphs), arr, mem_cap_bytes, max_slots, C.byref(self._h)), "server_create")
         self._outs = {}
 
-    def submit(self, graph_index: int, algo, src: int) -> int:
-        out = np.empty(self._graphs[graph_index].n, np.uint32)
+    def submit(self, graph_index: int, algo, src: int, out=None) -> int:
+        """Queues one query; `out` (numpy array or an object with data_ptr(),
+        e.g. a CUDA tensor) receives the distances, else a new host array."""
+        if out is None:
+            out = np.empty(self._graphs[graph_index].n, np.uint32)
+        ptr = C.c_void_p(out.data_ptr()) if hasattr(out, "data_ptr") else _ptr(out)
         t = C.c_uint64()
-        _check(N.load().gga_server_submit(self._h, graph_index, _algo(algo), src, _ptr(out), C.byref(t)), "server_submit")
+        _check(N.load().gga_server_submit(self._h, graph_index, _algo(algo), src, ptr, C.byref(t)), "server_submit")
         self._outs[t.value] = out
         return t.value
 

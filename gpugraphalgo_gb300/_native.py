@@ -55,6 +55,10 @@ class GraphInfo(C.Structure):
     ]
 
 
+class RoundTrace(C.Structure):
+    _fields_ = [("kind", u32), ("items", u32), ("edges", u32), ("far_items", u32)]
+
+
 class Params(C.Structure):
     _fields_ = [
         ("block_threads", u32),
@@ -67,6 +71,10 @@ class Params(C.Structure):
         ("cdp_mode", u32),
         ("cdp_pending_limit", u32),
         ("skip_reached", u32),
+        ("bfs_direction", u32),
+        ("bfs_alpha", u32),
+        ("bfs_beta", u32),
+        ("sssp_light_heavy", u32),
     ]
 
     def as_dict(self):
@@ -157,6 +165,8 @@ SIGNATURES = {
     "gga_server_wait": (C.c_int, [P, u64, u32, C.POINTER(C.c_double)]),
     "gga_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
     "gga_server_destroy": (None, [P]),
+    "gga_trace_enable": (C.c_int, [P, C.c_int]),
+    "gga_trace_get": (C.c_int, [P, C.POINTER(RoundTrace), u32, C.POINTER(u32), C.POINTER(u32), u32, C.POINTER(u32)]),
 }
 
 _lib = None

@@ -200,7 +200,7 @@ gga_params ctx_default_params(const gga_graph *g) {
     gga_params p;
     memset(&p, 0, sizeof p);
     p.block_threads = 256;
-    p.unit_iters = 8;
+    p.unit_iters = 0; /* per algorithm: 8 for BFS, 4 for SSSP */
     const double wavg = g->wavg > 0 ? g->wavg : 1.0; /* computed once when the graph is built */
     const double davg = g->n ? (double)g->m / g->n : 1.0;
     /* bucket width ~ a few average weights over the average degree */
@@ -324,11 +324,34 @@ gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_
 
     if (variant == GGA_VARIANT_AUTO || variant == GGA_VARIANT_FRONTIER) {
         const bool use_split = split && p.use_split;
-        const GraphView v = dev_graph_view(d, use_split);
+        if (!sssp && !use_split && p.bfs_direction == 0 && d->symmetric == 0 &&
+            (s = dev_graph_check_symmetric(g, c->dflag + 40, c->hflag + 40, c->st)))
+            return s;
+        GraphView v = dev_graph_view(d, use_split);
+        const uint32_t *light = nullptr;
+        if (sssp && !use_split && p.sssp_delta && p.sssp_light_heavy == 0) {
+            if ((s = dev_graph_light_heavy(g, p.sssp_delta, c->st))) return s;
+            v.col = d->lcol;
+            v.wt = d->lwt;
+            light = d->light;
+        }
         if ((s = frontier_scratch_ensure(&c->fs, v.n > d->n ? v.n : d->n, d->m))) return s;
         FrontierResult r;
-        s = frontier_run(&c->fs, v, use_split ? d->first : nullptr, src, sssp, p, c->sms, c->st, c->ev[0], c->ev[1], &r);
+        s = frontier_run(&c->fs, v, use_split ? d->first : nullptr, src, sssp, p, c->sms, c->st, c->ev[0], c->ev[1], &r,
+                         c->trace_on, light);
         if (s) return s;
+        if (c->trace_on) {
+            const uint32_t nr = r.rounds < TRACE_ROUNDS ? r.rounds : TRACE_ROUNDS;
+            const uint32_t nb = r.nblocks < TRACE_MAX_CTAS ? r.nblocks : TRACE_MAX_CTAS;
+            c->trace_rounds.assign((size_t)nr * 4, 0);
+            c->trace_cta.assign(nb, 0);
+            if (nr)
+                GGA_CK(cudaMemcpyAsync(c->trace_rounds.data(), c->fs.trace, (size_t)nr * 16, cudaMemcpyDeviceToHost, c->st));
+            if (nb)
+                GGA_CK(cudaMemcpyAsync(c->trace_cta.data(), c->fs.trace + (size_t)TRACE_ROUNDS * 4, (size_t)nb * 4,
+                                       cudaMemcpyDeviceToHost, c->st));
+            GGA_CK(cudaStreamSynchronize(c->st));
+        }
         st.iterations = r.rounds;
         st.kernel_launches = r.launches;
         st.edges_relaxed = r.edges_relaxed;
@@ -392,6 +415,34 @@ gga_status gga_bfs(gga_ctx *c, gga_graph *g, uint32_t src, gga_variant variant, 
 
 gga_status gga_sssp(gga_ctx *c, gga_graph *g, uint32_t src, gga_variant variant, uint32_t *dist_out, gga_stats *stats) {
     return gga_solve(c, g, GGA_SSSP, src, variant, dist_out, stats);
+}
+
+/* ------------------------------------------------------------ instrumentation */
+
+gga_status gga_trace_enable(gga_ctx *c, int enable) {
+    if (!c) return gga_fail(GGA_ERR_INVALID_ARG, "NULL context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->trace_on = enable != 0;
+    return GGA_OK;
+}
+
+gga_status gga_trace_get(gga_ctx *c, gga_round_trace *rounds, uint32_t cap, uint32_t *nrounds,
+                         uint32_t *cta_kcycles, uint32_t cta_cap, uint32_t *ncta) {
+    if (!c) return gga_fail(GGA_ERR_INVALID_ARG, "NULL context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    const uint32_t nr = (uint32_t)(c->trace_rounds.size() / 4), nb = (uint32_t)c->trace_cta.size();
+    if (nrounds) *nrounds = nr;
+    if (ncta) *ncta = nb;
+    if (rounds)
+        for (uint32_t i = 0; i < nr && i < cap; ++i) {
+            rounds[i].kind = c->trace_rounds[4 * i];
+            rounds[i].items = c->trace_rounds[4 * i + 1];
+            rounds[i].edges = c->trace_rounds[4 * i + 2];
+            rounds[i].far_items = c->trace_rounds[4 * i + 3];
+        }
+    if (cta_kcycles)
+        for (uint32_t i = 0; i < nb && i < cta_cap; ++i) cta_kcycles[i] = c->trace_cta[i];
+    return GGA_OK;
 }
 
 /* ------------------------------------------------------------ autotune */

@@ -539,6 +539,7 @@ void ctx_batch_release(gga_ctx *c) {
     mq_engine_free(&c->batch->eng);
     cudaFree(c->batch->pool);
     msbfs_scratch_free(c->batch->ms);
+    su_scratch_free(c->batch->su);
     delete c->batch;
     c->batch = nullptr;
 }
@@ -635,16 +636,3 @@ gga_status gga_multi_solve(gga_ctx *c, uint32_t nq, const gga_query *queries, gg
     return GGA_OK;
 }
 
-gga_status gga_sssp_batch(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *srcs, uint32_t *dist_out,
-                          gga_stats *stats) {
-    if (!c || !g || !srcs || !dist_out) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
-    if (nsrc == 0 || nsrc > 32) return gga_fail(GGA_ERR_INVALID_ARG, "nsrc %u (1..32)", nsrc);
-    std::vector<gga_query> q(nsrc);
-    for (uint32_t i = 0; i < nsrc; ++i) {
-        q[i].graph = g;
-        q[i].algo = GGA_SSSP;
-        q[i].src = srcs[i];
-        q[i].dist_out = dist_out + (size_t)i * g->n;
-    }
-    return gga_multi_solve(c, nsrc, q.data(), stats);
-}

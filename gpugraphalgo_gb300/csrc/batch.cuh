@@ -67,6 +67,7 @@ gga_status mq_engine_run(MqEngine *e, uint32_t max_rounds, cudaStream_t st, cuda
 gga_status mq_engine_count(MqEngine *e, uint32_t nslots, cudaStream_t st);
 
 struct MsbfsScratch;
+struct SuScratch;
 
 /* Batch state owned by a context (created on first batched call). */
 struct BatchScratch {
@@ -74,11 +75,13 @@ struct BatchScratch {
     uint32_t *pool = nullptr; /* per-query dist + visited / stamp words */
     size_t pool_words = 0;
     MsbfsScratch *ms = nullptr;
+    SuScratch *su = nullptr;
 };
 
 BatchScratch *ctx_batch(gga_ctx *c);
 gga_status batch_pool_reserve(BatchScratch *b, size_t words);
 void msbfs_scratch_free(MsbfsScratch *m);
+void su_scratch_free(SuScratch *s);
 /* Words of device state one query needs (dist + visited bits or stamps),
  * each part rounded up to 64 words. */
 size_t mq_state_words(uint32_t n, uint32_t algo);

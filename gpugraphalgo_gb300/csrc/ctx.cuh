@@ -3,6 +3,7 @@
  */
 #pragma once
 #include <mutex>
+#include <vector>
 
 #include "frontier.cuh"
 
@@ -24,6 +25,9 @@ struct gga_ctx {
     uint32_t *heavy = nullptr; /* CDP heavy-vertex list */
     uint32_t heavy_cap = 0;
     BatchScratch *batch = nullptr;
+    bool trace_on = false;
+    std::vector<uint32_t> trace_rounds; /* 4 words per round of the last traced solve */
+    std::vector<uint32_t> trace_cta;    /* busy kilocycles per CTA */
     std::mutex mu;
 };
 

@@ -116,6 +116,7 @@ static void dev_graph_release(gga_graph *g) {
     cudaSetDevice(d->device);
     dev_free_split(d);
     cudaFree(d->off); cudaFree(d->col); cudaFree(d->wt);
+    cudaFree(d->lcol); cudaFree(d->lwt); cudaFree(d->light);
     if (prev >= 0) cudaSetDevice(prev);
     free(d);
     g->dev = nullptr;
@@ -128,10 +129,128 @@ GraphView dev_graph_view(const DevGraph *d, bool split) {
     GraphView v;
     if (split && d->level != 0) {
         v.off = d->s_off; v.col = d->s_col; v.wt = d->wt; v.cc = d->s_cc; v.n = d->ns; v.m = d->m;
+        v.symmetric = 0;
     } else {
         v.off = d->off; v.col = d->col; v.wt = d->wt; v.cc = nullptr; v.n = d->n; v.m = d->m;
+        v.symmetric = d->symmetric > 0;
     }
     return v;
+}
+
+/* ------------------------------------------------------------ light / heavy */
+
+static unsigned grid_for(uint64_t items, unsigned bs);
+
+__global__ void k_light_flags(const uint32_t *wt, uint32_t m, uint32_t delta, uint32_t *flags) {
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x)
+        flags[e] = wt[e] < delta ? 1u : 0u;
+}
+
+/* Edge e of row u moves to off[u] + (its rank among the row's light edges)
+ * when light, else to off[u] + light(u) + (its rank among the heavy ones);
+ * ranks come from the exclusive scan `pos` of the light flags. */
+__global__ void k_lh_scatter(const uint32_t *off, const uint32_t *col, const uint32_t *wt, uint32_t n, uint32_t m,
+                             uint32_t delta, const uint32_t *pos, uint32_t *lcol, uint32_t *lwt) {
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n; /* row of e: largest u with off[u] <= e */
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (off[mid] <= e) lo = mid; else hi = mid;
+        }
+        const uint32_t b = off[lo], lrank = pos[e] - pos[b];
+        uint32_t dst;
+        if (wt[e] < delta) dst = b + lrank;
+        else dst = b + (pos[off[lo + 1]] - pos[b]) + ((uint32_t)e - b - lrank);
+        lcol[dst] = col[e];
+        lwt[dst] = wt[e];
+    }
+}
+
+__global__ void k_light_counts(const uint32_t *off, uint32_t n, const uint32_t *pos, uint32_t *light) {
+    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (uint64_t)gridDim.x * blockDim.x)
+        light[u] = pos[off[u + 1]] - pos[off[u]];
+}
+
+gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st) {
+    DevGraph *d = dev_graph_of(g);
+    if (!d) return gga_fail(GGA_ERR_INVALID_ARG, "graph not resident");
+    if (d->lcol && d->lh_delta == delta) return GGA_OK;
+    const size_t mpad = ((size_t)d->m + 4) & ~(size_t)3;
+    cudaError_t e = cudaSuccess;
+    if (!d->lcol) {
+        e = cudaMalloc((void **)&d->lcol, mpad * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d->lwt, mpad * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d->light, ((size_t)d->n + 1) * sizeof(uint32_t));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(d->lcol); cudaFree(d->lwt); cudaFree(d->light);
+            d->lcol = d->lwt = d->light = nullptr;
+            return gga_fail(GGA_ERR_CUDA, "light/heavy order (%u edges): %s", d->m, cudaGetErrorString(e));
+        }
+        GGA_CK(cudaMemsetAsync(d->lcol + d->m, 0, (mpad - d->m) * sizeof(uint32_t), st));
+        GGA_CK(cudaMemsetAsync(d->lwt + d->m, 0, (mpad - d->m) * sizeof(uint32_t), st));
+    }
+    d->lh_delta = 0;
+    uint32_t *flags = nullptr;
+    GGA_CK(cudaMallocAsync((void **)&flags, ((size_t)d->m + 1) * 2 * sizeof(uint32_t), st));
+    uint32_t *pos = flags + d->m + 1;
+    const unsigned grid = grid_for(d->m ? d->m : 1, 256);
+    k_light_flags<<<grid, 256, 0, st>>>(d->wt, d->m, delta, flags);
+    gga_status s = dev_exclusive_scan(flags, pos, d->m, st);
+    if (s == GGA_OK) {
+        if (d->m) k_lh_scatter<<<grid, 256, 0, st>>>(d->off, d->col, d->wt, d->n, d->m, delta, pos, d->lcol, d->lwt);
+        k_light_counts<<<grid_for(d->n ? d->n : 1, 256), 256, 0, st>>>(d->off, d->n, pos, d->light);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) s = gga_fail(GGA_ERR_CUDA, "light/heavy order: %s", cudaGetErrorString(e));
+    }
+    cudaFreeAsync(flags, st);
+    if (s) return s;
+    if ((s = dev_wait(st, 60.0))) return s;
+    d->lh_delta = delta;
+    return GGA_OK;
+}
+
+/* flag bit 0: a row is not sorted; bit 1: an edge (u, v) has no (v, u).
+ * One thread per edge: its row by binary search over the offsets, its
+ * reverse by binary search in the target's (sorted) row. */
+__global__ void k_check_symmetric(const uint32_t *off, const uint32_t *col, uint32_t n, uint32_t m, uint32_t *flag) {
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n; /* largest u with off[u] <= e */
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (off[mid] <= e) lo = mid; else hi = mid;
+        }
+        const uint32_t u = lo, v = col[e];
+        if (e + 1 < off[u + 1] && col[e + 1] < v) atomicOr(flag, 1u);
+        uint32_t b = off[v], t = off[v + 1];
+        const uint32_t end = t;
+        while (b < t) {
+            const uint32_t mid = b + ((t - b) >> 1);
+            if (col[mid] < u) b = mid + 1; else t = mid;
+        }
+        if (b >= end || col[b] != u) atomicOr(flag, 2u);
+    }
+}
+
+gga_status dev_graph_check_symmetric(gga_graph *g, uint32_t *dflag, uint32_t *hflag, cudaStream_t st) {
+    DevGraph *d = dev_graph_of(g);
+    if (!d) return gga_fail(GGA_ERR_INVALID_ARG, "graph not resident");
+    if (d->symmetric != 0) return GGA_OK;
+    GGA_CK(cudaMemsetAsync(dflag, 0, sizeof(uint32_t), st));
+    if (d->m) {
+        int sms = 0;
+        GGA_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d->device));
+        const uint64_t want = ((uint64_t)d->m + 255) / 256;
+        const unsigned grid = (unsigned)(want < (uint64_t)sms * 16 ? want : (uint64_t)sms * 16);
+        k_check_symmetric<<<grid, 256, 0, st>>>(d->off, d->col, d->n, d->m, dflag);
+        GGA_CK(cudaGetLastError());
+    }
+    GGA_CK(cudaMemcpyAsync(hflag, dflag, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    gga_status s = dev_wait(st, 60.0);
+    if (s) return s;
+    d->symmetric = *hflag ? -1 : 1;
+    g->symmetric = d->symmetric;
+    return GGA_OK;
 }
 
 /* Uploads g to `device` once; later calls return at once (cudaCopy,
@@ -156,6 +275,7 @@ gga_status dev_graph_ensure(gga_graph *g, int device, cudaStream_t st) {
         d->n = g->n;
         d->m = g->m;
         d->maxdeg = g->maxdeg;
+        d->symmetric = g->symmetric;
         size_t mpad = ((size_t)g->m + 4) & ~(size_t)3; /* room for 16-byte vector loads */
         cudaError_t e = cudaMalloc((void **)&d->off, ((size_t)g->n + 1) * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMalloc((void **)&d->col, mpad * sizeof(uint32_t));

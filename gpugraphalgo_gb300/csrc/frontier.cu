@@ -63,7 +63,29 @@ struct Args {
     uint32_t nblocks;
     uint32_t max_rounds;
     unsigned long long timeout_ns;
+    uint32_t bu;          /* BFS: bottom-up rounds allowed (symmetric, unsplit) */
+    uint32_t alpha, beta; /* direction rule */
+    uint32_t *trace;      /* NULL, or TRACE_ROUNDS x 4 round records then per-CTA busy kilocycles */
+    /* SSSP light/heavy mode (delta-stepping edge classes), when light != NULL:
+     * rows are ordered light (w < delta) first; near entries cover a vertex's
+     * light edges; its heavy edges go once per bucket to a heavy list that is
+     * expanded when the bucket closes.  Three heavy lists rotate by bucket. */
+    const uint32_t *light; /* n: light edges per row */
+    uint32_t *hstamp;      /* n: last bucket (+1) a vertex joined a heavy list */
+    uint32_t *hv0, *hv1, *hv2, *ho0, *ho1, *ho2, *hb0, *hb1, *hb2, *huf0, *huf1, *huf2;
 };
+
+/* Round record (block 0, thread 0) when tracing. */
+__device__ __forceinline__ void trace_round(const Args &a, uint32_t round, uint32_t kind, uint32_t items,
+                                            uint32_t edges, uint32_t far_items) {
+    if (a.trace && blockIdx.x == 0 && threadIdx.x == 0 && round < TRACE_ROUNDS) {
+        uint32_t *r = a.trace + (size_t)round * 4;
+        r[0] = kind;
+        r[1] = items;
+        r[2] = edges;
+        r[3] = far_items;
+    }
+}
 
 __device__ __forceinline__ uint32_t *sel(uint32_t p, uint32_t *a, uint32_t *b) { return p ? b : a; }
 __device__ __forceinline__ uint32_t *sel3(uint32_t p, uint32_t *a, uint32_t *b, uint32_t *c) {
@@ -90,20 +112,17 @@ struct Ctrl {
     uint32_t base_i, base_e; /* flush allocation */
     uint32_t unit, i0, cnt;  /* current unit */
     uint32_t nitems, total, fc, fm;
+    uint32_t hbase_i, hbase_e, hn, htot; /* heavy list: flush allocation, size at round start */
     uint32_t ws[32];         /* block-scan scratch */
+    unsigned long long ws64[32];
 };
 
-/* Stage a near-queue entry (any thread, any time between flushes). */
-__device__ __forceinline__ void stage_near(const Args &a, Ctrl &C, uint32_t *sv, uint32_t *sb, uint32_t *sd,
-                                           uint32_t v, uint32_t b, uint32_t d) {
+/* Stage a near-queue vertex (any thread, any time between flushes); its
+ * edge range is looked up when the stage is published. */
+__device__ __forceinline__ void stage_near(const Args &a, Ctrl &C, uint32_t *sv, uint32_t v) {
     const uint32_t k = atomicAdd(&C.nn, 1u);
-    if (k < a.scap) {
-        sv[k] = v;
-        sb[k] = b;
-        sd[k] = d;
-    } else {
-        set_err(a.ctl, GGA_DEV_OVERFLOW);
-    }
+    if (k < a.scap) sv[k] = v;
+    else set_err(a.ctl, GGA_DEV_OVERFLOW);
 }
 
 __device__ __forceinline__ void stage_far(const Args &a, Ctrl &C, uint32_t *sf, uint32_t v) {
@@ -112,59 +131,85 @@ __device__ __forceinline__ void stage_far(const Args &a, Ctrl &C, uint32_t *sf, 
     else set_err(a.ctl, GGA_DEV_OVERFLOW_FAR);
 }
 
-/* Publish the CTA's staged near-queue entries: a block scan of their degrees,
- * ONE 64-bit atomicAdd that allocates queue slots (high word) and edge
- * offsets (low word), coalesced writes of the entries, and the unit
- * boundaries k*U that fall inside the allocated edge range.  Called by every
- * thread of the CTA with the same nn (read from shared memory between two
+/* Publish the CTA's staged near-queue vertices.  Each thread takes a chunk
+ * of the stage, reads the row offsets of its vertices (kept out of the edge
+ * loop, whose dependent chain they would lengthen) and drops those without
+ * edges; a block scan of (count << 32 | edges) pairs and ONE 64-bit atomicAdd
+ * allocate queue slots (high word) and edge offsets (low word) together;
+ * each thread then writes its entries and the unit boundaries k*U that fall
+ * inside them.  In light/heavy mode a near entry covers the vertex's light
+ * edges, and the vertex's heavy edges join the bucket's heavy list once per
+ * bucket (second scan and allocation, same layout).  Called by every thread
+ * of the CTA with the same nn (read from shared memory between two
  * __syncthreads); no thread stages while it runs. */
+__device__ __forceinline__ void put_entries(const Args &a, uint32_t j0, uint32_t j1, const uint32_t *sv,
+                                            const uint32_t *sb, const uint32_t *sd, unsigned long long run,
+                                            uint32_t bi, uint32_t be, uint32_t *qv, uint32_t *qo, uint32_t *qb,
+                                            uint32_t *uf) {
+    for (uint32_t j = j0; j < j1; ++j) {
+        const uint32_t d = sd[j];
+        if (!d) continue;
+        const uint32_t i = bi + (uint32_t)(run >> 32), o = be + (uint32_t)run;
+        run += (1ull << 32) | d;
+        if (i >= a.cap) {
+            set_err(a.ctl, GGA_DEV_OVERFLOW);
+            continue;
+        }
+        qv[i] = sv[j];
+        qo[i] = o;
+        qb[i] = sb[j];
+        /* unit boundaries inside [o, o + d): this entry holds edge k*U */
+        for (uint64_t k = ((uint64_t)o + a.unit - 1) / a.unit; k * a.unit < (uint64_t)o + d; ++k) {
+            if (k < a.ucap) uf[k] = i;
+            else set_err(a.ctl, GGA_DEV_OVERFLOW_UNITS);
+        }
+    }
+}
+
 template <int BS>
 __device__ __forceinline__ void flush_near(const Args &a, Ctrl &C, uint32_t *sv, uint32_t *sb, uint32_t *sd,
-                                           uint32_t nn, uint32_t nxt, uint32_t r3n) {
+                                           uint32_t *sh, uint32_t nn, uint32_t nxt, uint32_t r3n, uint32_t bucket) {
     if (nn == 0) return;
     const uint32_t tid = threadIdx.x;
+    const bool lh = a.light != nullptr; /* the same in every thread */
+    const uint32_t hl = bucket % 3;
     const uint32_t chunk = (nn + BS - 1) / BS;
     const uint32_t j0 = min(tid * chunk, nn), j1 = min(j0 + chunk, nn);
-    uint32_t local = 0;
-    for (uint32_t j = j0; j < j1; ++j) local += sd[j];
-    uint32_t tot;
-    uint32_t run = block_exclusive_scan(local, C.ws, &tot);
-    for (uint32_t j = j0; j < j1; ++j) { /* degrees -> exclusive prefix within this flush */
-        const uint32_t d = sd[j];
-        sd[j] = run;
-        run += d;
+    unsigned long long local = 0, hlocal = 0;
+    for (uint32_t j = j0; j < j1; ++j) {
+        const uint32_t v = sv[j];
+        uint32_t b, d;
+        item_range(a, v, b, d);
+        const uint32_t dl = lh ? __ldg(a.light + v) : d;
+        sb[j] = b;
+        sd[j] = dl;
+        if (dl) local += (1ull << 32) | dl;
+        if (lh) {
+            const uint32_t hd = d - dl;
+            const bool first = hd && atomicExch(a.hstamp + v, bucket + 1) != bucket + 1;
+            sh[j] = first ? hd : 0u;
+            if (first) hlocal += (1ull << 32) | hd;
+        }
     }
+    unsigned long long tot, htot = 0;
+    const unsigned long long run = block_exclusive_scan64(local, C.ws64, &tot);
+    unsigned long long hrun = 0;
+    if (lh) hrun = block_exclusive_scan64(hlocal, C.ws64, &htot);
     if (tid == 0) {
-        const unsigned long long old =
-            atomicAdd(&a.ctl->qctr[r3n], ((unsigned long long)nn << 32) | (unsigned long long)tot);
+        const unsigned long long old = tot ? atomicAdd(&a.ctl->qctr[r3n], tot) : 0ull;
         C.base_i = (uint32_t)(old >> 32);
         C.base_e = (uint32_t)old;
+        const unsigned long long hold = htot ? atomicAdd(&a.ctl->hctr[hl], htot) : 0ull;
+        C.hbase_i = (uint32_t)(hold >> 32);
+        C.hbase_e = (uint32_t)hold;
     }
     __syncthreads();
-    const uint32_t bi = C.base_i, be = C.base_e;
-    uint32_t *qv = sel(nxt, a.qv0, a.qv1), *qo = sel(nxt, a.qo0, a.qo1), *qb = sel(nxt, a.qb0, a.qb1);
-    uint32_t *uf = sel(nxt, a.uf0, a.uf1);
-    for (uint32_t j = tid; j < nn; j += BS) {
-        const uint32_t i = bi + j;
-        if (i < a.cap) {
-            qv[i] = sv[j];
-            qo[i] = be + sd[j];
-            qb[i] = sb[j];
-        } else {
-            set_err(a.ctl, GGA_DEV_OVERFLOW);
-        }
-    }
-    /* unit boundaries inside [be, be + tot): the entry holding edge k*U */
-    const uint64_t k0 = ((uint64_t)be + a.unit - 1) / a.unit, k1 = ((uint64_t)be + tot + a.unit - 1) / a.unit;
-    for (uint64_t k = k0 + tid; k < k1; k += BS) {
-        const uint32_t rel = (uint32_t)(k * a.unit - be);
-        uint32_t lo = 0, hi = nn; /* last j with sd[j] <= rel */
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (sd[mid] <= rel) lo = mid; else hi = mid;
-        }
-        if (k < a.ucap) uf[k] = bi + lo;
-        else set_err(a.ctl, GGA_DEV_OVERFLOW_UNITS);
+    put_entries(a, j0, j1, sv, sb, sd, run, C.base_i, C.base_e, sel(nxt, a.qv0, a.qv1), sel(nxt, a.qo0, a.qo1),
+                sel(nxt, a.qb0, a.qb1), sel(nxt, a.uf0, a.uf1));
+    if (lh) {
+        for (uint32_t j = j0; j < j1; ++j) sb[j] += sd[j]; /* heavy edges start after the light ones */
+        put_entries(a, j0, j1, sv, sb, sh, hrun, C.hbase_i, C.hbase_e, sel3(hl, a.hv0, a.hv1, a.hv2),
+                    sel3(hl, a.ho0, a.ho1, a.ho2), sel3(hl, a.hb0, a.hb1, a.hb2), sel3(hl, a.huf0, a.huf1, a.huf2));
     }
     __syncthreads();
     if (tid == 0) C.nn = 0;
@@ -191,14 +236,90 @@ __device__ __forceinline__ void flush_far(const Args &a, Ctrl &C, uint32_t *sf, 
 
 /* Block-uniform checkpoint: wait for all staging, read the counts, and
  * publish a buffer when it is at least `limit` full (limit 1 = always). */
+struct Stage {
+    uint32_t *sv, *sb, *sd, *sh, *sf;
+};
+
 template <int BS, bool SSSP>
-__device__ __forceinline__ void checkpoint(const Args &a, Ctrl &C, uint32_t *sv, uint32_t *sb, uint32_t *sd,
-                                           uint32_t *sf, uint32_t nxt, uint32_t r3n, uint32_t fp, uint32_t limit) {
+__device__ __forceinline__ void checkpoint(const Args &a, Ctrl &C, const Stage &S, uint32_t nxt, uint32_t r3n,
+                                           uint32_t fp, uint32_t bucket, uint32_t limit) {
     __syncthreads();
     const uint32_t nn = C.nn, fn = SSSP ? C.fn : 0u;
     __syncthreads();
-    if (nn >= limit) flush_near<BS>(a, C, sv, sb, sd, nn, nxt, r3n);
-    if (SSSP && fn >= limit) flush_far<BS>(a, C, sf, fn, fp);
+    if (nn >= limit) flush_near<BS>(a, C, S.sv, S.sb, S.sd, S.sh, nn, nxt, r3n, bucket);
+    if (SSSP && fn >= limit) flush_far<BS>(a, C, S.sf, fn, fp);
+}
+
+/* One bottom-up BFS round (Beamer, Asanovic, Patterson, SC 2012): every
+ * unvisited vertex looks through its neighbours for one at level `round`
+ * (dist == round marks the frontier exactly: later levels are round + 1 or
+ * unset) and stops at the first.  A warp owns one 32-vertex word of the
+ * visited bitmap per step, lane i vertex 32w + i; the warp's finds are
+ * written back as one word and appended to the next round's queue with one
+ * packed 64-bit atomicAdd, so the queue has the same format as after a
+ * top-down round.  Needs every edge's reverse (a symmetric graph).  The loop
+ * trip count is warp-uniform; the per-lane neighbour scan reconverges before
+ * the ballot. */
+template <int BS>
+__device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, uint32_t nxt, uint32_t r3n,
+                                                unsigned long long &relaxed) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t gw = ((uint64_t)blockIdx.x * BS + threadIdx.x) >> 5, nw = ((uint64_t)gridDim.x * BS) >> 5;
+    const uint32_t nwords = (a.n + 31) / 32;
+    uint32_t *qv = sel(nxt, a.qv0, a.qv1), *qo = sel(nxt, a.qo0, a.qo1), *qb = sel(nxt, a.qb0, a.qb1);
+    uint32_t *uf = sel(nxt, a.uf0, a.uf1);
+    for (uint64_t w = gw; w < nwords; w += nw) {
+        const uint32_t vw = __ldcg(a.bits + w);
+        const uint32_t v = (uint32_t)w * 32u + lane;
+        bool found = false;
+        uint32_t b = 0, d = 0;
+        if (v < a.n && !(vw & (1u << lane))) {
+            b = __ldg(a.off + v);
+            const uint32_t e1 = __ldg(a.off + v + 1);
+            d = e1 - b;
+            for (uint32_t e = b; e < e1 && !found; e += 4) {
+                uint32_t u[4];
+#pragma unroll
+                for (uint32_t q = 0; q < 4; ++q) u[q] = e + q < e1 ? __ldg(a.col + e + q) : NONE;
+#pragma unroll
+                for (uint32_t q = 0; q < 4; ++q)
+                    if (u[q] != NONE && __ldcg(a.dist + u[q]) == round) found = true;
+                relaxed += min(4u, e1 - e);
+            }
+        }
+        const uint32_t fm = __ballot_sync(FULL, found);
+        if (fm == 0) continue; /* warp-uniform */
+        if (found) a.dist[v] = round + 1;
+        if (lane == 0) a.bits[w] = vw | fm; /* this warp is the word's only writer this round */
+        const uint32_t dd = found ? d : 0u;
+        uint32_t incl = dd;
+#pragma unroll
+        for (int k = 1; k < 32; k <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, k);
+            if (lane >= (uint32_t)k) incl += y;
+        }
+        const uint32_t wtot = __shfl_sync(FULL, incl, 31);
+        unsigned long long old = 0;
+        if (lane == 0)
+            old = atomicAdd(&a.ctl->qctr[r3n], ((unsigned long long)__popc(fm) << 32) | (unsigned long long)wtot);
+        old = __shfl_sync(FULL, old, 0);
+        if (found) {
+            const uint32_t idx = (uint32_t)(old >> 32) + (uint32_t)__popc(fm & lanemask_lt());
+            const uint32_t o = (uint32_t)old + incl - dd;
+            if (idx < a.cap) {
+                qv[idx] = v;
+                qo[idx] = o;
+                qb[idx] = b;
+                for (uint64_t k = ((uint64_t)o + a.unit - 1) / a.unit; k * a.unit < (uint64_t)o + dd; ++k) {
+                    if (k < a.ucap) uf[k] = idx;
+                    else set_err(a.ctl, GGA_DEV_OVERFLOW_UNITS);
+                }
+            } else {
+                set_err(a.ctl, GGA_DEV_OVERFLOW);
+            }
+        }
+    }
 }
 
 /* Relax one edge to v with candidate distance alt (atomicMin on uint32, as
@@ -243,6 +364,105 @@ __device__ __forceinline__ void relax_edge(const Args &a, uint32_t v, uint32_t a
     }
 }
 
+/* Expand one list of queue entries (the round's near queue, or a bucket's
+ * heavy list): CTAs take units of U edges by ticket from *work, load the
+ * unit's entries into shared memory and give consecutive edges to
+ * consecutive threads.  Each thread handles PB edges at a time in three
+ * passes (edge loads, then distance/bitmap probes, then updates), so PB
+ * independent memory chains are in flight per thread instead of one.
+ * Improvements at or above thr go to the far pile (thr = 0 sends all of them
+ * there).  Block-uniform: every thread runs the same tickets and
+ * checkpoints. */
+template <int BS, bool SSSP>
+__device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage &S, uint32_t *t_o, uint32_t *t_b,
+                                             uint32_t *t_du, const uint32_t *qv, const uint32_t *qo,
+                                             const uint32_t *qb, const uint32_t *uf, uint32_t nitems, uint32_t total,
+                                             uint32_t units, uint32_t *work, uint32_t round, uint32_t thr,
+                                             uint32_t nxt, uint32_t r3n, uint32_t fp, uint32_t bucket,
+                                             unsigned long long &relaxed) {
+    const uint32_t tid = threadIdx.x, U = a.unit;
+    FrontierCtl *ctl = a.ctl;
+    for (;;) {
+        if (tid == 0) {
+            const uint32_t k = atomicAdd(work, 1u);
+            C.unit = k;
+            if (k < units) {
+                const uint32_t i0 = min(__ldcg(uf + k), nitems - 1);
+                const uint32_t i1 = k + 1 < units ? min(__ldcg(uf + k + 1), nitems - 1) : nitems - 1;
+                C.i0 = i0;
+                C.cnt = i1 >= i0 ? min(i1 - i0 + 1, U + 1) : 1u;
+            }
+        }
+        __syncthreads();
+        const uint32_t k = C.unit;
+        if (k >= units) break;
+        const uint32_t i0 = C.i0, cnt = C.cnt;
+        const uint32_t ebase = k * U, eend = min(ebase + U, total);
+        for (uint32_t j = tid; j < cnt; j += BS) {
+            const uint32_t i = i0 + j;
+            t_o[j] = __ldcg(qo + i);
+            t_b[j] = __ldcg(qb + i);
+            if (SSSP) t_du[j] = __ldcg(a.dist + __ldcg(qv + i));
+        }
+        __syncthreads();
+        constexpr uint32_t PB = STAGE_BATCH;
+        for (uint32_t it0 = 0; it0 < a.iters; it0 += PB) {
+            if (it0) checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, BS);
+            uint32_t v[PB], alt[PB], probe[PB];
+            bool act[PB];
+#pragma unroll
+            for (uint32_t q = 0; q < PB; ++q) {
+                const uint32_t e = ebase + (it0 + q) * BS + tid;
+                act[q] = it0 + q < a.iters && e < eend;
+                v[q] = 0;
+                alt[q] = 0;
+                if (act[q]) {
+                    uint32_t lo = 0, hi = cnt; /* last j with t_o[j] <= e */
+                    while (hi - lo > 1) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (t_o[mid] <= e) lo = mid; else hi = mid;
+                    }
+                    const uint32_t ei = t_b[lo] + (e - t_o[lo]);
+                    if (ei < a.m) {
+                        v[q] = __ldg(a.col + ei);
+                        alt[q] = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
+                    } else { /* unreachable by construction; keeps reads in bounds */
+                        set_err(ctl, GGA_DEV_BAD_EDGE);
+                        act[q] = false;
+                    }
+                }
+            }
+#pragma unroll
+            for (uint32_t q = 0; q < PB; ++q)
+                probe[q] = act[q] ? (SSSP ? __ldcg(a.dist + v[q]) : __ldcg(a.bits + (v[q] >> 5))) : 0u;
+#pragma unroll
+            for (uint32_t q = 0; q < PB; ++q) {
+                if (!act[q]) continue;
+                bool nr, fr;
+                uint32_t fv;
+                relax_edge<SSSP>(a, v[q], alt[q], probe[q], round, thr, nr, fr, fv);
+                if (nr) stage_near(a, C, S.sv, v[q]);
+                if (SSSP && fv != NONE) {
+                    atomicMin(&C.fmin, fv);
+                    if (fr) stage_far(a, C, S.sf, v[q]);
+                }
+            }
+        }
+        if (tid == 0) relaxed += eend - ebase;
+        /* ends the unit: table reads done, staged counts stable */
+        checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, BS);
+    }
+}
+
+/* Unit boundaries of an entry list written directly (one thread). */
+__device__ __forceinline__ void put_one(const Args &a, uint32_t i, uint32_t o, uint32_t v, uint32_t b, uint32_t d,
+                                        uint32_t *qv, uint32_t *qo, uint32_t *qb, uint32_t *uf) {
+    qv[i] = v;
+    qo[i] = o;
+    qb[i] = b;
+    for (uint64_t k = ((uint64_t)o + a.unit - 1) / a.unit; k * a.unit < (uint64_t)o + d && k < a.ucap; ++k) uf[k] = i;
+}
+
 template <int BS, bool SSSP>
 __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_frontier(Args a) {
     extern __shared__ uint32_t dyn[];
@@ -251,10 +471,16 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
     FrontierCtl *ctl = a.ctl;
     const uint32_t tid = threadIdx.x;
     const uint64_t gtid = (uint64_t)blockIdx.x * BS + tid, gthreads = (uint64_t)gridDim.x * BS;
-    const uint32_t U = a.unit, S = a.scap;
+    const uint32_t U = a.unit, SC = a.scap;
+    const bool lh = SSSP && a.light != nullptr;
     uint32_t *t_o = dyn, *t_b = dyn + (U + 1), *t_du = dyn + 2 * (U + 1);
     uint32_t *stage = dyn + (SSSP ? 3u : 2u) * (U + 1);
-    uint32_t *sv = stage, *sb = stage + S, *sd = stage + 2 * S, *sf = stage + 3 * S;
+    Stage S;
+    S.sv = stage;
+    S.sb = stage + SC;
+    S.sd = stage + 2 * SC;
+    S.sf = stage + 3 * SC;
+    S.sh = stage + 4 * SC;
     uint32_t gen = 0;
     unsigned long long relaxed = 0;
 
@@ -262,6 +488,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
     for (uint64_t i = gtid; i < a.n; i += gthreads) {
         a.dist[i] = GGA_INFINITY;
         if (SSSP) a.stamp[i] = 0;
+        if (lh) a.hstamp[i] = 0;
     }
     const uint32_t nwords = (a.n + 31) / 32;
     for (uint64_t i = gtid; i < nwords; i += gthreads) {
@@ -289,12 +516,15 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
         if (!SSSP) a.bits[s0 >> 5] |= 1u << (s0 & 31);
         uint32_t b, d;
         item_range(a, s0, b, d);
-        if (d) {
-            ctl->qctr[0] = (1ull << 32) | d;
-            a.qv0[0] = s0;
-            a.qo0[0] = 0;
-            a.qb0[0] = b;
-            for (uint32_t k = 0; (uint64_t)k * U < d && k < a.ucap; ++k) a.uf0[k] = 0;
+        const uint32_t dl = lh ? a.light[s0] : d;
+        if (dl) {
+            ctl->qctr[0] = (1ull << 32) | dl;
+            put_one(a, 0, 0, s0, b, dl, a.qv0, a.qo0, a.qb0, a.uf0);
+        }
+        if (lh && d > dl) {
+            a.hstamp[s0] = 1; /* bucket 0 */
+            ctl->hctr[0] = (1ull << 32) | (d - dl);
+            put_one(a, 0, 0, s0, b + dl, d - dl, a.hv0, a.ho0, a.hb0, a.huf0);
         }
     }
     if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) return;
@@ -302,13 +532,21 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
     uint32_t thr = SSSP ? (a.delta ? a.delta : NONE) : 0;
     uint32_t fp = 0;
     uint32_t round = 0;
+    uint32_t bucket = 0;          /* SSSP: far passes so far (same value in every block) */
+    bool heavy_done = false;      /* this bucket's heavy list was expanded */
+    bool bottom_up = false;       /* BFS direction of the current round */
+    uint64_t unexplored = a.m;    /* edges of vertices not yet reached (same value in every block) */
+    unsigned long long busy = 0;  /* thread 0: cycles from round start to the barrier */
+    long long t_round = 0;
     /* Each block reads a round's counters once (thread 0) and shares them, and
      * those counters are not written during the round (pushes go to the next
-     * slot; when the queue is empty nothing relaxes, so the far pile is
-     * stable).  All blocks therefore take the same branches and meet the
-     * same barriers, and all threads of a block the same __syncthreads. */
+     * slot or list; when the near queue is empty nothing joins a heavy list,
+     * and nothing relaxes during a far pass's reads).  All blocks therefore
+     * take the same branches and meet the same barriers, and all threads of a
+     * block the same __syncthreads. */
     for (;; ++round) {
         const uint32_t r3 = round % 3, r3n = (round + 1) % 3, cur = round & 1, nxt = cur ^ 1;
+        const uint32_t hl = bucket % 3;
         if (tid == 0) {
             const unsigned long long qc = ld_relaxed_u64(&ctl->qctr[r3]);
             /* an overflowing push sets the error word, so an over-full queue
@@ -318,29 +556,59 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
             C.total = ni ? (uint32_t)qc : 0u;
             C.fc = SSSP ? min(ld_relaxed_u32(&ctl->far_count[fp]), a.cap) : 0u;
             C.fm = SSSP ? ld_relaxed_u32(&ctl->far_min[fp]) : NONE;
+            if (lh) {
+                const unsigned long long hc = ld_relaxed_u64(&ctl->hctr[hl]);
+                const uint32_t hn = min((uint32_t)(hc >> 32), a.cap);
+                C.hn = hn;
+                C.htot = hn ? (uint32_t)hc : 0u;
+            } else {
+                C.hn = 0;
+                C.htot = 0;
+            }
         }
         __syncthreads();
-        const uint32_t nitems = C.nitems, total = C.total, fc = C.fc, fm = C.fm;
+        const uint32_t nitems = C.nitems, total = C.total, fc = C.fc, fm = C.fm, hn = C.hn, htot = C.htot;
         const uint32_t units = min((uint32_t)(((uint64_t)total + U - 1) / U), a.ucap);
+        const uint32_t hunits = min((uint32_t)(((uint64_t)htot + U - 1) / U), a.ucap);
         __syncthreads(); /* C is rewritten below */
+        if (a.trace && tid == 0) t_round = clock64();
         if (round >= a.max_rounds) { /* safety net; every block stops in the same round */
             if (blockIdx.x == 0 && tid == 0) set_err(ctl, GGA_DEV_ROUND_LIMIT);
             break;
         }
-        const uint32_t *qv = sel(cur, a.qv0, a.qv1), *qo = sel(cur, a.qo0, a.qo1), *qb = sel(cur, a.qb0, a.qb1);
-        const uint32_t *uf = sel(cur, a.uf0, a.uf1);
         if (blockIdx.x == 0 && tid == 0) {
             const uint32_t r3nn = (round + 2) % 3;
             ctl->qctr[r3nn] = 0;
             ctl->work[r3nn] = 0;
         }
         if (units == 0) {
+            if (lh && !heavy_done && hunits > 0) {
+                /* ---- bucket closes: its vertices' distances are final, so
+                 * their heavy edges (w >= delta, results >= thr) are relaxed
+                 * once, all into the far pile */
+                heavy_done = true;
+                trace_round(a, round, 3, hn, htot, fc);
+                expand_units<BS, SSSP>(a, C, S, t_o, t_b, t_du, sel3(hl, a.hv0, a.hv1, a.hv2),
+                                       sel3(hl, a.ho0, a.ho1, a.ho2), sel3(hl, a.hb0, a.hb1, a.hb2),
+                                       sel3(hl, a.huf0, a.huf1, a.huf2), hn, htot, hunits, &ctl->hwork[hl], round,
+                                       0u, nxt, r3n, fp, bucket, relaxed);
+                checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, 1);
+                if (tid == 0 && C.fmin != NONE) {
+                    atomicMin(&ctl->far_min[fp], C.fmin);
+                    C.fmin = NONE;
+                }
+                if (a.trace && tid == 0) busy += clock64() - t_round;
+                if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+                continue;
+            }
             if (!SSSP || fc == 0) break;
             /* ---- near queue drained: raise the threshold and split the far
              * pile into the next round's near queue and the next pile */
             const uint32_t thr_old = thr;
             const uint32_t lowest = max(thr, fm);
             thr = lowest > NONE - a.delta ? NONE : lowest + a.delta;
+            ++bucket;
+            heavy_done = false;
             const uint32_t fq = fp == 2 ? 0 : fp + 1; /* pile that keeps the far items */
             if (blockIdx.x == 0 && tid == 0) {
                 /* three piles rotate: the one after fq was read by the
@@ -350,7 +618,13 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
                 ctl->far_count[dead] = 0;
                 ctl->far_min[dead] = NONE;
                 ctl->far_phases++;
+                /* heavy lists rotate by bucket the same way: the one after
+                 * the new bucket's was expanded two buckets ago */
+                const uint32_t hdead = (bucket + 1) % 3;
+                ctl->hctr[hdead] = 0;
+                ctl->hwork[hdead] = 0;
             }
+            trace_round(a, round, 2, fc, 0, fc);
             const uint32_t *fin = sel3(fp, a.far0, a.far1, a.far2);
             for (uint64_t base = (uint64_t)blockIdx.x * BS; base < fc; base += gthreads) {
                 const uint64_t i = base + tid;
@@ -359,119 +633,61 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
                     const uint32_t d = __ldcg(a.dist + v);
                     if (d >= thr) {
                         atomicMin(&C.fmin, d);
-                        stage_far(a, C, sf, v);
+                        stage_far(a, C, S.sf, v);
                     } else {
                         atomicAnd(a.farbits + (v >> 5), ~(1u << (v & 31)));
-                        if (d >= thr_old && atomicExch(a.stamp + v, round + 1) != round + 1) {
-                            uint32_t b, dg;
-                            item_range(a, v, b, dg);
-                            if (dg) stage_near(a, C, sv, sb, sd, v, b, dg);
-                        }
+                        if (d >= thr_old && atomicExch(a.stamp + v, round + 1) != round + 1)
+                            stage_near(a, C, S.sv, v);
                     }
                 }
-                checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fq, BS);
+                checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fq, bucket, BS);
             }
-            checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fq, 1);
+            checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fq, bucket, 1);
             if (tid == 0 && C.fmin != NONE) {
                 atomicMin(&ctl->far_min[fq], C.fmin);
                 C.fmin = NONE;
             }
+            if (a.trace && tid == 0) busy += clock64() - t_round;
             if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
             fp = fq;
             continue;
         }
-        for (;;) {
-            if (tid == 0) {
-                const uint32_t k = atomicAdd(&ctl->work[r3], 1u);
-                C.unit = k;
-                if (k < units) {
-                    const uint32_t i0 = min(__ldcg(uf + k), nitems - 1);
-                    const uint32_t i1 = k + 1 < units ? min(__ldcg(uf + k + 1), nitems - 1) : nitems - 1;
-                    C.i0 = i0;
-                    C.cnt = i1 >= i0 ? min(i1 - i0 + 1, U + 1) : 1u;
-                }
+        if (!SSSP && a.bu) {
+            /* direction rule from this round's counters (identical in every block) */
+            unexplored = unexplored > total ? unexplored - total : 0;
+            if (!bottom_up) bottom_up = (uint64_t)total * a.alpha > unexplored;
+            else bottom_up = (uint64_t)nitems * a.beta >= a.n;
+            if (bottom_up) {
+                trace_round(a, round, 1, nitems, total, 0);
+                bottom_up_round<BS>(a, round, nxt, r3n, relaxed);
+                if (a.trace && tid == 0) busy += clock64() - t_round;
+                if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+                continue;
             }
-            __syncthreads();
-            const uint32_t k = C.unit;
-            if (k >= units) break;
-            const uint32_t i0 = C.i0, cnt = C.cnt;
-            const uint32_t ebase = k * U, eend = min(ebase + U, total);
-            for (uint32_t j = tid; j < cnt; j += BS) {
-                const uint32_t i = i0 + j;
-                t_o[j] = __ldcg(qo + i);
-                t_b[j] = __ldcg(qb + i);
-                if (SSSP) t_du[j] = __ldcg(a.dist + __ldcg(qv + i));
-            }
-            __syncthreads();
-            /* Consecutive threads take consecutive edges of the unit.  Each
-             * thread handles PB edges at a time in three passes (edge loads,
-             * then distance/bitmap probes, then updates), so PB independent
-             * memory chains are in flight per thread instead of one. */
-            constexpr uint32_t PB = STAGE_BATCH;
-            for (uint32_t it0 = 0; it0 < a.iters; it0 += PB) {
-                if (it0) checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fp, BS);
-                uint32_t v[PB], alt[PB], probe[PB];
-                bool act[PB];
-#pragma unroll
-                for (uint32_t q = 0; q < PB; ++q) {
-                    const uint32_t e = ebase + (it0 + q) * BS + tid;
-                    act[q] = it0 + q < a.iters && e < eend;
-                    v[q] = 0;
-                    alt[q] = 0;
-                    if (act[q]) {
-                        uint32_t lo = 0, hi = cnt; /* last j with t_o[j] <= e */
-                        while (hi - lo > 1) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (t_o[mid] <= e) lo = mid; else hi = mid;
-                        }
-                        const uint32_t ei = t_b[lo] + (e - t_o[lo]);
-                        if (ei < a.m) {
-                            v[q] = __ldg(a.col + ei);
-                            alt[q] = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
-                        } else { /* unreachable by construction; keeps reads in bounds */
-                            set_err(ctl, GGA_DEV_BAD_EDGE);
-                            act[q] = false;
-                        }
-                    }
-                }
-#pragma unroll
-                for (uint32_t q = 0; q < PB; ++q)
-                    probe[q] = act[q] ? (SSSP ? __ldcg(a.dist + v[q]) : __ldcg(a.bits + (v[q] >> 5))) : 0u;
-#pragma unroll
-                for (uint32_t q = 0; q < PB; ++q) {
-                    if (!act[q]) continue;
-                    bool nr, fr;
-                    uint32_t fv;
-                    relax_edge<SSSP>(a, v[q], alt[q], probe[q], round, thr, nr, fr, fv);
-                    if (nr) {
-                        uint32_t b, dg;
-                        item_range(a, v[q], b, dg);
-                        if (dg) stage_near(a, C, sv, sb, sd, v[q], b, dg); /* nothing to expand otherwise */
-                    }
-                    if (SSSP && fv != NONE) {
-                        atomicMin(&C.fmin, fv);
-                        if (fr) stage_far(a, C, sf, v[q]);
-                    }
-                }
-            }
-            if (tid == 0) relaxed += eend - ebase;
-            /* ends the unit: table reads done, staged counts stable */
-            checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fp, BS);
         }
-        checkpoint<BS, SSSP>(a, C, sv, sb, sd, sf, nxt, r3n, fp, 1);
+        trace_round(a, round, 0, nitems, total, fc);
+        expand_units<BS, SSSP>(a, C, S, t_o, t_b, t_du, sel(cur, a.qv0, a.qv1), sel(cur, a.qo0, a.qo1),
+                               sel(cur, a.qb0, a.qb1), sel(cur, a.uf0, a.uf1), nitems, total, units, &ctl->work[r3],
+                               round, thr, nxt, r3n, fp, bucket, relaxed);
+        checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, 1);
         if (SSSP && tid == 0 && C.fmin != NONE) {
             atomicMin(&ctl->far_min[fp], C.fmin);
             C.fmin = NONE;
         }
+        if (a.trace && tid == 0) busy += clock64() - t_round;
         if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
     }
-    if (tid == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);
+    if (a.trace && tid == 0 && blockIdx.x < TRACE_MAX_CTAS)
+        a.trace[(size_t)TRACE_ROUNDS * 4 + blockIdx.x] = (uint32_t)min(busy / 1000ull, 0xffffffffull);
+    /* every thread of every block leaves the round loop at the same point */
+    for (int d = 16; d > 0; d >>= 1) relaxed += __shfl_down_sync(0xffffffffu, relaxed, d);
+    if ((tid & 31u) == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);
     if (blockIdx.x == 0 && tid == 0) ctl->rounds = round;
 }
 
 template <int BS, bool SSSP>
 size_t dyn_smem(uint32_t unit, uint32_t scap) {
-    return ((size_t)(unit + 1) * (SSSP ? 3 : 2) + (size_t)scap * (SSSP ? 4 : 3)) * sizeof(uint32_t);
+    return ((size_t)(unit + 1) * (SSSP ? 3 : 2) + (size_t)scap * (SSSP ? 5 : 3)) * sizeof(uint32_t);
 }
 
 template <int BS, bool SSSP>
@@ -517,7 +733,10 @@ void frontier_scratch_free(FrontierScratch *s) {
     cudaFree(s->qv0); cudaFree(s->qv1); cudaFree(s->qo0); cudaFree(s->qo1); cudaFree(s->qb0); cudaFree(s->qb1);
     cudaFree(s->uf0); cudaFree(s->uf1);
     cudaFree(s->far0); cudaFree(s->far1); cudaFree(s->far2);
-    cudaFree(s->out); cudaFree(s->ctl);
+    cudaFree(s->out); cudaFree(s->ctl); cudaFree(s->trace); cudaFree(s->hstamp);
+    for (int i = 0; i < 3; ++i) {
+        cudaFree(s->hv[i]); cudaFree(s->ho[i]); cudaFree(s->hb[i]); cudaFree(s->huf[i]);
+    }
     if (s->hctl) cudaFreeHost(s->hctl);
     memset(s, 0, sizeof *s);
 }
@@ -535,7 +754,11 @@ gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m) {
         (st = alloc_u32(&s->qo1, cap)) || (st = alloc_u32(&s->qb0, cap)) || (st = alloc_u32(&s->qb1, cap)) ||
         (st = alloc_u32(&s->uf0, ucap)) || (st = alloc_u32(&s->uf1, ucap)) ||
         (st = alloc_u32(&s->far0, cap)) || (st = alloc_u32(&s->far1, cap)) || (st = alloc_u32(&s->far2, cap)) ||
-        (st = alloc_u32(&s->out, cap))) {
+        (st = alloc_u32(&s->out, cap)) || (st = alloc_u32(&s->hstamp, cap)) ||
+        (st = alloc_u32(&s->hv[0], cap)) || (st = alloc_u32(&s->hv[1], cap)) || (st = alloc_u32(&s->hv[2], cap)) ||
+        (st = alloc_u32(&s->ho[0], cap)) || (st = alloc_u32(&s->ho[1], cap)) || (st = alloc_u32(&s->ho[2], cap)) ||
+        (st = alloc_u32(&s->hb[0], cap)) || (st = alloc_u32(&s->hb[1], cap)) || (st = alloc_u32(&s->hb[2], cap)) ||
+        (st = alloc_u32(&s->huf[0], ucap)) || (st = alloc_u32(&s->huf[1], ucap)) || (st = alloc_u32(&s->huf[2], ucap))) {
         frontier_scratch_free(s);
         return st;
     }
@@ -552,9 +775,14 @@ gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m) {
 
 gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_t *first, uint32_t src,
                         bool sssp, const gga_params &p, int sms, cudaStream_t st, cudaEvent_t ev0,
-                        cudaEvent_t ev1, FrontierResult *res) {
+                        cudaEvent_t ev1, FrontierResult *res, bool trace, const uint32_t *light) {
     Args a;
     memset(&a, 0, sizeof a);
+    if (trace) {
+        if (!s->trace) GGA_CK(cudaMalloc((void **)&s->trace, TRACE_WORDS * sizeof(uint32_t)));
+        GGA_CK(cudaMemsetAsync(s->trace, 0, TRACE_WORDS * sizeof(uint32_t), st));
+        a.trace = s->trace;
+    }
     a.off = view.off; a.col = view.col; a.wt = view.wt; a.cc = view.cc;
     a.first = first;
     a.n = view.n;
@@ -568,7 +796,9 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     a.ucap = s->ucap;
     a.src = src;
     const uint32_t bs = p.block_threads ? p.block_threads : 256;
-    a.iters = p.unit_iters ? p.unit_iters : 8;
+    /* measured on R-MAT 22 (GB300): BFS is fastest with 2048-edge units,
+     * SSSP with 1024-edge units (one batch of edges per thread per unit) */
+    a.iters = p.unit_iters ? p.unit_iters : (sssp ? 4 : 8);
     if (a.iters < 2 || a.iters > 16)
         return gga_fail(GGA_ERR_INVALID_ARG, "unit_iters must be in [2, 16] (got %u)", a.iters);
     a.unit = bs * a.iters;
@@ -577,6 +807,17 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
                         MIN_UNIT, MAX_UNIT);
     a.scap = bs * (STAGE_BATCH + 1); /* < BS staged after a checkpoint, + one batch */
     a.delta = p.sssp_delta;
+    a.bu = !sssp && view.cc == nullptr && view.symmetric && p.bfs_direction == 0;
+    if (sssp && light && a.delta) {
+        a.light = light;
+        a.hstamp = s->hstamp;
+        a.hv0 = s->hv[0]; a.hv1 = s->hv[1]; a.hv2 = s->hv[2];
+        a.ho0 = s->ho[0]; a.ho1 = s->ho[1]; a.ho2 = s->ho[2];
+        a.hb0 = s->hb[0]; a.hb1 = s->hb[1]; a.hb2 = s->hb[2];
+        a.huf0 = s->huf[0]; a.huf1 = s->huf[1]; a.huf2 = s->huf[2];
+    }
+    a.alpha = p.bfs_alpha ? p.bfs_alpha : 15;
+    a.beta = p.bfs_beta ? p.bfs_beta : 18;
     /* BFS needs at most n levels; near-far SSSP at most a level per
      * improvement, which the bound below leaves ample room for */
     a.max_rounds = view.n > 0x3fffffffu ? 0xffffffffu : 4u * view.n + 4096u;
@@ -614,6 +855,7 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
         res->launches = 1;
         res->edges_relaxed = h.edges_relaxed;
         res->kernel_ms = 0;
+        res->nblocks = a.nblocks;
         if (ev0 && ev1) cudaEventElapsedTime(&res->kernel_ms, ev0, ev1);
     }
     return GGA_OK;

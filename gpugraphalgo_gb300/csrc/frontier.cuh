@@ -14,6 +14,8 @@ struct FrontierCtl {
     uint32_t far_count[3];        /* three far piles rotate across far passes */
     uint32_t far_min[3];
     uint32_t far_phases;
+    unsigned long long hctr[3];   /* SSSP heavy lists: (entries << 32) | edges, rotating by bucket */
+    uint32_t hwork[3];            /* heavy-round unit tickets */
     uint32_t overflow_at;
     unsigned long long edges_relaxed;
     uint32_t diag[16];            /* first failed self-check: where and what */
@@ -33,6 +35,9 @@ struct FrontierScratch {
     uint32_t *uf0, *uf1; /* unit k's first entry */
     uint32_t *far0, *far1, *far2;
     uint32_t *out;       /* cap: gathered original-order output */
+    uint32_t *trace;     /* TRACE_ROUNDS x 4 round records + per-CTA busy kilocycles */
+    uint32_t *hstamp;    /* cap: SSSP light/heavy mode, bucket a vertex last joined a heavy list */
+    uint32_t *hv[3], *ho[3], *hb[3], *huf[3]; /* heavy lists (cap, cap, cap, ucap) */
     FrontierCtl *ctl;
     FrontierCtl *hctl;   /* pinned host mirror (keeps the read-back asynchronous) */
 };
@@ -42,14 +47,22 @@ struct FrontierResult {
     uint32_t launches;
     unsigned long long edges_relaxed;
     float kernel_ms;
+    uint32_t nblocks; /* CTAs of the launch */
 };
+
+constexpr uint32_t TRACE_ROUNDS = 65536;
+constexpr uint32_t TRACE_MAX_CTAS = 8192;
+constexpr size_t TRACE_WORDS = (size_t)TRACE_ROUNDS * 4 + TRACE_MAX_CTAS;
 
 gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m);
 void frontier_scratch_free(FrontierScratch *s);
 
 /* Runs one single-source BFS (sssp=false) or SSSP over `view`.  `first`
  * (split view) maps the original source to its split parent id; NULL for the
- * unsplit view.  Distances land in s->dist (view ids). */
+ * unsplit view.  `light` (SSSP, unsplit, delta > 0): light edges per row, with
+ * view.col / view.wt in light-first row order; turns on delta-stepping's
+ * light/heavy edge classes.  Distances land in s->dist (view ids). */
 gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_t *first, uint32_t src,
                         bool sssp, const gga_params &p, int sms, cudaStream_t st, cudaEvent_t ev0,
-                        cudaEvent_t ev1, FrontierResult *res);
+                        cudaEvent_t ev1, FrontierResult *res, bool trace = false,
+                        const uint32_t *light = nullptr);

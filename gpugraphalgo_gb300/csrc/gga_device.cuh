@@ -26,6 +26,13 @@ struct DevGraph {
     uint32_t *col; /* m */
     uint32_t *wt;  /* m */
     uint32_t maxdeg;
+    int symmetric; /* 1 yes, -1 no (or rows unsorted), 0 not checked */
+
+    /* delta-stepping light/heavy order of every row for bucket width lh_delta:
+     * edges with w < lh_delta first, then the rest, each group in CSR order */
+    uint32_t lh_delta;
+    uint32_t *lcol, *lwt; /* m each */
+    uint32_t *light;      /* n: light edges of each row */
 
     /* node split (graph.h:415-522) */
     int32_t level, buckets;
@@ -48,6 +55,7 @@ struct GraphView {
     const uint32_t *cc; /* child counts (split view) or nullptr */
     uint32_t n;
     uint32_t m;
+    int symmetric;      /* every edge has its reverse (unsplit view only) */
 };
 
 /* Error codes written by kernels into their control blocks. */
@@ -175,6 +183,34 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t *w
     return base + v - x;
 }
 
+/* The same scan for 64-bit values (e.g. (count << 32) | edges pairs). */
+__device__ __forceinline__ unsigned long long block_exclusive_scan64(unsigned long long x, unsigned long long *warp_sums,
+                                                                    unsigned long long *total) {
+    const uint32_t lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned long long v = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= (uint32_t)d) v += y;
+    }
+    if (lane == 31) warp_sums[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned long long s = lane < nw ? warp_sums[lane] : 0ull;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, s, d);
+            if (lane >= (uint32_t)d) s += y;
+        }
+        if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const unsigned long long base = wid ? warp_sums[wid - 1] : 0ull;
+    *total = warp_sums[nw - 1];
+    __syncthreads();
+    return base + v - x;
+}
+
 /* ---- host-side entry points implemented in the .cu files ----------------- */
 
 #ifdef __cplusplus
@@ -189,6 +225,11 @@ gga_status dev_graph_ensure(gga_graph *g, int device, cudaStream_t st);
 DevGraph *dev_graph_of(gga_graph *g);
 gga_status dev_exclusive_scan(const uint32_t *in, uint32_t *out, uint32_t count, cudaStream_t st);
 GraphView dev_graph_view(const DevGraph *d, bool split);
+/* Builds (or reuses) the light/heavy row order for bucket width delta. */
+gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st);
+/* Decides (once per resident graph) whether every edge has its reverse;
+ * dflag/hflag: 2 words of device / pinned scratch. */
+gga_status dev_graph_check_symmetric(gga_graph *g, uint32_t *dflag, uint32_t *hflag, cudaStream_t st);
 #ifdef __cplusplus
 }
 #endif

@@ -32,7 +32,7 @@ extern "C" {
 
 #define GGA_INFINITY 1000000000u /* MYINFINITY, bfs_sssp.cu:53 / graph.h:96 */
 #define GGA_MSBFS_MAX_SOURCES 64 /* one uint64 lane word per vertex */
-#define GGA_SSSP_BATCH_MAX_SOURCES 32
+#define GGA_SSSP_BATCH_MAX_SOURCES 32 /* one warp lane per source */
 /* Largest edge weight for which dist + weight cannot wrap in uint32 while
  * dist <= GGA_INFINITY; heavier weights are rejected (the reference's unsigned
  * arithmetic would wrap, bfs_sssp.cu/cudaKernels.h:323). */
@@ -94,7 +94,8 @@ typedef struct gga_graph_info {
     uint32_t mda;          /* MAX_EDGES_ALLOWED of the split (0 when not split) */
     uint32_t parents_with_children; /* myParentCount, bfs_sssp.cu:257-262 */
     uint32_t max_weight;
-    int32_t symmetric;     /* 1 generated symmetric, 0 unknown */
+    int32_t symmetric;     /* 1 symmetric (generated, or checked on the device), -1 checked: not
+                            * symmetric or rows unsorted, 0 not known yet */
 } gga_graph_info;
 
 /* ---- errors ----------------------------------------------------------- */
@@ -200,7 +201,7 @@ gga_status gga_solve(gga_ctx *ctx, gga_graph *g, gga_algo algo, uint32_t src,
 /* Frontier-engine parameters (picked by gga_autotune when not set). */
 typedef struct gga_params {
     uint32_t block_threads;  /* CTA size: 256, 512 or 1024 */
-    uint32_t unit_iters;     /* edges per work unit = block_threads x this (2..64, 0 = 4) */
+    uint32_t unit_iters;     /* edges per work unit = block_threads x this (2..16; 0 = 8 for BFS, 4 for SSSP) */
     uint32_t sssp_delta;     /* near-far bucket width (0 = plain improved-vertex frontier) */
     uint32_t use_split;      /* expand over the node-split graph when one exists */
     uint32_t blocks_per_sm;  /* persistent grid = SMs x this (0 = occupancy maximum) */
@@ -214,6 +215,19 @@ typedef struct gga_params {
     uint32_t cdp_mode;
     uint32_t cdp_pending_limit; /* cudaLimitDevRuntimePendingLaunchCount to set (0 = leave) */
     uint32_t skip_reached;      /* 1: gga_stats leaves vertices/edges_reached 0 (saves one launch) */
+    /* BFS direction: 0 = top-down rounds plus bottom-up rounds (unvisited
+     * vertices look for a parent in the frontier) chosen per round by Beamer's
+     * rule, on symmetric graphs walked unsplit; 1 = top-down only.  Levels
+     * are the same either way. */
+    uint32_t bfs_direction;
+    uint32_t bfs_alpha; /* go bottom-up when frontier edges x alpha > unexplored edges (0 = 15) */
+    uint32_t bfs_beta;  /* go back top-down when frontier vertices x beta < n (0 = 18) */
+    /* SSSP edge classes: 0 = delta-stepping light/heavy split when
+     * sssp_delta > 0 on the unsplit graph (rows reordered light-first once
+     * per graph and delta; near rounds relax light edges, each bucket's
+     * vertices relax their heavy edges once when the bucket closes);
+     * 1 = every near round relaxes all edges.  Distances are the same. */
+    uint32_t sssp_light_heavy;
 } gga_params;
 /* p = NULL returns to the per-graph defaults. */
 gga_status gga_set_params(gga_ctx *ctx, const gga_params *p);
@@ -221,6 +235,27 @@ gga_status gga_get_params(gga_ctx *ctx, gga_params *p);
 /* Picks parameters for g from its degree profile (and short timed trials when
  * trials > 0) and stores them in ctx. */
 gga_status gga_autotune(gga_ctx *ctx, gga_graph *g, uint32_t trials, gga_params *chosen);
+
+/* ---- instrumentation ------------------------------------------------------
+ * Device-counter counterparts of the reference's per-CTA clock64 histogram
+ * (my_drelax_metric, cudaKernels.h:1-70, combined per SM in metrics.h:68-84)
+ * and of its per-iteration convergence log (convergence.h:100-159). */
+typedef struct gga_round_trace {
+    uint32_t kind;      /* 0 top-down (SSSP: near) round, 1 bottom-up BFS round, 2 SSSP far pass,
+                         * 3 SSSP heavy round (a bucket's heavy edges) */
+    uint32_t items;     /* vertices expanded (kind 0/1) or far-pile entries split (kind 2) */
+    uint32_t edges;     /* edges owned by the expanded vertices */
+    uint32_t far_items; /* SSSP: far-pile size when the round started */
+} gga_round_trace;
+/* While enabled, each frontier-engine solve on ctx records one record per
+ * round (up to 65536) and each CTA's busy time in kilocycles (clock64 from
+ * round start to the grid barrier, summed over rounds). */
+gga_status gga_trace_enable(gga_ctx *ctx, int enable);
+/* Copies the last traced solve's records: up to `cap` rounds into `rounds`
+ * (*nrounds = rounds recorded) and up to `cta_cap` CTA busy times into
+ * `cta_kcycles` (*ncta = CTAs of that launch).  Any output may be NULL. */
+gga_status gga_trace_get(gga_ctx *ctx, gga_round_trace *rounds, uint32_t cap, uint32_t *nrounds,
+                         uint32_t *cta_kcycles, uint32_t cta_cap, uint32_t *ncta);
 
 /* ---- verification and output (myutils.h, L5) ---------------------------- */
 
@@ -273,9 +308,11 @@ gga_status gga_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_cols, ui
  * stats: iterations = levels, vertices/edges_reached summed over sources. */
 gga_status gga_msbfs(gga_ctx *ctx, gga_graph *g, uint32_t nsrc, const uint32_t *srcs,
                      uint32_t *dist_out, gga_stats *stats);
-/* Batched SSSP: nsrc <= 32 sources of one graph in one launch of the batch
- * engine (as gga_multi_solve).  dist_out: nsrc x nodes_orig, source-major,
- * host or device. */
+/* Batched SSSP: nsrc <= 32 sources of one graph in one launch, one warp lane
+ * per source (vertex-major distances: an edge read serves every source whose
+ * frontier holds its tail).  Distances equal nsrc single-source gga_sssp runs
+ * on the unsplit graph.  dist_out: nsrc x nodes_orig, source-major, host or
+ * device. */
 gga_status gga_sssp_batch(gga_ctx *ctx, gga_graph *g, uint32_t nsrc, const uint32_t *srcs,
                           uint32_t *dist_out, gga_stats *stats);
 

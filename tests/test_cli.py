@@ -1,0 +1,63 @@
+"""The drop-in CLI (gpugraphalgo_gb300/bin/gga_cli and its flavour
+links na_/n_/da_/d_ x bfs/sssp, named like the reference's genexe outputs):
+argv of bfs_sssp.cu:149-184, the Ary2File dump (myutils.h:51-62) and the
+17-column result.vi row (writeResult, myutils.h:86-113)."""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import gpugraphalgo_gb300 as gga
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BIN = os.path.join(ROOT, "gpugraphalgo_gb300", "bin")
+FLAVOURS = ["na_bfs", "na_sssp", "n_bfs", "n_sssp", "da_bfs", "da_sssp", "d_bfs", "d_sssp", "gga_bfs", "gga_sssp"]
+
+
+def _run(name, *args, cwd=None):
+    return subprocess.run([os.path.join(BIN, name), *args], capture_output=True, text=True, cwd=cwd, timeout=300)
+
+
+def test_cli_built_with_every_flavour():
+    for f in FLAVOURS + ["gga_cli"]:
+        assert os.access(os.path.join(BIN, f), os.X_OK), f
+
+
+@pytest.mark.parametrize("name,algo", [("na_sssp", "SSSP"), ("n_bfs", "BFS"), ("gga_cli", "BFS")])
+def test_cli_usage_without_graph(name, algo):
+    r = _run(name)
+    assert r.returncode == 1
+    assert r.stdout.splitlines()[0] == algo
+    assert "Usage:" in r.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flavour", FLAVOURS)
+@pytest.mark.parametrize("args", [[], ["0"], ["-1", "10"], ["4"]])
+def test_cli_matches_oracle_and_writes_result_row(tmp_path, flavour, args):
+    g = gga.Graph.rmat(11, 8, seed=31)
+    gr = str(tmp_path / "rmat11.gr")
+    g.save_gr(gr)
+    sssp = "sssp" in flavour
+    out = tmp_path / "dist.txt"
+    argv = [gr] + args
+    if args in ([], ["0"], ["4"]):
+        argv = [gr, args[0] if args else "0", str(out)]
+    r = _run(flavour, *argv, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "verifying: no of errors = 0." in r.stdout
+    want = oracle.serial_distances(*g.csr(), "sssp" if sssp else "bfs", 0)
+    if out.exists():
+        got = np.loadtxt(out, dtype=np.uint64).astype(np.uint32)
+        np.testing.assert_array_equal(got, want)
+    rows = (tmp_path / "result.vi").read_text().strip().splitlines()
+    f = rows[-1].split(",")
+    assert len(f) == 17
+    assert f[1] == ("SSSP" if sssp else "BFS") and f[2] == "rmat11.gr"
+    info = g.info()
+    assert int(f[4]) == info["nodes_orig"] and int(f[5]) == info["nedges"] and int(f[9]) == info["maxdeg"]
+    assert int(f[12]) >= 1  # iterations

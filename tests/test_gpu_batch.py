@@ -108,7 +108,8 @@ def test_sssp_batch_32_sources_match_oracle(ctx, graphs):
         got, st = ctx.sssp_batch(g, srcs, stats=True)
         for i, s in enumerate(srcs):
             np.testing.assert_array_equal(got[i], _want(g, "sssp", s), err_msg=f"{name} src#{i}={s}")
-        assert st["edges_relaxed"] >= st["edges_reached"] > 0
+        # one warp-edge visit serves every source whose frontier holds the tail
+        assert 0 < st["edges_relaxed"] and st["edges_reached"] > 0
 
 
 def test_sssp_batch_limits(ctx, graphs):

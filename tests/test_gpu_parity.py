@@ -240,8 +240,90 @@ def test_device_output_buffer(ctx):
 
 def test_stats_report_reached(ctx):
     g = gga.Graph.rmat(14, 8, seed=1)
-    d, st = ctx.bfs(g, 0, stats=True)
+    try:
+        ctx.set_params(bfs_direction=1)  # top-down only
+        d, st = ctx.bfs(g, 0, stats=True)
+    finally:
+        ctx.reset_params()
     vr, er = g.reached(d)
     assert st["vertices_reached"] == vr and st["edges_reached"] == er
-    assert st["edges_relaxed"] == er  # BFS expands each reached vertex once
+    assert st["edges_relaxed"] == er  # top-down BFS expands each reached vertex once
     assert st["kernel_ms"] > 0 and st["kernel_launches"] >= 1
+
+
+@pytest.mark.parametrize("alpha,beta", [(0, 0), (1000, 1000), (1, 2), (1000, 1)])
+def test_bfs_bottom_up_rounds_match_oracle(ctx, alpha, beta):
+    """Direction-optimising BFS (bottom-up rounds where the frontier is large)
+    gives the same levels for every mix of top-down and bottom-up rounds."""
+    for g in (gga.Graph.rmat(16, 16, seed=23), gga.Graph.grid(128, 96, seed=5)):
+        deg = g.degrees()
+        srcs = [int(np.argmax(deg)), 17, int(np.nonzero(deg == 0)[0][0]) if (deg == 0).any() else 3]
+        try:
+            ctx.set_params(bfs_direction=0, bfs_alpha=alpha, bfs_beta=beta)
+            for s in srcs:
+                np.testing.assert_array_equal(ctx.bfs(g, s), _oracle_dist(g, "bfs", s))
+        finally:
+            ctx.reset_params()
+        assert g.info()["symmetric"] == 1
+
+
+def test_bottom_up_checks_fewer_edges(ctx):
+    g = gga.Graph.rmat(16, 16, seed=3)
+    s = int(np.argmax(g.degrees()))
+    try:
+        ctx.set_params(bfs_direction=1)
+        d1, st1 = ctx.bfs(g, s, stats=True)
+    finally:
+        ctx.reset_params()
+    d0, st0 = ctx.bfs(g, s, stats=True)
+    np.testing.assert_array_equal(d0, d1)
+    assert st0["edges_relaxed"] < st1["edges_relaxed"] == st1["edges_reached"]
+
+
+def test_bfs_on_directed_graph_stays_top_down(ctx):
+    """Bottom-up rounds need every edge's reverse: a directed CSR is detected
+    on the device (symmetric = -1) and walked top-down only."""
+    off, col, wt = gga.Graph.rmat(12, 8, seed=9).csr()
+    u = np.repeat(np.arange(len(off) - 1, dtype=np.uint32), np.diff(off.astype(np.int64)))
+    keep = u < col
+    u, v, w = u[keep], col[keep], wt[keep]
+    noff = np.zeros(len(off), np.uint32)
+    np.add.at(noff, u + 1, 1)
+    noff = np.cumsum(noff, dtype=np.uint64).astype(np.uint32)
+    g = gga.Graph.from_csr(noff, v.astype(np.uint32), w.astype(np.uint32))
+    assert g.info()["symmetric"] == 0
+    for s in (0, 5, int(np.argmax(g.degrees()))):
+        np.testing.assert_array_equal(ctx.bfs(g, s), _oracle_dist(g, "bfs", s))
+    assert g.info()["symmetric"] == -1
+
+
+@pytest.mark.parametrize("delta", [1, 7, 33, 100, 5000])
+def test_sssp_light_heavy_classes_match_oracle(ctx, delta):
+    """Delta-stepping's light/heavy edge classes (light-first rows, heavy
+    edges relaxed once per bucket) give the same distances as relaxing every
+    edge in every near round, for every bucket width."""
+    for g in (gga.Graph.rmat(15, 16, seed=41), gga.Graph.grid(96, 80, seed=6)):
+        srcs = [int(np.argmax(g.degrees())), 11]
+        for s in srcs:
+            want = _oracle_dist(g, "sssp", s)
+            try:
+                for lh in (0, 1):
+                    ctx.set_params(sssp_delta=delta, sssp_light_heavy=lh)
+                    got, st = ctx.sssp(g, s, stats=True)
+                    np.testing.assert_array_equal(got, want, err_msg=f"delta={delta} lh={lh} src={s}")
+            finally:
+                ctx.reset_params()
+
+
+def test_sssp_light_heavy_relaxes_fewer_edges(ctx):
+    g = gga.Graph.rmat(16, 16, seed=8)
+    s = int(np.argmax(g.degrees()))
+    res = {}
+    try:
+        for lh in (0, 1):
+            ctx.set_params(sssp_delta=32, sssp_light_heavy=lh)
+            res[lh] = ctx.sssp(g, s, stats=True)
+    finally:
+        ctx.reset_params()
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    assert res[0][1]["edges_relaxed"] < res[1][1]["edges_relaxed"]
