@@ -56,7 +56,7 @@ class GraphInfo(C.Structure):
 
 
 class RoundTrace(C.Structure):
-    _fields_ = [("kind", u32), ("items", u32), ("edges", u32), ("far_items", u32)]
+    _fields_ = [("kind", u32), ("items", u32), ("edges", u32), ("far_items", u32), ("ns", u32)]
 
 
 class Params(C.Structure):

@@ -343,14 +343,23 @@ gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_
         if (c->trace_on) {
             const uint32_t nr = r.rounds < TRACE_ROUNDS ? r.rounds : TRACE_ROUNDS;
             const uint32_t nb = r.nblocks < TRACE_MAX_CTAS ? r.nblocks : TRACE_MAX_CTAS;
-            c->trace_rounds.assign((size_t)nr * 4, 0);
+            std::vector<uint32_t> raw((size_t)(nr + 1) * TRACE_REC);
             c->trace_cta.assign(nb, 0);
-            if (nr)
-                GGA_CK(cudaMemcpyAsync(c->trace_rounds.data(), c->fs.trace, (size_t)nr * 16, cudaMemcpyDeviceToHost, c->st));
+            GGA_CK(cudaMemcpyAsync(raw.data(), c->fs.trace, raw.size() * 4, cudaMemcpyDeviceToHost, c->st));
             if (nb)
-                GGA_CK(cudaMemcpyAsync(c->trace_cta.data(), c->fs.trace + (size_t)TRACE_ROUNDS * 4, (size_t)nb * 4,
-                                       cudaMemcpyDeviceToHost, c->st));
+                GGA_CK(cudaMemcpyAsync(c->trace_cta.data(), c->fs.trace + (size_t)(TRACE_ROUNDS + 1) * TRACE_REC,
+                                       (size_t)nb * 4, cudaMemcpyDeviceToHost, c->st));
             GGA_CK(cudaStreamSynchronize(c->st));
+            /* 5 words per round: the record and its duration (start of the next round - start) */
+            c->trace_rounds.assign((size_t)nr * 5, 0);
+            for (uint32_t i = 0; i < nr; ++i) {
+                const uint32_t *r = raw.data() + (size_t)i * TRACE_REC, *q = r + TRACE_REC;
+                const unsigned long long t0 = r[4] | ((unsigned long long)r[5] << 32);
+                const unsigned long long t1 = q[4] | ((unsigned long long)q[5] << 32);
+                for (int k = 0; k < 4; ++k) c->trace_rounds[(size_t)i * 5 + k] = r[k];
+                const unsigned long long dt = t1 > t0 ? t1 - t0 : 0;
+                c->trace_rounds[(size_t)i * 5 + 4] = (uint32_t)(dt < 0xffffffffull ? dt : 0xffffffffull);
+            }
         }
         st.iterations = r.rounds;
         st.kernel_launches = r.launches;
@@ -430,15 +439,16 @@ gga_status gga_trace_get(gga_ctx *c, gga_round_trace *rounds, uint32_t cap, uint
                          uint32_t *cta_kcycles, uint32_t cta_cap, uint32_t *ncta) {
     if (!c) return gga_fail(GGA_ERR_INVALID_ARG, "NULL context");
     std::lock_guard<std::mutex> lk(c->mu);
-    const uint32_t nr = (uint32_t)(c->trace_rounds.size() / 4), nb = (uint32_t)c->trace_cta.size();
+    const uint32_t nr = (uint32_t)(c->trace_rounds.size() / 5), nb = (uint32_t)c->trace_cta.size();
     if (nrounds) *nrounds = nr;
     if (ncta) *ncta = nb;
     if (rounds)
         for (uint32_t i = 0; i < nr && i < cap; ++i) {
-            rounds[i].kind = c->trace_rounds[4 * i];
-            rounds[i].items = c->trace_rounds[4 * i + 1];
-            rounds[i].edges = c->trace_rounds[4 * i + 2];
-            rounds[i].far_items = c->trace_rounds[4 * i + 3];
+            rounds[i].kind = c->trace_rounds[5 * (size_t)i];
+            rounds[i].items = c->trace_rounds[5 * (size_t)i + 1];
+            rounds[i].edges = c->trace_rounds[5 * (size_t)i + 2];
+            rounds[i].far_items = c->trace_rounds[5 * (size_t)i + 3];
+            rounds[i].ns = c->trace_rounds[5 * (size_t)i + 4];
         }
     if (cta_kcycles)
         for (uint32_t i = 0; i < nb && i < cta_cap; ++i) cta_kcycles[i] = c->trace_cta[i];

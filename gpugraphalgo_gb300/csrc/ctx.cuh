@@ -26,7 +26,7 @@ struct gga_ctx {
     uint32_t heavy_cap = 0;
     BatchScratch *batch = nullptr;
     bool trace_on = false;
-    std::vector<uint32_t> trace_rounds; /* 4 words per round of the last traced solve */
+    std::vector<uint32_t> trace_rounds; /* 5 words per round of the last traced solve */
     std::vector<uint32_t> trace_cta;    /* busy kilocycles per CTA */
     std::mutex mu;
 };

@@ -79,11 +79,22 @@ struct Args {
 __device__ __forceinline__ void trace_round(const Args &a, uint32_t round, uint32_t kind, uint32_t items,
                                             uint32_t edges, uint32_t far_items) {
     if (a.trace && blockIdx.x == 0 && threadIdx.x == 0 && round < TRACE_ROUNDS) {
-        uint32_t *r = a.trace + (size_t)round * 4;
+        uint32_t *r = a.trace + (size_t)round * TRACE_REC;
         r[0] = kind;
         r[1] = items;
         r[2] = edges;
         r[3] = far_items;
+    }
+}
+
+/* Round start time (block 0, thread 0) when tracing; round TRACE_ROUNDS'
+ * slot and the one after the last round hold the end time. */
+__device__ __forceinline__ void trace_time(const Args &a, uint32_t round) {
+    if (a.trace && blockIdx.x == 0 && threadIdx.x == 0 && round <= TRACE_ROUNDS) {
+        const unsigned long long t = global_timer_ns();
+        uint32_t *r = a.trace + (size_t)round * TRACE_REC;
+        r[4] = (uint32_t)t;
+        r[5] = (uint32_t)(t >> 32);
     }
 }
 
@@ -572,6 +583,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
         const uint32_t hunits = min((uint32_t)(((uint64_t)htot + U - 1) / U), a.ucap);
         __syncthreads(); /* C is rewritten below */
         if (a.trace && tid == 0) t_round = clock64();
+        trace_time(a, round);
         if (round >= a.max_rounds) { /* safety net; every block stops in the same round */
             if (blockIdx.x == 0 && tid == 0) set_err(ctl, GGA_DEV_ROUND_LIMIT);
             break;
@@ -677,8 +689,9 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
         if (a.trace && tid == 0) busy += clock64() - t_round;
         if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
     }
+    trace_time(a, round < TRACE_ROUNDS ? round + 1 : TRACE_ROUNDS);
     if (a.trace && tid == 0 && blockIdx.x < TRACE_MAX_CTAS)
-        a.trace[(size_t)TRACE_ROUNDS * 4 + blockIdx.x] = (uint32_t)min(busy / 1000ull, 0xffffffffull);
+        a.trace[(size_t)(TRACE_ROUNDS + 1) * TRACE_REC + blockIdx.x] = (uint32_t)min(busy / 1000ull, 0xffffffffull);
     /* every thread of every block leaves the round loop at the same point */
     for (int d = 16; d > 0; d >>= 1) relaxed += __shfl_down_sync(0xffffffffu, relaxed, d);
     if ((tid & 31u) == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);

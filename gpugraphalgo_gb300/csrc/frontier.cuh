@@ -35,7 +35,7 @@ struct FrontierScratch {
     uint32_t *uf0, *uf1; /* unit k's first entry */
     uint32_t *far0, *far1, *far2;
     uint32_t *out;       /* cap: gathered original-order output */
-    uint32_t *trace;     /* TRACE_ROUNDS x 4 round records + per-CTA busy kilocycles */
+    uint32_t *trace;     /* (TRACE_ROUNDS + 1) round records + per-CTA busy kilocycles */
     uint32_t *hstamp;    /* cap: SSSP light/heavy mode, bucket a vertex last joined a heavy list */
     uint32_t *hv[3], *ho[3], *hb[3], *huf[3]; /* heavy lists (cap, cap, cap, ucap) */
     FrontierCtl *ctl;
@@ -52,7 +52,8 @@ struct FrontierResult {
 
 constexpr uint32_t TRACE_ROUNDS = 65536;
 constexpr uint32_t TRACE_MAX_CTAS = 8192;
-constexpr size_t TRACE_WORDS = (size_t)TRACE_ROUNDS * 4 + TRACE_MAX_CTAS;
+constexpr uint32_t TRACE_REC = 8; /* words per round: kind, items, edges, far, start time (2 words), - */
+constexpr size_t TRACE_WORDS = (size_t)(TRACE_ROUNDS + 1) * TRACE_REC + TRACE_MAX_CTAS;
 
 gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m);
 void frontier_scratch_free(FrontierScratch *s);

@@ -246,6 +246,7 @@ typedef struct gga_round_trace {
     uint32_t items;     /* vertices expanded (kind 0/1) or far-pile entries split (kind 2) */
     uint32_t edges;     /* edges owned by the expanded vertices */
     uint32_t far_items; /* SSSP: far-pile size when the round started */
+    uint32_t ns;        /* round duration (block 0's clock from this round's start to the next's) */
 } gga_round_trace;
 /* While enabled, each frontier-engine solve on ctx records one record per
  * round (up to 65536) and each CTA's busy time in kilocycles (clock64 from

@@ -61,3 +61,28 @@ def test_cli_matches_oracle_and_writes_result_row(tmp_path, flavour, args):
     info = g.info()
     assert int(f[4]) == info["nodes_orig"] and int(f[5]) == info["nedges"] and int(f[9]) == info["maxdeg"]
     assert int(f[12]) >= 1  # iterations
+
+
+@pytest.mark.gpu
+def test_split_sweep_writes_one_row_per_point(tmp_path):
+    """The split-level sweep (the reference's mysc driver, levels then the
+    histogram rule per bucket count) in one process: 17-column rows, MDA per
+    level = ceil(maxdeg / level) as getSizeafterLoadBalance computes it
+    (graph.h:386-397)."""
+    from gpugraphalgo_gb300 import sweep
+
+    g = gga.Graph.rmat(12, 8, seed=33)
+    gr = str(tmp_path / "r12.gr")
+    g.save_gr(gr)
+    out = str(tmp_path / "result.vi")
+    rc = sweep.main([gr, "--flavours", "na,gga,d", "--algos", "bfs,sssp", "--levels", "1-3", "--buckets", "2,10",
+                     "--out", out])
+    assert rc == 0
+    rows = [r.split(",") for r in open(out).read().strip().splitlines()]
+    assert len(rows) == 3 * 2 * 5 and all(len(r) == 17 for r in rows)
+    maxdeg = g.info()["maxdeg"]
+    for r in rows:
+        level = int(r[10])
+        if r[0].startswith(("na_", "gga_")) and level < 2**31:
+            assert int(r[11]) == -(-maxdeg // level)
+        assert float(r[14]) > 0 and int(r[12]) >= 1
