@@ -393,21 +393,30 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                                              unsigned long long &relaxed) {
     const uint32_t tid = threadIdx.x, U = a.unit;
     FrontierCtl *ctl = a.ctl;
-    for (;;) {
-        if (tid == 0) {
-            const uint32_t k = atomicAdd(work, 1u);
-            C.unit = k;
-            if (k < units) {
-                const uint32_t i0 = min(__ldcg(uf + k), nitems - 1);
-                const uint32_t i1 = k + 1 < units ? min(__ldcg(uf + k + 1), nitems - 1) : nitems - 1;
-                C.i0 = i0;
-                C.cnt = i1 >= i0 ? min(i1 - i0 + 1, U + 1) : 1u;
-            }
+    /* Two CTA barriers per unit: thread 0 takes the NEXT unit's ticket while
+     * the CTA works on the current one, and the barrier that publishes it
+     * also ends the unit's staging (the checkpoint's count read), so the
+     * flush and the next table load follow without further barriers. */
+    auto take = [&]() {
+        const uint32_t k = atomicAdd(work, 1u);
+        C.unit = k;
+        if (k < units) {
+            const uint32_t i0 = min(__ldcg(uf + k), nitems - 1);
+            const uint32_t i1 = k + 1 < units ? min(__ldcg(uf + k + 1), nitems - 1) : nitems - 1;
+            C.i0 = i0;
+            C.cnt = i1 >= i0 ? min(i1 - i0 + 1, U + 1) : 1u;
         }
-        __syncthreads();
-        const uint32_t k = C.unit;
+    };
+    if (tid == 0) take();
+    for (;;) {
+        __syncthreads(); /* ticket published; previous unit's table reads and staging done */
+        /* C is next rewritten inside a flush (after its own barriers) or by
+         * the next take() (after the table barrier below), so no second
+         * barrier is needed before those writes */
+        const uint32_t k = C.unit, i0 = C.i0, cnt = C.cnt, nn = C.nn, fn = SSSP ? C.fn : 0u;
+        if (nn >= BS) flush_near<BS>(a, C, S.sv, S.sb, S.sd, S.sh, nn, nxt, r3n, bucket);
+        if (SSSP && fn >= BS) flush_far<BS>(a, C, S.sf, fn, fp);
         if (k >= units) break;
-        const uint32_t i0 = C.i0, cnt = C.cnt;
         const uint32_t ebase = k * U, eend = min(ebase + U, total);
         for (uint32_t j = tid; j < cnt; j += BS) {
             const uint32_t i = i0 + j;
@@ -459,9 +468,10 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                 }
             }
         }
-        if (tid == 0) relaxed += eend - ebase;
-        /* ends the unit: table reads done, staged counts stable */
-        checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, BS);
+        if (tid == 0) {
+            relaxed += eend - ebase;
+            take();
+        }
     }
 }
 

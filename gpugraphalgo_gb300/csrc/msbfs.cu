@@ -8,7 +8,8 @@
  *
  *   settle(L): every candidate vertex v (nxt[v] became non-zero during the
  *     previous expand) takes its new bits f = nxt[v] & ~seen[v], records level
- *     L for each set bit (dist[s * n + v] = L, source-major), folds f into
+ *     L for each set bit (vertex-major, the vertex's levels in one short
+ *     span; one tiled transpose gives the source-major output), folds f into
  *     seen[v] and, if it has out-edges, is appended to the expansion list with
  *     its frontier mask f and an exclusive edge offset (warp-aggregated 64-bit
  *     atomicAdd of (entries << 32 | edges), so entry index and edge offset
@@ -59,7 +60,8 @@ struct MsArgs {
     uint32_t *xv, *xo, *xb;         /* n each: vertex, edge offset, first edge */
     unsigned long long *xf;         /* n: frontier mask of the entry */
     uint32_t *uf;                   /* ucap: first entry of each unit */
-    uint32_t *dist;                 /* nsrc * n, source-major */
+    uint32_t *dist;                 /* n * ns, vertex-major: levels of vertex v at dist[v * ns ...] */
+    uint32_t ns;                    /* sources (row stride of dist) */
     MsCtl *ctl;
     uint32_t ucap, nblocks, max_levels;
     unsigned long long timeout_ns;
@@ -128,10 +130,8 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
                 f = __ldcg(a.nxt + v) & ~s0;
                 a.nxt[v] = 0;
                 a.seen[v] = s0 | f;
-                for (unsigned long long mm = f; mm; mm &= mm - 1) {
-                    const uint32_t s = (uint32_t)__ffsll((long long)mm) - 1;
-                    a.dist[(size_t)s * a.n + v] = L;
-                }
+                uint32_t *lv = a.dist + (size_t)v * a.ns; /* this vertex's levels: one short span */
+                for (unsigned long long mm = f; mm; mm &= mm - 1) lv[__ffsll((long long)mm) - 1] = L;
                 b = __ldg(a.off + v);
                 d = f ? __ldg(a.off + v + 1) - b : 0u;
             }
@@ -205,9 +205,15 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
             __syncthreads();
             for (uint32_t it0 = 0; it0 < MB_ITERS; it0 += MB_BATCH) {
                 if (it0) ms_checkpoint(a, C, sc, np, MB_BS);
+                /* MB_BATCH edges per thread: table lookups and edge loads,
+                 * then the seen/nxt probes, then the updates */
+                uint32_t v[MB_BATCH];
+                unsigned long long f[MB_BATCH], sn[MB_BATCH], nx[MB_BATCH];
 #pragma unroll
                 for (uint32_t s = 0; s < MB_BATCH; ++s) {
                     const uint32_t e = ebase + (it0 + s) * MB_BS + tid;
+                    f[s] = 0;
+                    v[s] = 0;
                     if (e >= eend) continue;
                     uint32_t lo = 0, hi = cnt;
                     while (hi - lo > 1) {
@@ -219,14 +225,21 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
                         ms_err(ctl, GGA_DEV_BAD_EDGE);
                         continue;
                     }
-                    const uint32_t v = __ldg(a.col + ei);
-                    const unsigned long long nb = t_f[lo] & ~__ldcg(a.seen + v);
-                    if (nb && (nb & ~__ldcg(a.nxt + v))) {
-                        if (atomicOr(a.nxt + v, nb) == 0) {
-                            const uint32_t slot = atomicAdd(&C.nn, 1u);
-                            if (slot < MB_SCAP) sc[slot] = v;
-                            else ms_err(ctl, GGA_DEV_OVERFLOW);
-                        }
+                    v[s] = __ldg(a.col + ei);
+                    f[s] = t_f[lo];
+                }
+#pragma unroll
+                for (uint32_t s = 0; s < MB_BATCH; ++s) {
+                    sn[s] = f[s] ? __ldcg(a.seen + v[s]) : 0ull;
+                    nx[s] = f[s] ? __ldcg(a.nxt + v[s]) : 0ull;
+                }
+#pragma unroll
+                for (uint32_t s = 0; s < MB_BATCH; ++s) {
+                    const unsigned long long nb = f[s] & ~sn[s];
+                    if (nb && (nb & ~nx[s]) && atomicOr(a.nxt + v[s], nb) == 0) {
+                        const uint32_t slot = atomicAdd(&C.nn, 1u);
+                        if (slot < MB_SCAP) sc[slot] = v[s];
+                        else ms_err(ctl, GGA_DEV_OVERFLOW);
                     }
                 }
             }
@@ -243,6 +256,21 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
 __global__ void k_ms_fill(uint32_t *p, size_t count, uint32_t value) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
         p[i] = value;
+}
+
+/* Source-major output: out[s * n + v] = lvl[v * ns + s], through a shared
+ * tile of 32 vertices x ns sources (coalesced reads and writes). */
+__global__ void k_ms_transpose(const uint32_t *lvl, uint32_t n, uint32_t ns, uint32_t *out) {
+    __shared__ uint32_t tile[32][65];
+    const uint32_t tx = threadIdx.x & 31, ty = threadIdx.x >> 5; /* 32 x 8 threads */
+    for (uint64_t v0 = (uint64_t)blockIdx.x * 32; v0 < n; v0 += (uint64_t)gridDim.x * 32) {
+        const uint32_t nv = (uint32_t)min((uint64_t)32, n - v0);
+        for (uint32_t k = threadIdx.x; k < nv * ns; k += blockDim.x) tile[k / ns][k % ns] = lvl[v0 * ns + k];
+        __syncthreads();
+        for (uint32_t s = ty; s < ns; s += 8)
+            if (tx < nv) out[(size_t)s * n + v0 + tx] = tile[tx][s];
+        __syncthreads();
+    }
 }
 
 /* Level-0 candidates: each distinct source vertex once, carrying the bits of
@@ -283,7 +311,8 @@ size_t ms_smem() { return (size_t)(MB_UNIT + 1) * 16 + (size_t)MB_SCAP * 4; }
 struct MsbfsScratch {
     int device = -1;
     uint32_t ncap = 0, ucap = 0;
-    size_t dcap = 0;
+    size_t dcap = 0, ocap = 0;
+    uint32_t *out = nullptr; /* source-major levels for host output */
     unsigned long long *seen = nullptr, *nxt = nullptr, *xf = nullptr;
     uint32_t *cand = nullptr, *xv = nullptr, *xo = nullptr, *xb = nullptr, *uf = nullptr;
     uint32_t *dist = nullptr, *srcs = nullptr;
@@ -302,13 +331,14 @@ void msbfs_scratch_free(MsbfsScratch *m) {
     cudaFree(m->xb);
     cudaFree(m->uf);
     cudaFree(m->dist);
+    cudaFree(m->out);
     cudaFree(m->srcs);
     cudaFree(m->ctl);
     cudaFreeHost(m->hctl);
     delete m;
 }
 
-static gga_status ms_reserve(MsbfsScratch *m, uint32_t n, uint32_t edges, size_t dist_words) {
+static gga_status ms_reserve(MsbfsScratch *m, uint32_t n, uint32_t edges, size_t dist_words, size_t out_words) {
     cudaError_t e = cudaSuccess;
     if (m->ncap < n) {
         cudaFree(m->seen); cudaFree(m->nxt); cudaFree(m->xf);
@@ -349,6 +379,17 @@ static gga_status ms_reserve(MsbfsScratch *m, uint32_t n, uint32_t edges, size_t
         }
         m->dcap = dist_words;
     }
+    if (m->ocap < out_words) {
+        cudaFree(m->out);
+        m->out = nullptr;
+        m->ocap = 0;
+        e = cudaMalloc((void **)&m->out, out_words * 4);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return gga_fail(GGA_ERR_CUDA, "msbfs output (%zu MiB): %s", (out_words * 4) >> 20, cudaGetErrorString(e));
+        }
+        m->ocap = out_words;
+    }
     if (!m->ctl) {
         GGA_CK(cudaMalloc((void **)&m->ctl, sizeof(MsCtl)));
         GGA_CK(cudaMallocHost((void **)&m->hctl, sizeof(MsCtl)));
@@ -388,8 +429,9 @@ gga_status gga_msbfs(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *sr
     MsbfsScratch *m = b->ms;
     const bool dev_out = ptr_is_device(dist_out);
     const size_t words = (size_t)nsrc * d->n;
-    if ((s = ms_reserve(m, d->n, d->m, dev_out ? 0 : words))) return s;
-    uint32_t *levels = dev_out ? dist_out : m->dist;
+    if ((s = ms_reserve(m, d->n, d->m, words, dev_out ? 0 : words))) return s;
+    uint32_t *levels = m->dist;                      /* vertex-major */
+    uint32_t *out = dev_out ? dist_out : m->out;     /* source-major */
 
     MsArgs a;
     memset(&a, 0, sizeof a);
@@ -406,6 +448,7 @@ gga_status gga_msbfs(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *sr
     a.xf = m->xf;
     a.uf = m->uf;
     a.dist = levels;
+    a.ns = nsrc;
     a.ctl = m->ctl;
     a.ucap = m->ucap;
     a.nblocks = (uint32_t)m->nblocks;
@@ -424,8 +467,10 @@ gga_status gga_msbfs(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *sr
     GGA_CK(cudaLaunchCooperativeKernel((const void *)k_msbfs, dim3(a.nblocks), dim3(MB_BS), args, ms_smem(), c->st));
     GGA_CK(cudaEventRecord(c->ev[1], c->st));
     GGA_CK(cudaMemcpyAsync(m->hctl, m->ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, c->st));
-    uint32_t launches = 4;
-    if (!dev_out) GGA_CK(cudaMemcpyAsync(dist_out, levels, words * 4, cudaMemcpyDeviceToHost, c->st));
+    k_ms_transpose<<<ctx_grid(c, ((uint64_t)d->n + 31) / 32 * 256, 256), 256, 0, c->st>>>(levels, d->n, nsrc, out);
+    GGA_CK(cudaGetLastError());
+    uint32_t launches = 5;
+    if (!dev_out) GGA_CK(cudaMemcpyAsync(dist_out, out, words * 4, cudaMemcpyDeviceToHost, c->st));
     if (stats) {
         unsigned long long *acc = (unsigned long long *)(c->dflag + 32);
         GGA_CK(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), c->st));

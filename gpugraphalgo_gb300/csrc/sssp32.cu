@@ -36,6 +36,7 @@ constexpr uint32_t SU_UNIT = 1024;              /* edges per unit */
 constexpr uint32_t SU_EPW = SU_UNIT / SU_WARPS; /* edges per warp per unit */
 constexpr uint32_t SU_SCAP = SU_BS * 2;         /* staging slots (<= one push per warp-edge between checkpoints) */
 constexpr uint32_t SU_CHECK = 16;               /* warp-edges per warp between checkpoints */
+constexpr uint32_t SU_EB = 4;                   /* edges per warp in flight */
 constexpr unsigned FULL = 0xffffffffu;
 
 struct SuCtl {
@@ -204,38 +205,61 @@ __global__ void __launch_bounds__(SU_BS, 4) k_sssp32(SuArgs a) {
             }
             __syncthreads();
             /* warp w takes edges ebase + w, + SU_WARPS, ...; a checkpoint
-             * every SU_CHECK edges bounds the staging (one push per warp-edge) */
+             * every SU_CHECK edges bounds the staging (one push per
+             * warp-edge).  SU_EB edges per step: lanes 0..SU_EB-1 each look
+             * one up and broadcast it, then every lane issues all its
+             * distance loads before any update (SU_EB independent chains). */
             for (uint32_t c0 = 0; c0 < SU_EPW; c0 += SU_CHECK) {
                 if (c0) su_checkpoint(a, C, sv, sb, sd, r3n, nb, SU_BS);
-                for (uint32_t c = c0; c < c0 + SU_CHECK; ++c) {
-                    const uint32_t e = ebase + c * SU_WARPS + warp; /* warp-uniform */
-                    if (e >= eend) break;
-                    uint32_t lo = 0, hi = cnt;
-                    while (hi - lo > 1) {
-                        const uint32_t mid = (lo + hi) >> 1;
-                        if (t_o[mid] <= e) lo = mid; else hi = mid;
+                for (uint32_t c = c0; c < c0 + SU_CHECK; c += SU_EB) { /* warp-uniform */
+                    uint32_t my_u = 0, my_m = 0, my_v = 0, my_w = 0;
+                    if (lane < SU_EB) {
+                        const uint32_t e = ebase + (c + lane) * SU_WARPS + warp;
+                        if (e < eend) {
+                            uint32_t lo = 0, hi = cnt;
+                            while (hi - lo > 1) {
+                                const uint32_t mid = (lo + hi) >> 1;
+                                if (t_o[mid] <= e) lo = mid; else hi = mid;
+                            }
+                            const uint32_t ei = t_b[lo] + (e - t_o[lo]);
+                            if (ei < a.m) {
+                                my_u = t_u[lo];
+                                my_m = t_m[lo];
+                                my_v = __ldg(a.col + ei);
+                                my_w = __ldg(a.wt + ei);
+                            } else {
+                                su_err(ctl, GGA_DEV_BAD_EDGE);
+                            }
+                        }
                     }
-                    const uint32_t ei = t_b[lo] + (e - t_o[lo]);
-                    if (ei >= a.m) {
-                        su_err(ctl, GGA_DEV_BAD_EDGE);
-                        break;
+                    uint32_t u[SU_EB], m[SU_EB], v[SU_EB], w[SU_EB], du[SU_EB], dv[SU_EB];
+#pragma unroll
+                    for (uint32_t q = 0; q < SU_EB; ++q) {
+                        u[q] = __shfl_sync(FULL, my_u, q);
+                        m[q] = __shfl_sync(FULL, my_m, q); /* 0 for a missing edge */
+                        v[q] = __shfl_sync(FULL, my_v, q);
+                        w[q] = __shfl_sync(FULL, my_w, q);
                     }
-                    const uint32_t u = t_u[lo], mask = t_m[lo];
-                    const uint32_t v = __ldg(a.col + ei), w = __ldg(a.wt + ei);
-                    bool imp = false;
-                    if ((mask >> lane) & 1u) {
-                        const uint32_t alt = __ldcg(a.D + (size_t)u * 32 + lane) + w;
-                        uint32_t *dv = a.D + (size_t)v * 32 + lane;
-                        if (alt < __ldcg(dv)) imp = alt < atomicMin(dv, alt);
+#pragma unroll
+                    for (uint32_t q = 0; q < SU_EB; ++q) {
+                        const bool on = (m[q] >> lane) & 1u;
+                        du[q] = on ? __ldcg(a.D + (size_t)u[q] * 32 + lane) : 0u;
+                        dv[q] = on ? __ldcg(a.D + (size_t)v[q] * 32 + lane) : 0u;
                     }
-                    const uint32_t im = __ballot_sync(FULL, imp);
-                    if (im && lane == 0) {
-                        if (atomicOr(Mn + v, im) == 0) {
-                            const uint32_t b = __ldg(a.off + v), d = __ldg(a.off + v + 1) - b;
+#pragma unroll
+                    for (uint32_t q = 0; q < SU_EB; ++q) {
+                        bool imp = false;
+                        if ((m[q] >> lane) & 1u) {
+                            const uint32_t alt = du[q] + w[q];
+                            if (alt < dv[q]) imp = alt < atomicMin(a.D + (size_t)v[q] * 32 + lane, alt);
+                        }
+                        const uint32_t im = __ballot_sync(FULL, imp);
+                        if (im && lane == 0 && atomicOr(Mn + v[q], im) == 0) {
+                            const uint32_t b = __ldg(a.off + v[q]), d = __ldg(a.off + v[q] + 1) - b;
                             if (d) {
                                 const uint32_t slot = atomicAdd(&C.nn, 1u);
                                 if (slot < SU_SCAP) {
-                                    sv[slot] = v;
+                                    sv[slot] = v[q];
                                     sb[slot] = b;
                                     sd[slot] = d;
                                 } else {

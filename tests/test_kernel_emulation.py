@@ -1,0 +1,102 @@
+"""The persistent kernels' own source text, run on the CPU against the oracle.
+
+tests/emu/gen_kernels.py turns a kernel file (frontier.cu, sssp32.cu,
+msbfs.cu, batch.cu) into host C++ and tests/emu/prelude.h emulates the CUDA
+constructs it uses: one host thread per CUDA thread, real barriers for
+__syncthreads and for warp collectives (so a collective reached by part of a
+warp hangs here instead of passing), host atomics, and grid barriers between
+2-4 emulated blocks that interleave freely.  Each case checks bit-exact
+distances against the oracle (the reference's serial BFS/SSSP,
+graph.h:115-184) and that the kernel's error word stays clear.  This is how
+every change to a persistent kernel's synchronisation is checked before it
+runs on a GPU; it needs only g++ (C++20)."""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import gpugraphalgo_gb300 as gga
+import oracle
+
+EMU = os.path.join(os.path.dirname(os.path.abspath(__file__)), "emu")
+
+
+@pytest.fixture(scope="module")
+def emu(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    root = tmp_path_factory.mktemp("emu")
+    rng = np.random.default_rng(1)
+    graphs = {"r10": gga.Graph.rmat(10, 8, seed=5), "grid": gga.Graph.grid(24, 20, seed=7)}
+    for name, g in graphs.items():
+        d = root / name
+        d.mkdir()
+        off, col, wt = g.csr()
+        deg = g.degrees()
+        srcs = [int(np.argmax(deg))] + [int(x) for x in rng.integers(0, g.n, 63)]
+        srcs[5] = srcs[0]  # a repeated source vertex
+        for arr, f in ((off, "off"), (col, "col"), (wt, "wt")):
+            arr.astype(np.uint32).tofile(d / f"{f}.bin")
+        np.array(srcs, np.uint32).tofile(d / "srcs.bin")
+        np.stack([oracle.serial_distances(off, col, wt, "bfs", s) for s in srcs]).astype(np.uint32).tofile(d / "want_bfs.bin")
+        np.stack([oracle.serial_distances(off, col, wt, "sssp", s) for s in srcs[:32]]).astype(np.uint32).tofile(
+            d / "want_sssp.bin")
+        algos = [i % 2 for i in range(16)]
+        np.array(algos, np.uint32).tofile(d / "algos.bin")
+        np.stack([oracle.serial_distances(off, col, wt, "sssp" if a else "bfs", s) for s, a in zip(srcs[:16], algos)]
+                 ).astype(np.uint32).tofile(d / "want_mix.bin")
+    shutil.copy(os.path.join(EMU, "prelude.h"), root / "prelude.h")
+    bins = {}
+    for k in ("frontier", "sssp32", "msbfs", "mq"):
+        harness = os.path.join(EMU, f"emu_{k}.cpp")
+        if not os.path.exists(harness):
+            continue
+        subprocess.run(["python3", os.path.join(EMU, "gen_kernels.py"), k, str(root / f"kernel_{k}.inc")], check=True)
+        shutil.copy(harness, root / f"emu_{k}.cpp")
+        exe = str(root / f"emu_{k}")
+        subprocess.run(["g++", "-std=c++20", "-O1", "-pthread", "-w", "-I", str(root), str(root / f"emu_{k}.cpp"),
+                        "-o", exe], check=True)
+        bins[k] = exe
+    return root, bins
+
+
+def _run(emu, kernel, *args):
+    root, bins = emu
+    if kernel not in bins:
+        pytest.skip(f"no harness for {kernel}")
+    r = subprocess.run([bins[kernel], str(root / args[0]), *map(str, args[1:])], capture_output=True, text=True,
+                       timeout=900)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert " bad=0" in r.stdout and "err=0" in r.stdout, r.stdout
+
+
+# graph, blocks, source row, sssp, unit_iters, delta, bottom-up, alpha, beta, light/heavy
+FRONTIER = [
+    ("r10", 4, 0, 0, 8, 0, 1, 15, 18, 0),
+    ("r10", 3, 3, 0, 2, 0, 0, 15, 18, 0),
+    ("grid", 4, 2, 0, 16, 0, 1, 1000, 1000, 0),
+    ("r10", 4, 0, 1, 4, 33, 0, 15, 18, 1),
+    ("r10", 2, 9, 1, 2, 64, 0, 15, 18, 1),
+    ("grid", 4, 1, 1, 8, 100, 0, 15, 18, 1),
+    ("grid", 3, 4, 1, 16, 0, 0, 15, 18, 0),
+    ("r10", 4, 7, 1, 4, 1, 0, 15, 18, 1),
+]
+
+
+@pytest.mark.parametrize("case", FRONTIER, ids=lambda c: "-".join(map(str, c)))
+def test_frontier_kernel_text(emu, case):
+    _run(emu, "frontier", *case)
+
+
+@pytest.mark.parametrize("case", [("r10", 4, 32), ("grid", 3, 5)], ids=lambda c: "-".join(map(str, c)))
+def test_sssp32_kernel_text(emu, case):
+    _run(emu, "sssp32", *case)
+
+
+@pytest.mark.parametrize("case", [("r10", 4, 64), ("grid", 2, 7)], ids=lambda c: "-".join(map(str, c)))
+def test_msbfs_kernel_text(emu, case):
+    _run(emu, "msbfs", *case)
