@@ -29,15 +29,20 @@
 
 namespace {
 
+constexpr uint32_t NONE = 0xffffffffu;
 constexpr uint32_t MQ_BS = 256;
-constexpr uint32_t MQ_ITERS = 8;
-constexpr uint32_t MQ_UNIT = MQ_BS * MQ_ITERS;
-constexpr uint32_t MQ_BATCH = 4;                     /* edge batches between staging checkpoints */
+constexpr uint32_t MQ_ITERS = 4;
+constexpr uint32_t MQ_UNIT = MQ_BS * MQ_ITERS;       /* edges per unit */
+constexpr uint32_t MQ_BATCH = 4;                     /* edges per thread between staging checkpoints */
 constexpr uint32_t MQ_SCAP = MQ_BS * (MQ_BATCH + 1); /* staging slots per CTA */
+constexpr uint32_t MQ_FCH = MQ_BS * 4;               /* far-pile items per split chunk */
+static_assert(MQ_MAXQ <= MQ_BS, "one query per thread in the round-start scan");
 
 struct MqArgs {
     const MqQuery *__restrict__ qt;
-    uint32_t nq;
+    MqQstate *qs;
+    uint32_t nq;      /* table slots in use */
+    uint32_t nearfar; /* SSSP queries run near-far buckets (nq <= MQ_MAXQ) */
     uint32_t *qq0, *qq1, *qv0, *qv1, *qo0, *qo1, *qb0, *qb1, *uf0, *uf1;
     MqCtl *ctl;
     uint32_t cap, ucap;
@@ -49,12 +54,21 @@ struct MqArgs {
 __device__ __forceinline__ uint32_t *sel(uint32_t p, uint32_t *a, uint32_t *b) { return p ? b : a; }
 __device__ __forceinline__ void set_err(MqCtl *c, uint32_t code) { atomicCAS(&c->err, GGA_DEV_OK, code); }
 
+/* Shared control of one CTA.  The per-query arrays hold this round's view of
+ * each query (near-far mode): threshold, the previous threshold (a far split
+ * re-queues only items the previous buckets did not expand), the pile far
+ * pushes go to, the prefix of far-split work, and flush histograms. */
 struct MqCtrl {
-    uint32_t nn;
+    uint32_t nn, fn;
     uint32_t base_i, base_e;
     uint32_t unit, i0, cnt;
     uint32_t nitems, total;
+    uint32_t ftot, fany;
+    uint32_t fchunk; /* far-split ticket: its own field, because threads may still
+                      * be reading `unit` for the expansion loop's exit test */
     uint32_t ws[32];
+    uint32_t thr[MQ_MAXQ], old[MQ_MAXQ], tgt[MQ_MAXQ], pre[MQ_MAXQ + 1];
+    uint32_t hist[MQ_MAXQ], base[MQ_MAXQ], fmin[MQ_MAXQ];
 };
 
 /* Write queue entry i and the unit boundaries inside its edge range. */
@@ -75,28 +89,48 @@ __device__ __forceinline__ void mq_put(const MqArgs &a, uint32_t buf, uint32_t i
     }
 }
 
-__device__ __forceinline__ void mq_stage(const MqArgs &a, MqCtrl &C, uint32_t *sq, uint32_t *sv, uint32_t *sb,
-                                         uint32_t *sd, uint32_t q, uint32_t v, uint32_t b, uint32_t d) {
+struct MqStage {
+    uint32_t *sq, *sv, *sb, *sd; /* near: query, vertex, first edge, degree */
+    uint32_t *fq, *fv;           /* far: query (| rank << 8 during a flush), vertex */
+};
+
+__device__ __forceinline__ void mq_stage(const MqArgs &a, MqCtrl &C, const MqStage &S, uint32_t q, uint32_t v,
+                                         uint32_t b, uint32_t d) {
     const uint32_t k = atomicAdd(&C.nn, 1u);
     if (k < MQ_SCAP) {
-        sq[k] = q;
-        sv[k] = v;
-        sb[k] = b;
-        sd[k] = d;
+        S.sq[k] = q;
+        S.sv[k] = v;
+        S.sb[k] = b;
+        S.sd[k] = d;
     } else {
         set_err(a.ctl, GGA_DEV_OVERFLOW);
     }
 }
 
-/* Publish the CTA's staged entries (block-uniform call, see frontier.cu). */
-__device__ __forceinline__ void mq_flush(const MqArgs &a, MqCtrl &C, uint32_t *sq, uint32_t *sv, uint32_t *sb,
-                                         uint32_t *sd, uint32_t nn, uint32_t nxt, uint32_t r3n) {
+__device__ __forceinline__ void mq_stage_far(const MqArgs &a, MqCtrl &C, const MqStage &S, uint32_t q, uint32_t v) {
+    const uint32_t k = atomicAdd(&C.fn, 1u);
+    if (k < MQ_SCAP) {
+        S.fq[k] = q;
+        S.fv[k] = v;
+    } else {
+        set_err(a.ctl, GGA_DEV_OVERFLOW_FAR);
+    }
+}
+
+/* Publish the CTA's staged queue entries (block-uniform call, see
+ * frontier.cu); in near-far mode also count them per query for round + 1. */
+__device__ __forceinline__ void mq_flush(const MqArgs &a, MqCtrl &C, const MqStage &S, uint32_t nn, uint32_t nxt,
+                                         uint32_t r3n) {
     if (nn == 0) return;
     const uint32_t tid = threadIdx.x;
+    uint32_t *sq = S.sq, *sv = S.sv, *sb = S.sb, *sd = S.sd;
     const uint32_t chunk = (nn + MQ_BS - 1) / MQ_BS;
     const uint32_t j0 = min(tid * chunk, nn), j1 = min(j0 + chunk, nn);
     uint32_t local = 0;
-    for (uint32_t j = j0; j < j1; ++j) local += sd[j];
+    for (uint32_t j = j0; j < j1; ++j) {
+        local += sd[j];
+        if (a.nearfar) atomicAdd(&C.hist[sq[j]], 1u);
+    }
     uint32_t tot;
     uint32_t run = block_exclusive_scan(local, C.ws, &tot);
     for (uint32_t j = j0; j < j1; ++j) {
@@ -109,6 +143,10 @@ __device__ __forceinline__ void mq_flush(const MqArgs &a, MqCtrl &C, uint32_t *s
             atomicAdd(&a.ctl->qctr[r3n], ((unsigned long long)nn << 32) | (unsigned long long)tot);
         C.base_i = (uint32_t)(old >> 32);
         C.base_e = (uint32_t)old;
+    }
+    if (a.nearfar && tid < a.nq && C.hist[tid]) { /* the scan's barriers ordered the histogram */
+        atomicAdd(&a.qs[tid].nr[r3n], C.hist[tid]);
+        C.hist[tid] = 0;
     }
     __syncthreads();
     const uint32_t bi = C.base_i, be = C.base_e;
@@ -140,17 +178,62 @@ __device__ __forceinline__ void mq_flush(const MqArgs &a, MqCtrl &C, uint32_t *s
     __syncthreads();
 }
 
-__device__ __forceinline__ void mq_checkpoint(const MqArgs &a, MqCtrl &C, uint32_t *sq, uint32_t *sv, uint32_t *sb,
-                                              uint32_t *sd, uint32_t nxt, uint32_t r3n, uint32_t limit) {
+/* Publish staged far-pile items: a shared histogram gives each item its rank
+ * within its query and the query's smallest distance, then one atomicAdd per
+ * query allocates room in the pile the query fills this round. */
+__device__ __forceinline__ void mq_flush_far(const MqArgs &a, MqCtrl &C, const MqStage &S, uint32_t nf) {
+    if (nf == 0) return;
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t j = tid; j < nf; j += MQ_BS) {
+        const uint32_t q = S.fq[j];
+        const uint32_t r = atomicAdd(&C.hist[q], 1u);
+        atomicMin(&C.fmin[q], __ldcg(a.qt[q].dist + S.fv[j]));
+        S.fq[j] = q | (r << 8);
+    }
     __syncthreads();
-    const uint32_t nn = C.nn;
+    if (tid < a.nq && C.hist[tid]) {
+        MqQstate *st = a.qs + tid;
+        const uint32_t t = C.tgt[tid];
+        C.base[tid] = atomicAdd(&st->fc[t], C.hist[tid]);
+        atomicMin(&st->fmin[t], C.fmin[tid]);
+        C.hist[tid] = 0;
+        C.fmin[tid] = NONE;
+    }
     __syncthreads();
-    if (nn >= limit) mq_flush(a, C, sq, sv, sb, sd, nn, nxt, r3n);
+    for (uint32_t j = tid; j < nf; j += MQ_BS) {
+        const uint32_t q = S.fq[j] & 0xffu, r = S.fq[j] >> 8;
+        const MqQuery &Q = a.qt[q];
+        const uint32_t pos = C.base[q] + r;
+        if (pos < Q.n) (C.tgt[q] ? Q.pile1 : Q.pile0)[pos] = S.fv[j];
+        else set_err(a.ctl, GGA_DEV_OVERFLOW_FAR);
+    }
+    __syncthreads();
+    if (tid == 0) C.fn = 0;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void mq_checkpoint(const MqArgs &a, MqCtrl &C, const MqStage &S, uint32_t nxt,
+                                              uint32_t r3n, uint32_t limit) {
+    __syncthreads();
+    const uint32_t nn = C.nn, nf = C.fn;
+    __syncthreads();
+    if (nn >= limit) mq_flush(a, C, S, nn, nxt, r3n);
+    if (nf >= limit) mq_flush_far(a, C, S, nf);
 }
 
 /* The batch kernel.  Rounds continue from ctl->round; the launch stops when
- * the queue is empty or after a.max_rounds rounds and records where it
- * stopped, so the next launch (after injecting new queries) picks up there. */
+ * no query has work left or after a.max_rounds rounds and records where it
+ * stopped, so the next launch (after injecting new queries) picks up there.
+ *
+ * SSSP in near-far mode, per query q (the single-source engine's buckets,
+ * frontier.cu, run independently per query inside shared rounds): an
+ * improvement below q's threshold joins the next round's queue, one at or
+ * above it joins q's far pile.  A round in which q has no queue entries
+ * (and q did not split a pile in the previous round) splits q's pile with
+ * the threshold raised by q's delta: items below it join the next round's
+ * queue, the rest the other pile.  Such a query has no expansion work in
+ * that round, so its split runs beside the other queries' expansions without
+ * a barrier between them.  Every answer equals the single-source one. */
 __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
     extern __shared__ uint32_t dyn[];
     __shared__ MqCtrl C;
@@ -158,10 +241,25 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
     const uint32_t tid = threadIdx.x;
     uint32_t *t_o = dyn, *t_b = dyn + (MQ_UNIT + 1), *t_q = dyn + 2 * (MQ_UNIT + 1), *t_a = dyn + 3 * (MQ_UNIT + 1);
     uint32_t *stage = dyn + 4 * (MQ_UNIT + 1);
-    uint32_t *sq = stage, *sv = stage + MQ_SCAP, *sb = stage + 2 * MQ_SCAP, *sd = stage + 3 * MQ_SCAP;
+    MqStage S;
+    S.sq = stage;
+    S.sv = stage + MQ_SCAP;
+    S.sb = stage + 2 * MQ_SCAP;
+    S.sd = stage + 3 * MQ_SCAP;
+    S.fq = stage + 4 * MQ_SCAP;
+    S.fv = stage + 5 * MQ_SCAP;
     uint32_t gen = 0;
     unsigned long long relaxed = 0;
-    if (tid == 0) C.nn = 0;
+    if (tid == 0) {
+        C.nn = 0;
+        C.fn = 0;
+    }
+    if (tid < MQ_MAXQ) {
+        C.hist[tid] = 0;
+        C.fmin[tid] = NONE;
+        C.thr[tid] = NONE;
+        C.tgt[tid] = 0;
+    }
     __syncthreads();
     uint32_t round = ld_relaxed_u32(&ctl->round); /* fixed before launch */
     uint32_t done = 0;
@@ -172,19 +270,72 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
             const uint32_t ni = min((uint32_t)(qc >> 32), a.cap);
             C.nitems = ni;
             C.total = ni ? (uint32_t)qc : 0u;
+            C.fany = 0;
         }
         __syncthreads();
-        const uint32_t nitems = C.nitems, total = C.total;
+        /* ---- this round's view of every query (near-far mode): one thread
+         * per table slot; block 0 also writes the next round's bucket state */
+        uint32_t fcount = 0;
+        if (a.nearfar && tid < a.nq) {
+            const MqQuery &Q = a.qt[tid];
+            MqQstate *st = a.qs + tid;
+            uint32_t thr = NONE, old = NONE, tgt = 0;
+            if (Q.algo == GGA_SSSP) {
+                const uint32_t par = round & 1;
+                thr = ld_relaxed_u32(&st->thr[par]);
+                const uint32_t fp = ld_relaxed_u32(&st->fp[par]) & 1u, cool = ld_relaxed_u32(&st->cool[par]);
+                const uint32_t nr = ld_relaxed_u32(&st->nr[r3]);
+                const uint32_t fc = min(ld_relaxed_u32(&st->fc[fp]), Q.n);
+                const uint32_t fm = ld_relaxed_u32(&st->fmin[fp]);
+                old = thr;
+                const bool split = nr == 0 && fc > 0 && !cool;
+                if (split) {
+                    const uint32_t lowest = max(thr, fm);
+                    thr = lowest > NONE - Q.delta ? NONE : lowest + Q.delta;
+                    fcount = fc;
+                }
+                tgt = split ? fp ^ 1u : fp;
+                if (fc) atomicAdd(&C.fany, 1u);
+                if (blockIdx.x == 0) {
+                    st->thr[par ^ 1] = thr;
+                    st->fp[par ^ 1] = tgt;
+                    st->cool[par ^ 1] = split ? 1u : 0u;
+                    st->nr[(round + 2) % 3] = 0; /* read two rounds ago, counted from next round */
+                    if (cool) {                  /* the pile split last round is free again */
+                        st->fc[fp ^ 1] = 0;
+                        st->fmin[fp ^ 1] = NONE;
+                    }
+                }
+            }
+            C.thr[tid] = thr;
+            C.old[tid] = old;
+            C.tgt[tid] = tgt;
+        }
+        uint32_t ftot = 0;
+        if (a.nearfar) { /* prefix of the far-split work (block-uniform) */
+            uint32_t t;
+            const uint32_t p = block_exclusive_scan(fcount, C.ws, &t);
+            if (tid < a.nq) C.pre[tid] = p;
+            if (tid == 0) {
+                C.pre[a.nq] = t;
+                C.ftot = t;
+            }
+            __syncthreads();
+            ftot = C.ftot;
+        }
+        const uint32_t nitems = C.nitems, total = C.total, fany = a.nearfar ? C.fany : 0u;
         const uint32_t units = min((uint32_t)(((uint64_t)total + MQ_UNIT - 1) / MQ_UNIT), a.ucap);
         __syncthreads();
-        if (done >= a.max_rounds || units == 0) break; /* same decision in every block */
+        if (done >= a.max_rounds || (units == 0 && fany == 0)) break; /* same decision in every block */
         if (blockIdx.x == 0 && tid == 0) {
             ctl->qctr[(round + 2) % 3] = 0;
             ctl->work[(round + 2) % 3] = 0;
+            ctl->fwork[(round + 2) % 3] = 0;
         }
         const uint32_t *qq = sel(cur, a.qq0, a.qq1), *qv = sel(cur, a.qv0, a.qv1);
         const uint32_t *qo = sel(cur, a.qo0, a.qo1), *qb = sel(cur, a.qb0, a.qb1);
         const uint32_t *uf = sel(cur, a.uf0, a.uf1);
+        /* ---- expansion of the round's queue */
         for (;;) {
             if (tid == 0) {
                 const uint32_t k = atomicAdd(&ctl->work[r3], 1u);
@@ -213,11 +364,11 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
             }
             __syncthreads();
             for (uint32_t it0 = 0; it0 < MQ_ITERS; it0 += MQ_BATCH) {
-                if (it0) mq_checkpoint(a, C, sq, sv, sb, sd, nxt, r3n, MQ_BS);
+                if (it0) mq_checkpoint(a, C, S, nxt, r3n, MQ_BS);
 #pragma unroll
                 for (uint32_t s = 0; s < MQ_BATCH; ++s) {
                     const uint32_t e = ebase + (it0 + s) * MQ_BS + tid;
-                    if (e >= eend) continue;
+                    if (it0 + s >= MQ_ITERS || e >= eend) continue;
                     uint32_t lo = 0, hi = cnt;
                     while (hi - lo > 1) {
                         const uint32_t mid = (lo + hi) >> 1;
@@ -236,8 +387,15 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
                     bool push = false;
                     if (Q.algo == GGA_SSSP) {
                         const uint32_t alt = t_a[lo] + __ldg(Q.wt + ei);
-                        if (alt < __ldcg(dist + v) && alt < atomicMin(dist + v, alt))
-                            push = atomicExch(aux + v, round + 1) != round + 1;
+                        if (alt < __ldcg(dist + v) && alt < atomicMin(dist + v, alt)) {
+                            const uint32_t thr = a.nearfar ? C.thr[q] : NONE;
+                            if (alt < thr) {
+                                push = atomicExch(aux + v, round + 1) != round + 1;
+                            } else {
+                                const uint32_t bit = 1u << (v & 31);
+                                if (!(atomicOr(Q.fbits + (v >> 5), bit) & bit)) mq_stage_far(a, C, S, q, v);
+                            }
+                        }
                     } else {
                         const uint32_t bit = 1u << (v & 31);
                         if (!(__ldcg(aux + (v >> 5)) & bit) && !(atomicOr(aux + (v >> 5), bit) & bit)) {
@@ -248,14 +406,46 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
                     if (push) {
                         const uint32_t *off = Q.off;
                         const uint32_t b = __ldg(off + v), d = __ldg(off + v + 1) - b;
-                        if (d) mq_stage(a, C, sq, sv, sb, sd, q, v, b, d);
+                        if (d) mq_stage(a, C, S, q, v, b, d);
                     }
                 }
             }
             if (tid == 0) relaxed += eend - ebase;
-            mq_checkpoint(a, C, sq, sv, sb, sd, nxt, r3n, MQ_BS);
+            mq_checkpoint(a, C, S, nxt, r3n, MQ_BS);
         }
-        mq_checkpoint(a, C, sq, sv, sb, sd, nxt, r3n, 1);
+        /* ---- far-pile splits of the queries that had no queue entries */
+        if (ftot) {
+            for (;;) {
+                if (tid == 0) C.fchunk = atomicAdd(&ctl->fwork[r3], 1u);
+                __syncthreads();
+                const uint64_t c0 = (uint64_t)C.fchunk * MQ_FCH;
+                if (c0 >= ftot) break;
+                const uint32_t c1 = (uint32_t)min((uint64_t)ftot, c0 + MQ_FCH);
+                for (uint32_t i = (uint32_t)c0 + tid; i < c1; i += MQ_BS) {
+                    uint32_t lo = 0, hi = a.nq; /* last q with pre[q] <= i */
+                    while (hi - lo > 1) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (C.pre[mid] <= i) lo = mid; else hi = mid;
+                    }
+                    const uint32_t q = lo;
+                    const MqQuery &Q = a.qt[q];
+                    const uint32_t *pile = C.tgt[q] ? Q.pile0 : Q.pile1; /* splitting: the pile not being filled */
+                    const uint32_t v = __ldcg(pile + (i - C.pre[q]));
+                    const uint32_t d = __ldcg(Q.dist + v);
+                    if (d >= C.thr[q]) {
+                        mq_stage_far(a, C, S, q, v); /* stays far, in the other pile */
+                    } else {
+                        atomicAnd(Q.fbits + (v >> 5), ~(1u << (v & 31)));
+                        if (d >= C.old[q] && atomicExch(Q.aux + v, round + 1) != round + 1) {
+                            const uint32_t b = __ldg(Q.off + v), dg = __ldg(Q.off + v + 1) - b;
+                            if (dg) mq_stage(a, C, S, q, v, b, dg);
+                        }
+                    }
+                }
+                mq_checkpoint(a, C, S, nxt, r3n, MQ_BS);
+            }
+        }
+        mq_checkpoint(a, C, S, nxt, r3n, 1);
         if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
     }
     if (tid == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);
@@ -266,25 +456,28 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
 }
 
 /* Copies each staged record to its table slot and sets the query's state
- * before its first round: dist = MYINFINITY, visited bits / stamps cleared.
- * Block row y handles queries y, y + gridDim.y, ... of the list. */
+ * before its first round: dist = MYINFINITY, visited bits / stamps and the
+ * far bitmap cleared.  Block row y handles queries y, y + gridDim.y, ... */
 __global__ void k_mq_init(MqQuery *qt, const MqQuery *stage, const uint32_t *list, uint32_t nlist) {
     for (uint32_t t = blockIdx.y; t < nlist; t += gridDim.y) {
         const MqQuery Q = stage[t];
         if (blockIdx.x == 0 && threadIdx.x == 0) qt[list[t]] = Q;
         const uint32_t naux = Q.algo == GGA_SSSP ? Q.n : (Q.n + 31) / 32;
+        const uint32_t nfb = Q.algo == GGA_SSSP ? (Q.n + 31) / 32 : 0;
         for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < Q.n; i += gridDim.x * blockDim.x)
             Q.dist[i] = GGA_INFINITY;
         for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < naux; i += gridDim.x * blockDim.x) Q.aux[i] = 0;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nfb; i += gridDim.x * blockDim.x) Q.fbits[i] = 0;
     }
 }
 
-/* Puts each listed query's source into the queue of round ctl->round (one
- * thread, a few queries per call: appends are serialised on purpose). */
+/* Puts each listed query's source into the queue of round ctl->round and
+ * sets its counters and bucket state (one thread, a few queries per call:
+ * appends are serialised on purpose). */
 __global__ void k_mq_inject(MqArgs a, MqQuery *qt, const uint32_t *list, uint32_t nlist) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     MqCtl *ctl = a.ctl;
-    const uint32_t round = ctl->round;
+    const uint32_t round = ctl->round, par = round & 1;
     for (uint32_t t = 0; t < nlist; ++t) {
         const uint32_t q = list[t];
         MqQuery *Q = qt + q;
@@ -294,13 +487,26 @@ __global__ void k_mq_inject(MqArgs a, MqQuery *qt, const uint32_t *list, uint32_
         if (Q->algo == GGA_SSSP) Q->aux[s] = round;
         else Q->aux[s >> 5] |= 1u << (s & 31);
         const uint32_t b = Q->off[s], d = Q->off[s + 1] - b;
+        if (a.qs) {
+            MqQstate *st = a.qs + q;
+            for (int k = 0; k < 3; ++k) st->nr[k] = 0;
+            for (int k = 0; k < 2; ++k) {
+                st->fc[k] = 0;
+                st->fmin[k] = NONE;
+            }
+            st->thr[par] = Q->algo == GGA_SSSP && Q->delta ? Q->delta : NONE;
+            st->fp[par] = 0;
+            st->cool[par] = 0;
+            st->nr[round % 3] = d ? 1u : 0u;
+        }
         if (!d) continue;
         const unsigned long long old = atomicAdd(&ctl->qctr[round % 3], (1ull << 32) | d);
         mq_put(a, round & 1, (uint32_t)(old >> 32), (uint32_t)old, q, s, b, d);
     }
 }
 
-/* active[q] = queue entries of query q waiting for round ctl->round. */
+/* active[q] = queue entries and far-pile items query q still has when round
+ * ctl->round starts (0: its distances are final). */
 __global__ void k_mq_count(MqArgs a, uint32_t *active) {
     const MqCtl *ctl = a.ctl;
     const uint32_t round = ctl->round;
@@ -309,6 +515,12 @@ __global__ void k_mq_count(MqArgs a, uint32_t *active) {
     const uint32_t *qq = sel(round & 1, a.qq0, a.qq1);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x)
         atomicAdd(active + qq[i], 1u);
+    if (a.nearfar)
+        for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < a.nq; q += gridDim.x * blockDim.x) {
+            const MqQstate &st = a.qs[q];
+            const uint32_t fc = st.fc[st.fp[round & 1] & 1u];
+            if (fc) atomicAdd(active + q, fc);
+        }
 }
 
 /* Reached vertices and their out-edges summed over the listed queries. */
@@ -338,7 +550,7 @@ __global__ void k_mq_reached(const MqQuery *qt, uint32_t nq, unsigned long long 
 
 namespace {
 
-size_t mq_smem() { return ((size_t)4 * (MQ_UNIT + 1) + (size_t)4 * MQ_SCAP) * sizeof(uint32_t); }
+size_t mq_smem() { return ((size_t)4 * (MQ_UNIT + 1) + (size_t)6 * MQ_SCAP) * sizeof(uint32_t); }
 
 template <typename T> gga_status grow(T **p, uint32_t *have, uint32_t want, const char *what) {
     if (*have >= want) return GGA_OK;
@@ -358,7 +570,9 @@ MqArgs mq_args(const MqEngine *e) {
     MqArgs a;
     memset(&a, 0, sizeof a);
     a.qt = e->qt;
-    a.nq = e->qcap;
+    a.qs = e->qs;
+    a.nq = e->nslots ? std::min(e->nslots, e->qcap) : e->qcap;
+    a.nearfar = a.nq <= MQ_MAXQ ? 1u : 0u;
     a.qq0 = e->qq[0]; a.qq1 = e->qq[1];
     a.qv0 = e->qv[0]; a.qv1 = e->qv[1];
     a.qo0 = e->qo[0]; a.qo1 = e->qo[1];
@@ -400,6 +614,9 @@ gga_status mq_engine_reserve(MqEngine *e, int device, uint32_t cap, uint64_t edg
         uint32_t h = e->qcap;
         if ((s = grow(&e->qt, &h, qcap, "query table"))) return s;
         h = e->qcap; if ((s = grow(&e->qstage, &h, qcap, "query staging"))) return s;
+        h = e->qcap; if ((s = grow(&e->qs, &h, qcap, "query counters"))) return s;
+        GGA_CK(cudaMemset(e->qt, 0, (size_t)qcap * sizeof(MqQuery)));
+        GGA_CK(cudaMemset(e->qs, 0, (size_t)qcap * sizeof(MqQstate)));
         h = e->qcap; if ((s = grow(&e->list, &h, qcap, "query list"))) return s;
         h = e->qcap; if ((s = grow(&e->active, &h, qcap, "query counts"))) return s;
         cudaFreeHost(e->hactive);
@@ -432,6 +649,7 @@ void mq_engine_free(MqEngine *e) {
         cudaFree(e->uf[b]);
     }
     cudaFree(e->qt);
+    cudaFree(e->qs);
     cudaFree(e->qstage);
     cudaFree(e->list);
     cudaFree(e->active);
@@ -443,6 +661,7 @@ void mq_engine_free(MqEngine *e) {
 
 gga_status mq_engine_reset(MqEngine *e, cudaStream_t st) {
     GGA_CK(cudaMemsetAsync(e->ctl, 0, sizeof(MqCtl), st));
+    if (e->qs) GGA_CK(cudaMemsetAsync(e->qs, 0, (size_t)e->qcap * sizeof(MqQstate), st));
     e->rounds_done = 0;
     e->edges_relaxed = 0;
     return GGA_OK;
@@ -510,9 +729,24 @@ gga_status mq_engine_count(MqEngine *e, uint32_t nslots, cudaStream_t st) {
 
 /* ------------------------------------------------------------ scratch */
 
+static size_t r64(size_t w) { return (w + 63) & ~(size_t)63; }
+
 size_t mq_state_words(uint32_t n, uint32_t algo) {
-    const size_t aux = algo == GGA_SSSP ? n : ((size_t)n + 31) / 32;
-    return (((size_t)n + 63) & ~(size_t)63) + ((aux + 63) & ~(size_t)63);
+    if (algo == GGA_SSSP) /* dist, stamps, far bitmap, two far piles */
+        return r64(n) + r64(n) + r64(((size_t)n + 31) / 32) + 2 * r64(n);
+    return r64(n) + r64(((size_t)n + 31) / 32); /* levels, visited bitmap */
+}
+
+void mq_state_layout(MqQuery *q, uint32_t *base) {
+    const size_t n = q->n;
+    q->dist = base;
+    q->aux = base + r64(n);
+    q->fbits = q->pile0 = q->pile1 = nullptr;
+    if (q->algo == GGA_SSSP) {
+        q->fbits = q->aux + r64(n);
+        q->pile0 = q->fbits + r64((n + 31) / 32);
+        q->pile1 = q->pile0 + r64(n);
+    }
 }
 
 BatchScratch *ctx_batch(gga_ctx *c) {
@@ -594,18 +828,20 @@ gga_status gga_multi_solve(gga_ctx *c, uint32_t nq, const gga_query *queries, gg
         r.m = d->m;
         r.algo = q.algo;
         r.src = q.src;
-        r.dist = b->pool + at;
-        r.aux = b->pool + at + (((size_t)d->n + 63) & ~(size_t)63);
+        r.delta = q.algo == GGA_SSSP ? ctx_default_params(q.graph).sssp_delta : 0;
+        mq_state_layout(&r, b->pool + at);
         at += mq_state_words(d->n, q.algo);
         slots[i] = i;
     }
     MqEngine *e = &b->eng;
+    e->nslots = nq;
     if ((s = mq_engine_reset(e, c->st))) return s;
     if ((s = mq_engine_admit(e, hq.data(), slots.data(), nq, c->st))) return s;
     uint32_t rounds = 0;
     float ms = 0;
-    if ((s = mq_engine_run(e, maxn + 2, c->st, c->ev[0], c->ev[1], &rounds, &ms))) return s;
-    if ((e->hctl->qctr[e->hctl->round % 3] >> 32) != 0)
+    const uint32_t max_rounds = maxn > 0x3fffffffu ? 0xffffffffu : 4u * maxn + 4096u;
+    if ((s = mq_engine_run(e, max_rounds, c->st, c->ev[0], c->ev[1], &rounds, &ms))) return s;
+    if (rounds >= max_rounds)
         return gga_fail(GGA_ERR_CUDA, "batch did not converge in %u rounds (internal error)", rounds);
     st.iterations = rounds;
     st.kernel_launches = 3;

@@ -6,16 +6,36 @@
 
 #include "ctx.cuh"
 
+/* Queries per launch for which SSSP runs near-far buckets (per-query shared
+ * memory in the kernel); larger batches run SSSP in Bellman-Ford order. */
+constexpr uint32_t MQ_MAXQ = 256;
+
 /* One query as the batch kernel sees it (device memory). */
 struct MqQuery {
     const uint32_t *off, *col, *wt; /* the graph's unsplit CSR (device) */
     uint32_t *dist;                 /* n distances / levels */
     uint32_t *aux;                  /* BFS: visited bitmap (n/32 words); SSSP: round stamps (n) */
+    uint32_t *fbits;                /* SSSP: "in a far pile" bitmap (n/32 words) */
+    uint32_t *pile0, *pile1;        /* SSSP: far piles (n each) */
     uint32_t n, m;
     uint32_t algo;        /* gga_algo */
     uint32_t src;
     uint32_t start_round; /* round in which the source is expanded */
-    uint32_t pad[3];
+    uint32_t delta;       /* SSSP bucket width (0: Bellman-Ford order) */
+    uint32_t pad[2];
+};
+
+/* Per-query counters and bucket state of the batch kernel.  Counters are
+ * updated with atomics; the bucket state is double-buffered by round parity
+ * (round r reads entry r & 1, block 0 writes entry (r + 1) & 1). */
+struct MqQstate {
+    uint32_t nr[3];   /* queue entries for the round with this index mod 3 */
+    uint32_t fc[2];   /* far pile sizes */
+    uint32_t fmin[2]; /* smallest distance in each pile (a lower bound) */
+    uint32_t thr[2];  /* near threshold */
+    uint32_t fp[2];   /* pile that far pushes go to */
+    uint32_t cool[2]; /* 1: split a pile in the previous round */
+    uint32_t pad;
 };
 
 /* Control block of the batch kernel; persists across superstep launches
@@ -28,7 +48,7 @@ struct MqCtl {
     uint32_t pad0;
     unsigned long long qctr[3]; /* (entries << 32) | edges, rotating by round */
     uint32_t work[3];
-    uint32_t pad1;
+    uint32_t fwork[3];          /* far-split chunk tickets, rotating by round */
     unsigned long long edges_relaxed;
 };
 
@@ -40,6 +60,8 @@ struct MqEngine {
     uint32_t qcap = 0; /* query-table slots */
     uint32_t *qq[2] = {}, *qv[2] = {}, *qo[2] = {}, *qb[2] = {}, *uf[2] = {};
     MqQuery *qt = nullptr;    /* device query table */
+    MqQstate *qs = nullptr;   /* device per-query counters (qcap) */
+    uint32_t nslots = 0;      /* table slots the kernel scans (set by the caller) */
     MqQuery *qstage = nullptr; /* device staging for admitted records (qcap) */
     uint32_t *list = nullptr; /* device index list for init / inject (qcap) */
     uint32_t *active = nullptr; /* device per-query entry counts (qcap) */
@@ -85,3 +107,6 @@ void su_scratch_free(SuScratch *s);
 /* Words of device state one query needs (dist + visited bits or stamps),
  * each part rounded up to 64 words. */
 size_t mq_state_words(uint32_t n, uint32_t algo);
+/* Lays one query's state out at `base` (dist, aux, and for SSSP the far
+ * bitmap and piles). */
+void mq_state_layout(MqQuery *q, uint32_t *base);

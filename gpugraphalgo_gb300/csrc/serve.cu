@@ -101,6 +101,7 @@ struct gga_server {
     int device = 0;
     std::vector<gga_graph *> graphs;
     std::vector<const DevGraph *> dgraphs;
+    std::vector<uint32_t> delta; /* SSSP bucket width per graph */
     uint32_t max_slots = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -207,8 +208,8 @@ void server_loop(gga_server *s) {
                 q.m = d->m;
                 q.algo = rq.algo;
                 q.src = rq.src;
-                q.dist = s->pool + off;
-                q.aux = s->pool + off + (((size_t)d->n + 63) & ~(size_t)63);
+                q.delta = rq.algo == GGA_SSSP ? s->delta[rq.graph] : 0;
+                mq_state_layout(&q, s->pool + off);
                 hq.push_back(q);
                 hslots.push_back(slot);
                 s->pending.pop_front();
@@ -288,15 +289,17 @@ gga_status gga_server_create(gga_ctx *c, uint32_t ngraphs, gga_graph *const *gra
     for (uint32_t i = 0; i < ngraphs; ++i) {
         sv->graphs.push_back(graphs[i]);
         sv->dgraphs.push_back(dev_graph_of(graphs[i]));
+        sv->delta.push_back(ctx_default_params(graphs[i]).sssp_delta);
         max_n = std::max<uint64_t>(max_n, graphs[i]->n);
         max_m = std::max<uint64_t>(max_m, graphs[i]->m);
     }
-    /* split the cap: queue entries (32 B per vertex) and state words (<= 8 B
+    /* split the cap: queue entries (32 B per vertex) and state words (<= 16 B
      * per vertex) in proportion, bounded by what max_slots queries could use */
     const uint64_t budget = mem_cap_bytes;
-    uint64_t cap = std::min<uint64_t>(budget * 4 / 5 / QUEUE_BYTES_PER_VERTEX, (uint64_t)max_slots * max_n);
+    uint64_t cap = std::min<uint64_t>(budget * 2 / 3 / QUEUE_BYTES_PER_VERTEX, (uint64_t)max_slots * max_n);
     cap = std::min<uint64_t>(cap, 0xFFFFFFF0ull);
-    uint64_t pool_words = std::min<uint64_t>(budget / 5 / 4, (uint64_t)max_slots * (2 * max_n + 128));
+    /* SSSP state is the largest: distances, stamps, far bitmap, two piles */
+    uint64_t pool_words = std::min<uint64_t>(budget / 3 / 4, (uint64_t)max_slots * (4 * max_n + 320));
     sv->edges_cap = std::min<uint64_t>((uint64_t)max_slots * max_m, 0xFFFFFFFFull - 2 * 2048 - 1);
     if (cap < 1 || pool_words < 128) {
         server_free(sv);
@@ -313,6 +316,7 @@ gga_status gga_server_create(gga_ctx *c, uint32_t ngraphs, gga_graph *const *gra
         return gga_fail(GGA_ERR_CUDA, "server setup: %s", cudaGetErrorString(e));
     }
     sv->pa.init(pool_words);
+    sv->eng.nslots = max_slots;
     if ((s = mq_engine_reserve(&sv->eng, sv->device, (uint32_t)cap, sv->edges_cap, max_slots)) ||
         (s = mq_engine_reset(&sv->eng, sv->st))) {
         server_free(sv);

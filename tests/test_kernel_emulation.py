@@ -100,3 +100,19 @@ def test_sssp32_kernel_text(emu, case):
 @pytest.mark.parametrize("case", [("r10", 4, 64), ("grid", 2, 7)], ids=lambda c: "-".join(map(str, c)))
 def test_msbfs_kernel_text(emu, case):
     _run(emu, "msbfs", *case)
+
+
+# graph, blocks, rounds per launch, queries admitted per launch, SSSP delta
+MQ = [
+    ("r10", 4, 1000000, 0, 0),
+    ("r10", 4, 1000000, 0, 33),
+    ("grid", 4, 1000000, 0, 100),
+    ("r10", 3, 2, 3, 16),
+    ("grid", 4, 5, 1, 300),
+    ("grid", 3, 3, 2, 1),
+]
+
+
+@pytest.mark.parametrize("case", MQ, ids=lambda c: "-".join(map(str, c)))
+def test_batch_kernel_text(emu, case):
+    _run(emu, "mq", *case)
