@@ -43,7 +43,7 @@ namespace {
 constexpr uint32_t NONE = 0xffffffffu;
 constexpr uint32_t MIN_UNIT = 512;  /* smallest edges-per-unit the buffers are sized for */
 constexpr uint32_t MAX_UNIT = 4096; /* largest edges-per-unit (shared-memory bound) */
-constexpr uint32_t STAGE_BATCH = 4; /* edge batches per thread between staging checkpoints */
+constexpr uint32_t STAGE_BATCH = 8; /* edges per thread in flight between staging checkpoints */
 
 struct Args {
     const uint32_t *off, *col, *wt, *cc;
@@ -148,38 +148,35 @@ __device__ __forceinline__ void stage_far(const Args &a, Ctrl &C, uint32_t *sf, 
  * edges; a block scan of (count << 32 | edges) pairs and ONE 64-bit atomicAdd
  * allocate queue slots (high word) and edge offsets (low word) together;
  * each thread then writes its entries and the unit boundaries k*U that fall
- * inside them.  In light/heavy mode a near entry covers the vertex's light
- * edges, and the vertex's heavy edges join the bucket's heavy list once per
- * bucket (second scan and allocation, same layout).  Called by every thread
- * of the CTA with the same nn (read from shared memory between two
- * __syncthreads); no thread stages while it runs. */
-__device__ __forceinline__ void put_entries(const Args &a, uint32_t j0, uint32_t j1, const uint32_t *sv,
-                                            const uint32_t *sb, const uint32_t *sd, unsigned long long run,
-                                            uint32_t bi, uint32_t be, uint32_t *qv, uint32_t *qo, uint32_t *qb,
-                                            uint32_t *uf) {
-    for (uint32_t j = j0; j < j1; ++j) {
-        const uint32_t d = sd[j];
-        if (!d) continue;
-        const uint32_t i = bi + (uint32_t)(run >> 32), o = be + (uint32_t)run;
-        run += (1ull << 32) | d;
-        if (i >= a.cap) {
-            set_err(a.ctl, GGA_DEV_OVERFLOW);
-            continue;
-        }
-        qv[i] = sv[j];
-        qo[i] = o;
-        qb[i] = sb[j];
-        /* unit boundaries inside [o, o + d): this entry holds edge k*U */
-        for (uint64_t k = ((uint64_t)o + a.unit - 1) / a.unit; k * a.unit < (uint64_t)o + d; ++k) {
-            if (k < a.ucap) uf[k] = i;
-            else set_err(a.ctl, GGA_DEV_OVERFLOW_UNITS);
-        }
+ * inside them, reading the (L1-resident) offsets again instead of keeping
+ * them in shared memory.  In light/heavy mode a near entry covers the
+ * vertex's light edges, and the vertex's heavy edges join the bucket's heavy
+ * list once per bucket (second scan and allocation, same layout); the stage
+ * keeps that "first time in this bucket" mark in bit 31 of the vertex id
+ * (ids are below 2^31).  Called by every thread of the CTA with the same nn
+ * (read from shared memory between two __syncthreads); no thread stages
+ * while it runs. */
+constexpr uint32_t HEAVY_MARK = 0x80000000u;
+
+__device__ __forceinline__ void put_entry(const Args &a, uint32_t i, uint32_t o, uint32_t v, uint32_t b, uint32_t d,
+                                          uint32_t *qv, uint32_t *qo, uint32_t *qb, uint32_t *uf) {
+    if (i >= a.cap) {
+        set_err(a.ctl, GGA_DEV_OVERFLOW);
+        return;
+    }
+    qv[i] = v;
+    qo[i] = o;
+    qb[i] = b;
+    /* unit boundaries inside [o, o + d): this entry holds edge k*U */
+    for (uint64_t k = ((uint64_t)o + a.unit - 1) / a.unit; k * a.unit < (uint64_t)o + d; ++k) {
+        if (k < a.ucap) uf[k] = i;
+        else set_err(a.ctl, GGA_DEV_OVERFLOW_UNITS);
     }
 }
 
 template <int BS>
-__device__ __forceinline__ void flush_near(const Args &a, Ctrl &C, uint32_t *sv, uint32_t *sb, uint32_t *sd,
-                                           uint32_t *sh, uint32_t nn, uint32_t nxt, uint32_t r3n, uint32_t bucket) {
+__device__ __forceinline__ void flush_near(const Args &a, Ctrl &C, uint32_t *sv, uint32_t nn, uint32_t nxt,
+                                           uint32_t r3n, uint32_t bucket) {
     if (nn == 0) return;
     const uint32_t tid = threadIdx.x;
     const bool lh = a.light != nullptr; /* the same in every thread */
@@ -192,18 +189,17 @@ __device__ __forceinline__ void flush_near(const Args &a, Ctrl &C, uint32_t *sv,
         uint32_t b, d;
         item_range(a, v, b, d);
         const uint32_t dl = lh ? __ldg(a.light + v) : d;
-        sb[j] = b;
-        sd[j] = dl;
         if (dl) local += (1ull << 32) | dl;
         if (lh) {
             const uint32_t hd = d - dl;
-            const bool first = hd && atomicExch(a.hstamp + v, bucket + 1) != bucket + 1;
-            sh[j] = first ? hd : 0u;
-            if (first) hlocal += (1ull << 32) | hd;
+            if (hd && atomicExch(a.hstamp + v, bucket + 1) != bucket + 1) {
+                hlocal += (1ull << 32) | hd;
+                sv[j] = v | HEAVY_MARK;
+            }
         }
     }
     unsigned long long tot, htot = 0;
-    const unsigned long long run = block_exclusive_scan64(local, C.ws64, &tot);
+    unsigned long long run = block_exclusive_scan64(local, C.ws64, &tot);
     unsigned long long hrun = 0;
     if (lh) hrun = block_exclusive_scan64(hlocal, C.ws64, &htot);
     if (tid == 0) {
@@ -215,12 +211,25 @@ __device__ __forceinline__ void flush_near(const Args &a, Ctrl &C, uint32_t *sv,
         C.hbase_e = (uint32_t)hold;
     }
     __syncthreads();
-    put_entries(a, j0, j1, sv, sb, sd, run, C.base_i, C.base_e, sel(nxt, a.qv0, a.qv1), sel(nxt, a.qo0, a.qo1),
-                sel(nxt, a.qb0, a.qb1), sel(nxt, a.uf0, a.uf1));
-    if (lh) {
-        for (uint32_t j = j0; j < j1; ++j) sb[j] += sd[j]; /* heavy edges start after the light ones */
-        put_entries(a, j0, j1, sv, sb, sh, hrun, C.hbase_i, C.hbase_e, sel3(hl, a.hv0, a.hv1, a.hv2),
-                    sel3(hl, a.ho0, a.ho1, a.ho2), sel3(hl, a.hb0, a.hb1, a.hb2), sel3(hl, a.huf0, a.huf1, a.huf2));
+    const uint32_t bi = C.base_i, be = C.base_e, hbi = C.hbase_i, hbe = C.hbase_e;
+    uint32_t *qv = sel(nxt, a.qv0, a.qv1), *qo = sel(nxt, a.qo0, a.qo1), *qb = sel(nxt, a.qb0, a.qb1);
+    uint32_t *uf = sel(nxt, a.uf0, a.uf1);
+    for (uint32_t j = j0; j < j1; ++j) {
+        const uint32_t raw = sv[j], v = raw & ~HEAVY_MARK;
+        uint32_t b, d;
+        item_range(a, v, b, d);
+        const uint32_t dl = lh ? __ldg(a.light + v) : d;
+        if (dl) {
+            put_entry(a, bi + (uint32_t)(run >> 32), be + (uint32_t)run, v, b, dl, qv, qo, qb, uf);
+            run += (1ull << 32) | dl;
+        }
+        if (raw & HEAVY_MARK) { /* heavy edges start after the light ones */
+            const uint32_t hd = d - dl;
+            put_entry(a, hbi + (uint32_t)(hrun >> 32), hbe + (uint32_t)hrun, v, b + dl, hd,
+                      sel3(hl, a.hv0, a.hv1, a.hv2), sel3(hl, a.ho0, a.ho1, a.ho2), sel3(hl, a.hb0, a.hb1, a.hb2),
+                      sel3(hl, a.huf0, a.huf1, a.huf2));
+            hrun += (1ull << 32) | hd;
+        }
     }
     __syncthreads();
     if (tid == 0) C.nn = 0;
@@ -248,7 +257,7 @@ __device__ __forceinline__ void flush_far(const Args &a, Ctrl &C, uint32_t *sf, 
 /* Block-uniform checkpoint: wait for all staging, read the counts, and
  * publish a buffer when it is at least `limit` full (limit 1 = always). */
 struct Stage {
-    uint32_t *sv, *sb, *sd, *sh, *sf;
+    uint32_t *sv, *sf; /* staged near-queue vertices, far-pile vertices */
 };
 
 template <int BS, bool SSSP>
@@ -257,7 +266,7 @@ __device__ __forceinline__ void checkpoint(const Args &a, Ctrl &C, const Stage &
     __syncthreads();
     const uint32_t nn = C.nn, fn = SSSP ? C.fn : 0u;
     __syncthreads();
-    if (nn >= limit) flush_near<BS>(a, C, S.sv, S.sb, S.sd, S.sh, nn, nxt, r3n, bucket);
+    if (nn >= limit) flush_near<BS>(a, C, S.sv, nn, nxt, r3n, bucket);
     if (SSSP && fn >= limit) flush_far<BS>(a, C, S.sf, fn, fp);
 }
 
@@ -414,7 +423,7 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
          * the next take() (after the table barrier below), so no second
          * barrier is needed before those writes */
         const uint32_t k = C.unit, i0 = C.i0, cnt = C.cnt, nn = C.nn, fn = SSSP ? C.fn : 0u;
-        if (nn >= BS) flush_near<BS>(a, C, S.sv, S.sb, S.sd, S.sh, nn, nxt, r3n, bucket);
+        if (nn >= BS) flush_near<BS>(a, C, S.sv, nn, nxt, r3n, bucket);
         if (SSSP && fn >= BS) flush_far<BS>(a, C, S.sf, fn, fp);
         if (k >= units) break;
         const uint32_t ebase = k * U, eend = min(ebase + U, total);
@@ -498,10 +507,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
     uint32_t *stage = dyn + (SSSP ? 3u : 2u) * (U + 1);
     Stage S;
     S.sv = stage;
-    S.sb = stage + SC;
-    S.sd = stage + 2 * SC;
-    S.sf = stage + 3 * SC;
-    S.sh = stage + 4 * SC;
+    S.sf = stage + SC;
     uint32_t gen = 0;
     unsigned long long relaxed = 0;
 
@@ -710,7 +716,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
 
 template <int BS, bool SSSP>
 size_t dyn_smem(uint32_t unit, uint32_t scap) {
-    return ((size_t)(unit + 1) * (SSSP ? 3 : 2) + (size_t)scap * (SSSP ? 5 : 3)) * sizeof(uint32_t);
+    return ((size_t)(unit + 1) * (SSSP ? 3 : 2) + (size_t)scap * (SSSP ? 2 : 1)) * sizeof(uint32_t);
 }
 
 template <int BS, bool SSSP>
@@ -819,9 +825,9 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     a.ucap = s->ucap;
     a.src = src;
     const uint32_t bs = p.block_threads ? p.block_threads : 256;
-    /* measured on R-MAT 22 (GB300): BFS is fastest with 2048-edge units,
-     * SSSP with 1024-edge units (one batch of edges per thread per unit) */
-    a.iters = p.unit_iters ? p.unit_iters : (sssp ? 4 : 8);
+    /* 2048-edge units at 256 threads: one batch of STAGE_BATCH edges per
+     * thread per unit, so a unit's loads are all in flight together */
+    a.iters = p.unit_iters ? p.unit_iters : 8;
     if (a.iters < 2 || a.iters > 16)
         return gga_fail(GGA_ERR_INVALID_ARG, "unit_iters must be in [2, 16] (got %u)", a.iters);
     a.unit = bs * a.iters;

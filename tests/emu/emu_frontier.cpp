@@ -21,7 +21,7 @@ int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint
     a.dist = dist.data(); a.bits = bits.data(); a.farbits = farbits.data(); a.stamp = stamp.data();
     a.qv0 = q[0].data(); a.qv1 = q[1].data(); a.qo0 = q[2].data(); a.qo1 = q[3].data(); a.qb0 = q[4].data(); a.qb1 = q[5].data();
     a.uf0 = uf[0].data(); a.uf1 = uf[1].data(); a.far0 = far[0].data(); a.far1 = far[1].data(); a.far2 = far[2].data();
-    a.ctl = &ctl; a.cap = cap; a.ucap = ucap; a.src = src; a.iters = iters; a.unit = BS * iters; a.scap = BS * 5;
+    a.ctl = &ctl; a.cap = cap; a.ucap = ucap; a.src = src; a.iters = iters; a.unit = BS * iters; a.scap = BS * 9;
     a.delta = delta; a.nblocks = NB; a.max_rounds = 4 * n + 4096; a.timeout_ns = 60000000000ull;
     a.bu = bu; a.alpha = alpha; a.beta = beta;
     std::vector<uint32_t> lcol(m + 4), lwt(m + 4), light(n + 1), hstamp(cap), hq[9], huf[3];
