@@ -43,7 +43,7 @@ namespace {
 constexpr uint32_t NONE = 0xffffffffu;
 constexpr uint32_t MIN_UNIT = 512;  /* smallest edges-per-unit the buffers are sized for */
 constexpr uint32_t MAX_UNIT = 4096; /* largest edges-per-unit (shared-memory bound) */
-constexpr uint32_t STAGE_BATCH = 8; /* edges per thread in flight between staging checkpoints */
+constexpr uint32_t STAGE_BATCH = 4; /* edges per thread in flight between staging checkpoints */
 
 struct Args {
     const uint32_t *off, *col, *wt, *cc;
@@ -342,48 +342,6 @@ __device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, u
     }
 }
 
-/* Relax one edge to v with candidate distance alt (atomicMin on uint32, as
- * M_my_drelax does, cudaKernels.h:323-330); reports whether v joins the
- * near queue or the far pile (farval = its new distance). */
-template <bool SSSP>
-__device__ __forceinline__ void relax_edge(const Args &a, uint32_t v, uint32_t alt, uint32_t probe, uint32_t round,
-                                           uint32_t thr, bool &near, bool &far, uint32_t &farval) {
-    /* probe: a recent read of the visited word (BFS) or of dist[v] (SSSP);
-     * it may be stale but never lower than the truth, so it only filters */
-    near = false;
-    far = false;
-    farval = NONE;
-    if (!SSSP) {
-        const uint32_t bit = 1u << (v & 31);
-        if (!(probe & bit)) {
-            const uint32_t old = atomicOr(a.bits + (v >> 5), bit);
-            if (!(old & bit)) {
-                a.dist[v] = alt;
-                if (a.cc) {
-                    const uint32_t c = a.cc[v];
-                    for (uint32_t k = 1; k <= c; ++k) a.dist[v + k] = alt;
-                }
-                near = true;
-            }
-        }
-    } else if (alt < probe) {
-        const uint32_t old = atomicMin(a.dist + v, alt);
-        if (alt < old) {
-            if (a.cc) {
-                const uint32_t c = a.cc[v];
-                for (uint32_t k = 1; k <= c; ++k) atomicMin(a.dist + v + k, alt);
-            }
-            if (alt < thr) {
-                near = atomicExch(a.stamp + v, round + 1) != round + 1;
-            } else {
-                farval = alt;
-                const uint32_t bit = 1u << (v & 31);
-                far = !(atomicOr(a.farbits + (v >> 5), bit) & bit);
-            }
-        }
-    }
-}
-
 /* Expand one list of queue entries (the round's near queue, or a bucket's
  * heavy list): CTAs take units of U edges by ticket from *work, load the
  * unit's entries into shared memory and give consecutive edges to
@@ -464,17 +422,69 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
 #pragma unroll
             for (uint32_t q = 0; q < PB; ++q)
                 probe[q] = act[q] ? (SSSP ? __ldcg(a.dist + v[q]) : __ldcg(a.bits + (v[q] >> 5))) : 0u;
+            /* updates in phases, so a thread's atomics for its PB edges are in
+             * flight together instead of one dependent pair after another:
+             * first the distance atomicMin / visited atomicOr of every edge,
+             * then the stamp / far-bit atomic of every improved one, then the
+             * shared-memory staging.  Relaxation is atomicMin on uint32
+             * distances as M_my_drelax does (cudaKernels.h:323-330); the
+             * probe (a recent read of dist[v] or of the visited word) may be
+             * stale but never lower than the truth, so it only filters. */
+            uint32_t won = 0; /* bit q: edge q improved v (SSSP) or visited it first (BFS) */
 #pragma unroll
             for (uint32_t q = 0; q < PB; ++q) {
                 if (!act[q]) continue;
-                bool nr, fr;
-                uint32_t fv;
-                relax_edge<SSSP>(a, v[q], alt[q], probe[q], round, thr, nr, fr, fv);
-                if (nr) stage_near(a, C, S.sv, v[q]);
-                if (SSSP && fv != NONE) {
-                    atomicMin(&C.fmin, fv);
-                    if (fr) stage_far(a, C, S.sf, v[q]);
+                if (SSSP) {
+                    if (alt[q] < probe[q] && alt[q] < atomicMin(a.dist + v[q], alt[q])) won |= 1u << q;
+                } else {
+                    const uint32_t bit = 1u << (v[q] & 31);
+                    if (!(probe[q] & bit) && !(atomicOr(a.bits + (v[q] >> 5), bit) & bit)) won |= 1u << q;
                 }
+            }
+            uint32_t nearm = 0, farm = 0, fmin = NONE;
+#pragma unroll
+            for (uint32_t q = 0; q < PB; ++q) {
+                if (!((won >> q) & 1u)) continue;
+                const uint32_t vq = v[q], aq = alt[q];
+                if (a.cc) { /* split view: the children mirror the parent */
+                    const uint32_t c = a.cc[vq];
+                    for (uint32_t k = 1; k <= c; ++k) {
+                        if (SSSP) atomicMin(a.dist + vq + k, aq);
+                        else a.dist[vq + k] = aq;
+                    }
+                }
+                if (!SSSP) {
+                    a.dist[vq] = aq;
+                    nearm |= 1u << q;
+                } else if (aq < thr) {
+                    if (atomicExch(a.stamp + vq, round + 1) != round + 1) nearm |= 1u << q;
+                } else {
+                    fmin = min(fmin, aq);
+                    const uint32_t bit = 1u << (vq & 31);
+                    if (!(atomicOr(a.farbits + (vq >> 5), bit) & bit)) farm |= 1u << q;
+                }
+            }
+            if (nearm) {
+                const uint32_t k0 = atomicAdd(&C.nn, (uint32_t)__popc(nearm));
+                uint32_t k = k0;
+#pragma unroll
+                for (uint32_t q = 0; q < PB; ++q)
+                    if ((nearm >> q) & 1u) {
+                        if (k < a.scap) S.sv[k] = v[q];
+                        else set_err(ctl, GGA_DEV_OVERFLOW);
+                        ++k;
+                    }
+            }
+            if (SSSP && fmin != NONE) atomicMin(&C.fmin, fmin);
+            if (SSSP && farm) {
+                uint32_t k = atomicAdd(&C.fn, (uint32_t)__popc(farm));
+#pragma unroll
+                for (uint32_t q = 0; q < PB; ++q)
+                    if ((farm >> q) & 1u) {
+                        if (k < a.scap) S.sf[k] = v[q];
+                        else set_err(ctl, GGA_DEV_OVERFLOW_FAR);
+                        ++k;
+                    }
             }
         }
         if (tid == 0) {
@@ -825,9 +835,9 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     a.ucap = s->ucap;
     a.src = src;
     const uint32_t bs = p.block_threads ? p.block_threads : 256;
-    /* 2048-edge units at 256 threads: one batch of STAGE_BATCH edges per
-     * thread per unit, so a unit's loads are all in flight together */
-    a.iters = p.unit_iters ? p.unit_iters : 8;
+    /* measured on R-MAT 22 (GB300): BFS is fastest with 2048-edge units,
+     * SSSP with 1024-edge units (one batch of edges per thread per unit) */
+    a.iters = p.unit_iters ? p.unit_iters : (sssp ? 4 : 8);
     if (a.iters < 2 || a.iters > 16)
         return gga_fail(GGA_ERR_INVALID_ARG, "unit_iters must be in [2, 16] (got %u)", a.iters);
     a.unit = bs * a.iters;
