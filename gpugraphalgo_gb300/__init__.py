@@ -354,9 +354,9 @@ class Context:
         cta = np.zeros(max(1, nb.value), np.uint32)
         _check(N.load().gga_trace_get(self._h, rounds, nr.value, C.byref(nr),
                                       cta.ctypes.data_as(C.POINTER(C.c_uint32)), nb.value, C.byref(nb)), "trace_get")
-        kinds = ("near", "bottom_up", "far", "heavy")
-        return {"rounds": [{"kind": kinds[r.kind] if r.kind < 4 else r.kind, "items": r.items, "edges": r.edges,
-                            "far_items": r.far_items, "us": r.ns / 1e3} for r in rounds[: nr.value]],
+        kinds = ("near", "bottom_up", "far", "heavy", "pull_scan", "pull")
+        return {"rounds": [{"kind": kinds[r.kind] if r.kind < len(kinds) else r.kind, "items": r.items,
+                            "edges": r.edges, "far_items": r.far_items, "us": r.ns / 1e3} for r in rounds[: nr.value]],
                 "cta_kcycles": cta[: nb.value]}
 
     def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False):

@@ -52,6 +52,7 @@ class GraphInfo(C.Structure):
         ("parents_with_children", u32),
         ("max_weight", u32),
         ("symmetric", i32),
+        ("wsymmetric", i32),
     ]
 
 
@@ -75,6 +76,7 @@ class Params(C.Structure):
         ("bfs_alpha", u32),
         ("bfs_beta", u32),
         ("sssp_light_heavy", u32),
+        ("sssp_pull", u32),
     ]
 
     def as_dict(self):

@@ -184,6 +184,7 @@ gga_status gga_set_params(gga_ctx *c, const gga_params *p) {
     if (p->block_threads && p->block_threads != 256 && p->block_threads != 512 && p->block_threads != 1024)
         return gga_fail(GGA_ERR_INVALID_ARG, "block_threads must be 256, 512 or 1024");
     if (p->cdp_mode > 2) return gga_fail(GGA_ERR_INVALID_ARG, "cdp_mode must be 0, 1 or 2");
+    if (p->sssp_pull > 2) return gga_fail(GGA_ERR_INVALID_ARG, "sssp_pull must be 0, 1 or 2");
     c->params = *p;
     c->params_set = true;
     return GGA_OK;
@@ -328,17 +329,23 @@ gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_
             (s = dev_graph_check_symmetric(g, c->dflag + 40, c->hflag + 40, c->st)))
             return s;
         GraphView v = dev_graph_view(d, use_split);
-        const uint32_t *light = nullptr;
+        LightHeavy lh;
         if (sssp && !use_split && p.sssp_delta && p.sssp_light_heavy == 0) {
             if ((s = dev_graph_light_heavy(g, p.sssp_delta, c->st))) return s;
+            /* pulling bucket closes need every edge's reverse with its weight */
+            if (p.sssp_pull != 1 && (d->symmetric == 0 || d->wsymmetric == 0) &&
+                (s = dev_graph_check_symmetric(g, c->dflag + 40, c->hflag + 40, c->st)))
+                return s;
             v.col = d->lcol;
             v.wt = d->lwt;
-            light = d->light;
+            lh.light = d->light;
+            lh.heavy_edges = d->lh_heavy;
+            lh.pull = p.sssp_pull == 1 || d->wsymmetric <= 0 ? 0u : (p.sssp_pull == 2 ? 2u : 1u);
         }
         if ((s = frontier_scratch_ensure(&c->fs, v.n > d->n ? v.n : d->n, d->m))) return s;
         FrontierResult r;
         s = frontier_run(&c->fs, v, use_split ? d->first : nullptr, src, sssp, p, c->sms, c->st, c->ev[0], c->ev[1], &r,
-                         c->trace_on, light);
+                         c->trace_on, lh);
         if (s) return s;
         if (c->trace_on) {
             const uint32_t nr = r.rounds < TRACE_ROUNDS ? r.rounds : TRACE_ROUNDS;

@@ -197,23 +197,28 @@ gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st) 
     const unsigned grid = grid_for(d->m ? d->m : 1, 256);
     k_light_flags<<<grid, 256, 0, st>>>(d->wt, d->m, delta, flags);
     gga_status s = dev_exclusive_scan(flags, pos, d->m, st);
+    uint32_t nlight = 0;
     if (s == GGA_OK) {
+        e = cudaMemcpyAsync(&nlight, pos + d->m, sizeof nlight, cudaMemcpyDeviceToHost, st);
         if (d->m) k_lh_scatter<<<grid, 256, 0, st>>>(d->off, d->col, d->wt, d->n, d->m, delta, pos, d->lcol, d->lwt);
         k_light_counts<<<grid_for(d->n ? d->n : 1, 256), 256, 0, st>>>(d->off, d->n, pos, d->light);
-        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) s = gga_fail(GGA_ERR_CUDA, "light/heavy order: %s", cudaGetErrorString(e));
     }
     cudaFreeAsync(flags, st);
     if (s) return s;
     if ((s = dev_wait(st, 60.0))) return s;
     d->lh_delta = delta;
+    d->lh_heavy = d->m - nlight;
     return GGA_OK;
 }
 
-/* flag bit 0: a row is not sorted; bit 1: an edge (u, v) has no (v, u).
- * One thread per edge: its row by binary search over the offsets, its
- * reverse by binary search in the target's (sorted) row. */
-__global__ void k_check_symmetric(const uint32_t *off, const uint32_t *col, uint32_t n, uint32_t m, uint32_t *flag) {
+/* flag bit 0: a row is not sorted; bit 1: an edge (u, v) has no (v, u);
+ * bit 2: the (v, u) found has another weight.  One thread per edge: its row
+ * by binary search over the offsets, its reverse by binary search in the
+ * target's (sorted) row. */
+__global__ void k_check_symmetric(const uint32_t *off, const uint32_t *col, const uint32_t *wt, uint32_t n, uint32_t m,
+                                  uint32_t *flag) {
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = n; /* largest u with off[u] <= e */
         while (hi - lo > 1) {
@@ -229,27 +234,30 @@ __global__ void k_check_symmetric(const uint32_t *off, const uint32_t *col, uint
             if (col[mid] < u) b = mid + 1; else t = mid;
         }
         if (b >= end || col[b] != u) atomicOr(flag, 2u);
+        else if (wt[b] != wt[e]) atomicOr(flag, 4u);
     }
 }
 
 gga_status dev_graph_check_symmetric(gga_graph *g, uint32_t *dflag, uint32_t *hflag, cudaStream_t st) {
     DevGraph *d = dev_graph_of(g);
     if (!d) return gga_fail(GGA_ERR_INVALID_ARG, "graph not resident");
-    if (d->symmetric != 0) return GGA_OK;
+    if (d->symmetric != 0 && d->wsymmetric != 0) return GGA_OK;
     GGA_CK(cudaMemsetAsync(dflag, 0, sizeof(uint32_t), st));
     if (d->m) {
         int sms = 0;
         GGA_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d->device));
         const uint64_t want = ((uint64_t)d->m + 255) / 256;
         const unsigned grid = (unsigned)(want < (uint64_t)sms * 16 ? want : (uint64_t)sms * 16);
-        k_check_symmetric<<<grid, 256, 0, st>>>(d->off, d->col, d->n, d->m, dflag);
+        k_check_symmetric<<<grid, 256, 0, st>>>(d->off, d->col, d->wt, d->n, d->m, dflag);
         GGA_CK(cudaGetLastError());
     }
     GGA_CK(cudaMemcpyAsync(hflag, dflag, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     gga_status s = dev_wait(st, 60.0);
     if (s) return s;
-    d->symmetric = *hflag ? -1 : 1;
+    d->symmetric = (*hflag & 3u) ? -1 : 1;
+    d->wsymmetric = *hflag ? -1 : 1;
     g->symmetric = d->symmetric;
+    g->wsymmetric = d->wsymmetric;
     return GGA_OK;
 }
 
@@ -276,6 +284,7 @@ gga_status dev_graph_ensure(gga_graph *g, int device, cudaStream_t st) {
         d->m = g->m;
         d->maxdeg = g->maxdeg;
         d->symmetric = g->symmetric;
+        d->wsymmetric = g->wsymmetric;
         size_t mpad = ((size_t)g->m + 4) & ~(size_t)3; /* room for 16-byte vector loads */
         cudaError_t e = cudaMalloc((void **)&d->off, ((size_t)g->n + 1) * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMalloc((void **)&d->col, mpad * sizeof(uint32_t));

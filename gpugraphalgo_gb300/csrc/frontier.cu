@@ -73,6 +73,10 @@ struct Args {
     const uint32_t *light; /* n: light edges per row */
     uint32_t *hstamp;      /* n: last bucket (+1) a vertex joined a heavy list */
     uint32_t *hv0, *hv1, *hv2, *ho0, *ho1, *ho2, *hb0, *hb1, *hb2, *huf0, *huf1, *huf2;
+    /* bucket closes by pull (every edge's reverse has its weight): 0 never,
+     * 1 when the cost rule picks it, 2 always */
+    uint32_t pull;
+    uint32_t heavy_edges; /* edges with w >= delta */
 };
 
 /* Round record (block 0, thread 0) when tracing. */
@@ -121,7 +125,6 @@ __device__ __forceinline__ void item_range(const Args &a, uint32_t v, uint32_t &
 struct Ctrl {
     uint32_t nn, fn, fmin;   /* staged near / far counts, smallest far distance */
     uint32_t base_i, base_e; /* flush allocation */
-    uint32_t unit, i0, cnt;  /* current unit */
     uint32_t nitems, total, fc, fm;
     uint32_t hbase_i, hbase_e, hn, htot; /* heavy list: flush allocation, size at round start */
     uint32_t ws[32];         /* block-scan scratch */
@@ -342,60 +345,123 @@ __device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, u
     }
 }
 
+/* First half of a pulling bucket close (SSSP, light/heavy mode): list every
+ * unsettled vertex (d >= thr) that has heavy edges as a queue entry over
+ * those edges, in the next round's queue, where expand_units<PULL> relaxes
+ * them from the settled side.  A warp takes 32 x PV consecutive vertices per
+ * step, lane i vertices 32q + i, so the distance, offset and light-count
+ * loads are coalesced and PV of each are in flight per lane; the warp's
+ * entries are allocated with one packed 64-bit atomicAdd (entries << 32 |
+ * edges), as bottom_up_round does.  Trip counts are warp-uniform; no CTA
+ * barrier is used. */
+template <int BS>
+__device__ __forceinline__ void pull_scan(const Args &a, uint32_t thr, uint32_t nxt, uint32_t r3n) {
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr uint32_t PV = 4;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t gw = ((uint64_t)blockIdx.x * BS + threadIdx.x) >> 5, nw = ((uint64_t)gridDim.x * BS) >> 5;
+    const uint64_t steps = ((uint64_t)a.n + 32 * PV - 1) / (32 * PV);
+    uint32_t *qv = sel(nxt, a.qv0, a.qv1), *qo = sel(nxt, a.qo0, a.qo1), *qb = sel(nxt, a.qb0, a.qb1);
+    uint32_t *uf = sel(nxt, a.uf0, a.uf1);
+    for (uint64_t w = gw; w < steps; w += nw) {
+        uint32_t b[PV], hd[PV], dv[PV];
+        const uint64_t v0 = w * 32 * PV + lane;
+#pragma unroll
+        for (uint32_t q = 0; q < PV; ++q) dv[q] = v0 + 32 * q < a.n ? __ldcg(a.dist + v0 + 32 * q) : 0u;
+        uint32_t cnt = 0, edges = 0;
+#pragma unroll
+        for (uint32_t q = 0; q < PV; ++q) {
+            b[q] = 0;
+            hd[q] = 0;
+            if (dv[q] >= thr) { /* unsettled (0 past the end) */
+                const uint32_t v = (uint32_t)(v0 + 32 * q);
+                const uint32_t o0 = __ldg(a.off + v);
+                b[q] = o0 + __ldg(a.light + v);
+                hd[q] = __ldg(a.off + v + 1) - b[q];
+                cnt += hd[q] ? 1u : 0u;
+                edges += hd[q];
+            }
+        }
+        uint32_t ic = cnt, ie = edges;
+#pragma unroll
+        for (int k = 1; k < 32; k <<= 1) {
+            const uint32_t yc = __shfl_up_sync(FULL, ic, k), ye = __shfl_up_sync(FULL, ie, k);
+            if (lane >= (uint32_t)k) {
+                ic += yc;
+                ie += ye;
+            }
+        }
+        const uint32_t tc = __shfl_sync(FULL, ic, 31), te = __shfl_sync(FULL, ie, 31);
+        if (tc == 0) continue; /* warp-uniform */
+        unsigned long long old = 0;
+        if (lane == 0) old = atomicAdd(&a.ctl->qctr[r3n], ((unsigned long long)tc << 32) | (unsigned long long)te);
+        old = __shfl_sync(FULL, old, 0);
+        uint32_t i = (uint32_t)(old >> 32) + ic - cnt, o = (uint32_t)old + ie - edges;
+#pragma unroll
+        for (uint32_t q = 0; q < PV; ++q)
+            if (hd[q]) {
+                put_entry(a, i, o, (uint32_t)(v0 + 32 * q), b[q], hd[q], qv, qo, qb, uf);
+                ++i;
+                o += hd[q];
+            }
+    }
+}
+
 /* Expand one list of queue entries (the round's near queue, or a bucket's
- * heavy list): CTAs take units of U edges by ticket from *work, load the
- * unit's entries into shared memory and give consecutive edges to
- * consecutive threads.  Each thread handles PB edges at a time in three
- * passes (edge loads, then distance/bitmap probes, then updates), so PB
- * independent memory chains are in flight per thread instead of one.
- * Improvements at or above thr go to the far pile (thr = 0 sends all of them
- * there).  Block-uniform: every thread runs the same tickets and
- * checkpoints. */
-template <int BS, bool SSSP>
+ * heavy list): units of U edges are dealt round-robin (CTA b takes units b,
+ * b + G, b + 2G, ...); each CTA loads its unit's entries into shared memory
+ * and gives consecutive edges to consecutive threads.  Units hold equal edge
+ * counts, so the static deal balances like a ticket counter would, without
+ * an atomic on the path, and the next unit's bounds load while the current
+ * one is expanded.  Each thread handles PB edges at a time in three passes
+ * (edge loads, then distance/bitmap probes, then updates), so PB independent
+ * memory chains are in flight per thread instead of one.  Improvements at or
+ * above thr go to the far pile (thr = 0 sends all of them there).
+ * Block-uniform: every thread runs the same units and checkpoints.
+ *
+ * PULL (SSSP): the entries are unsettled vertices and their heavy edges;
+ * an edge whose other end u is settled (d(u) < thr) offers d(u) + w to the
+ * entry's vertex, and every improvement goes to the far pile. */
+template <int BS, bool SSSP, bool PULL = false>
 __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage &S, uint32_t *t_o, uint32_t *t_b,
                                              uint32_t *t_du, const uint32_t *qv, const uint32_t *qo,
                                              const uint32_t *qb, const uint32_t *uf, uint32_t nitems, uint32_t total,
-                                             uint32_t units, uint32_t *work, uint32_t round, uint32_t thr,
-                                             uint32_t nxt, uint32_t r3n, uint32_t fp, uint32_t bucket,
+                                             uint32_t units, uint32_t round, uint32_t thr, uint32_t nxt,
+                                             uint32_t r3n, uint32_t fp, uint32_t bucket,
                                              unsigned long long &relaxed) {
-    const uint32_t tid = threadIdx.x, U = a.unit;
+    const uint32_t tid = threadIdx.x, U = a.unit, G = gridDim.x;
     FrontierCtl *ctl = a.ctl;
-    /* Two CTA barriers per unit: thread 0 takes the NEXT unit's ticket while
-     * the CTA works on the current one, and the barrier that publishes it
-     * also ends the unit's staging (the checkpoint's count read), so the
-     * flush and the next table load follow without further barriers. */
-    auto take = [&]() {
-        const uint32_t k = atomicAdd(work, 1u);
-        C.unit = k;
-        if (k < units) {
-            const uint32_t i0 = min(__ldcg(uf + k), nitems - 1);
-            const uint32_t i1 = k + 1 < units ? min(__ldcg(uf + k + 1), nitems - 1) : nitems - 1;
-            C.i0 = i0;
-            C.cnt = i1 >= i0 ? min(i1 - i0 + 1, U + 1) : 1u;
-        }
+    /* entries [i0, i0 + cnt) hold unit k's edges (every thread reads the
+     * same two boundary words) */
+    auto bounds = [&](uint32_t k, uint32_t &i0, uint32_t &cnt) {
+        i0 = min(__ldcg(uf + k), nitems - 1);
+        const uint32_t i1 = k + 1 < units ? min(__ldcg(uf + k + 1), nitems - 1) : nitems - 1;
+        cnt = i1 >= i0 ? min(i1 - i0 + 1, U + 1) : 1u;
     };
-    if (tid == 0) take();
+    uint32_t k = blockIdx.x, i0 = 0, cnt = 0;
+    if (k < units) bounds(k, i0, cnt);
     for (;;) {
-        __syncthreads(); /* ticket published; previous unit's table reads and staging done */
-        /* C is next rewritten inside a flush (after its own barriers) or by
-         * the next take() (after the table barrier below), so no second
-         * barrier is needed before those writes */
-        const uint32_t k = C.unit, i0 = C.i0, cnt = C.cnt, nn = C.nn, fn = SSSP ? C.fn : 0u;
+        __syncthreads(); /* previous unit's table reads and staging done */
+        const uint32_t nn = C.nn, fn = SSSP ? C.fn : 0u;
         if (nn >= BS) flush_near<BS>(a, C, S.sv, nn, nxt, r3n, bucket);
         if (SSSP && fn >= BS) flush_far<BS>(a, C, S.sf, fn, fp);
         if (k >= units) break;
+        const uint32_t kn = k + G;
+        uint32_t ni0 = 0, ncnt = 0;
+        if (kn < units) bounds(kn, ni0, ncnt); /* used after this unit */
         const uint32_t ebase = k * U, eend = min(ebase + U, total);
         for (uint32_t j = tid; j < cnt; j += BS) {
             const uint32_t i = i0 + j;
             t_o[j] = __ldcg(qo + i);
             t_b[j] = __ldcg(qb + i);
-            if (SSSP) t_du[j] = __ldcg(a.dist + __ldcg(qv + i));
+            /* the entry's distance, or in a pull its vertex */
+            if (SSSP) t_du[j] = PULL ? __ldcg(qv + i) : __ldcg(a.dist + __ldcg(qv + i));
         }
         __syncthreads();
         constexpr uint32_t PB = STAGE_BATCH;
         for (uint32_t it0 = 0; it0 < a.iters; it0 += PB) {
             if (it0) checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, BS);
-            uint32_t v[PB], alt[PB], probe[PB];
+            uint32_t v[PB], alt[PB], probe[PB], tgt[PB];
             bool act[PB];
 #pragma unroll
             for (uint32_t q = 0; q < PB; ++q) {
@@ -403,6 +469,7 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                 act[q] = it0 + q < a.iters && e < eend;
                 v[q] = 0;
                 alt[q] = 0;
+                tgt[q] = 0;
                 if (act[q]) {
                     uint32_t lo = 0, hi = cnt; /* last j with t_o[j] <= e */
                     while (hi - lo > 1) {
@@ -412,7 +479,12 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                     const uint32_t ei = t_b[lo] + (e - t_o[lo]);
                     if (ei < a.m) {
                         v[q] = __ldg(a.col + ei);
-                        alt[q] = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
+                        if (PULL) {
+                            alt[q] = __ldg(a.wt + ei);
+                            tgt[q] = t_du[lo];
+                        } else {
+                            alt[q] = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
+                        }
                     } else { /* unreachable by construction; keeps reads in bounds */
                         set_err(ctl, GGA_DEV_BAD_EDGE);
                         act[q] = false;
@@ -422,6 +494,15 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
 #pragma unroll
             for (uint32_t q = 0; q < PB; ++q)
                 probe[q] = act[q] ? (SSSP ? __ldcg(a.dist + v[q]) : __ldcg(a.bits + (v[q] >> 5))) : 0u;
+            if (PULL) { /* the offer d(u) + w to the entry's vertex, from settled u only */
+#pragma unroll
+                for (uint32_t q = 0; q < PB; ++q) {
+                    act[q] = act[q] && probe[q] < thr;
+                    alt[q] += probe[q];
+                    v[q] = tgt[q];
+                    probe[q] = NONE;
+                }
+            }
             /* updates in phases, so a thread's atomics for its PB edges are in
              * flight together instead of one dependent pair after another:
              * first the distance atomicMin / visited atomicOr of every edge,
@@ -456,7 +537,7 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                 if (!SSSP) {
                     a.dist[vq] = aq;
                     nearm |= 1u << q;
-                } else if (aq < thr) {
+                } else if (!PULL && aq < thr) {
                     if (atomicExch(a.stamp + vq, round + 1) != round + 1) nearm |= 1u << q;
                 } else {
                     fmin = min(fmin, aq);
@@ -487,10 +568,10 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                     }
             }
         }
-        if (tid == 0) {
-            relaxed += eend - ebase;
-            take();
-        }
+        if (tid == 0) relaxed += eend - ebase;
+        k = kn;
+        i0 = ni0;
+        cnt = ncnt;
     }
 }
 
@@ -570,7 +651,9 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
     uint32_t fp = 0;
     uint32_t round = 0;
     uint32_t bucket = 0;          /* SSSP: far passes so far (same value in every block) */
-    bool heavy_done = false;      /* this bucket's heavy list was expanded */
+    bool heavy_done = false;      /* this bucket's heavy list was expanded (or pulled) */
+    bool pulling = false;         /* this round's queue is a pull list */
+    uint64_t hsettled = 0;        /* heavy edges of the closed buckets' vertices */
     bool bottom_up = false;       /* BFS direction of the current round */
     uint64_t unexplored = a.m;    /* edges of vertices not yet reached (same value in every block) */
     unsigned long long busy = 0;  /* thread 0: cycles from round start to the barrier */
@@ -615,21 +698,34 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
             break;
         }
         if (blockIdx.x == 0 && tid == 0) {
-            const uint32_t r3nn = (round + 2) % 3;
-            ctl->qctr[r3nn] = 0;
-            ctl->work[r3nn] = 0;
+            ctl->qctr[(round + 2) % 3] = 0;
         }
         if (units == 0) {
+            pulling = false;
             if (lh && !heavy_done && hunits > 0) {
                 /* ---- bucket closes: its vertices' distances are final, so
                  * their heavy edges (w >= delta, results >= thr) are relaxed
                  * once, all into the far pile */
                 heavy_done = true;
+                hsettled += htot;
+                /* by pull when the unsettled vertices' heavy edges (plus a
+                 * scan of every vertex) are far fewer than the bucket's: the
+                 * same relaxations seen from the other end (edge (u, v, w)
+                 * is also (v, u, w)), done in this round's scan and the next
+                 * round's expansion */
+                const uint64_t hleft = a.heavy_edges > hsettled ? a.heavy_edges - hsettled : 0;
+                if (a.pull == 2 || (a.pull == 1 && (uint64_t)htot > 2 * hleft + a.n / 2)) {
+                    trace_round(a, round, 4, hn, htot, fc);
+                    pull_scan<BS>(a, thr, nxt, r3n);
+                    pulling = true;
+                    if (a.trace && tid == 0) busy += clock64() - t_round;
+                    if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+                    continue;
+                }
                 trace_round(a, round, 3, hn, htot, fc);
                 expand_units<BS, SSSP>(a, C, S, t_o, t_b, t_du, sel3(hl, a.hv0, a.hv1, a.hv2),
                                        sel3(hl, a.ho0, a.ho1, a.ho2), sel3(hl, a.hb0, a.hb1, a.hb2),
-                                       sel3(hl, a.huf0, a.huf1, a.huf2), hn, htot, hunits, &ctl->hwork[hl], round,
-                                       0u, nxt, r3n, fp, bucket, relaxed);
+                                       sel3(hl, a.huf0, a.huf1, a.huf2), hn, htot, hunits, round, 0u, nxt, r3n, fp, bucket, relaxed);
                 checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, 1);
                 if (tid == 0 && C.fmin != NONE) {
                     atomicMin(&ctl->far_min[fp], C.fmin);
@@ -658,9 +754,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
                 ctl->far_phases++;
                 /* heavy lists rotate by bucket the same way: the one after
                  * the new bucket's was expanded two buckets ago */
-                const uint32_t hdead = (bucket + 1) % 3;
-                ctl->hctr[hdead] = 0;
-                ctl->hwork[hdead] = 0;
+                ctl->hctr[(bucket + 1) % 3] = 0;
             }
             trace_round(a, round, 2, fc, 0, fc);
             const uint32_t *fin = sel3(fp, a.far0, a.far1, a.far2);
@@ -703,10 +797,25 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
                 continue;
             }
         }
+        if (SSSP && pulling) {
+            /* ---- second half of a pulling bucket close */
+            pulling = false;
+            trace_round(a, round, 5, nitems, total, fc);
+            expand_units<BS, SSSP, true>(a, C, S, t_o, t_b, t_du, sel(cur, a.qv0, a.qv1), sel(cur, a.qo0, a.qo1),
+                                         sel(cur, a.qb0, a.qb1), sel(cur, a.uf0, a.uf1), nitems, total, units, round,
+                                         thr, nxt, r3n, fp, bucket, relaxed);
+            checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, 1);
+            if (tid == 0 && C.fmin != NONE) {
+                atomicMin(&ctl->far_min[fp], C.fmin);
+                C.fmin = NONE;
+            }
+            if (a.trace && tid == 0) busy += clock64() - t_round;
+            if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+            continue;
+        }
         trace_round(a, round, 0, nitems, total, fc);
         expand_units<BS, SSSP>(a, C, S, t_o, t_b, t_du, sel(cur, a.qv0, a.qv1), sel(cur, a.qo0, a.qo1),
-                               sel(cur, a.qb0, a.qb1), sel(cur, a.uf0, a.uf1), nitems, total, units, &ctl->work[r3],
-                               round, thr, nxt, r3n, fp, bucket, relaxed);
+                               sel(cur, a.qb0, a.qb1), sel(cur, a.uf0, a.uf1), nitems, total, units, round, thr, nxt, r3n, fp, bucket, relaxed);
         checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, 1);
         if (SSSP && tid == 0 && C.fmin != NONE) {
             atomicMin(&ctl->far_min[fp], C.fmin);
@@ -814,7 +923,7 @@ gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m) {
 
 gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_t *first, uint32_t src,
                         bool sssp, const gga_params &p, int sms, cudaStream_t st, cudaEvent_t ev0,
-                        cudaEvent_t ev1, FrontierResult *res, bool trace, const uint32_t *light) {
+                        cudaEvent_t ev1, FrontierResult *res, bool trace, const LightHeavy &lh) {
     Args a;
     memset(&a, 0, sizeof a);
     if (trace) {
@@ -847,8 +956,10 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     a.scap = bs * (STAGE_BATCH + 1); /* < BS staged after a checkpoint, + one batch */
     a.delta = p.sssp_delta;
     a.bu = !sssp && view.cc == nullptr && view.symmetric && p.bfs_direction == 0;
-    if (sssp && light && a.delta) {
-        a.light = light;
+    if (sssp && lh.light && a.delta) {
+        a.light = lh.light;
+        a.pull = lh.pull;
+        a.heavy_edges = lh.heavy_edges;
         a.hstamp = s->hstamp;
         a.hv0 = s->hv[0]; a.hv1 = s->hv[1]; a.hv2 = s->hv[2];
         a.ho0 = s->ho[0]; a.ho1 = s->ho[1]; a.ho2 = s->ho[2];

@@ -10,12 +10,10 @@ struct FrontierCtl {
     uint32_t err;
     uint32_t rounds;
     unsigned long long qctr[3];   /* near queue: (entries << 32) | edges, rotating by round */
-    uint32_t work[3];             /* work-unit tickets, rotating by round */
     uint32_t far_count[3];        /* three far piles rotate across far passes */
     uint32_t far_min[3];
     uint32_t far_phases;
     unsigned long long hctr[3];   /* SSSP heavy lists: (entries << 32) | edges, rotating by bucket */
-    uint32_t hwork[3];            /* heavy-round unit tickets */
     uint32_t overflow_at;
     unsigned long long edges_relaxed;
     uint32_t diag[16];            /* first failed self-check: where and what */
@@ -58,12 +56,20 @@ constexpr size_t TRACE_WORDS = (size_t)(TRACE_ROUNDS + 1) * TRACE_REC + TRACE_MA
 gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m);
 void frontier_scratch_free(FrontierScratch *s);
 
+/* SSSP light/heavy edge classes of an unsplit graph (light == NULL: off). */
+struct LightHeavy {
+    const uint32_t *light = nullptr; /* n: light edges per row, rows in light-first order */
+    uint32_t heavy_edges = 0;        /* edges with w >= delta */
+    uint32_t pull = 0;               /* bucket closes by pull: 0 never, 1 by the cost rule, 2 always (every
+                                      * edge's reverse must have its weight) */
+};
+
 /* Runs one single-source BFS (sssp=false) or SSSP over `view`.  `first`
  * (split view) maps the original source to its split parent id; NULL for the
- * unsplit view.  `light` (SSSP, unsplit, delta > 0): light edges per row, with
- * view.col / view.wt in light-first row order; turns on delta-stepping's
- * light/heavy edge classes.  Distances land in s->dist (view ids). */
+ * unsplit view.  `lh.light` (SSSP, unsplit, delta > 0): light edges per row,
+ * with view.col / view.wt in light-first row order; turns on
+ * delta-stepping's light/heavy edge classes.  Distances land in s->dist
+ * (view ids). */
 gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_t *first, uint32_t src,
                         bool sssp, const gga_params &p, int sms, cudaStream_t st, cudaEvent_t ev0,
-                        cudaEvent_t ev1, FrontierResult *res, bool trace = false,
-                        const uint32_t *light = nullptr);
+                        cudaEvent_t ev1, FrontierResult *res, bool trace = false, const LightHeavy &lh = {});

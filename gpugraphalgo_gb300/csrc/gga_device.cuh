@@ -27,12 +27,14 @@ struct DevGraph {
     uint32_t *wt;  /* m */
     uint32_t maxdeg;
     int symmetric; /* 1 yes, -1 no (or rows unsorted), 0 not checked */
+    int wsymmetric; /* symmetric with equal weights both ways: 1 yes, -1 no, 0 not checked */
 
     /* delta-stepping light/heavy order of every row for bucket width lh_delta:
      * edges with w < lh_delta first, then the rest, each group in CSR order */
     uint32_t lh_delta;
     uint32_t *lcol, *lwt; /* m each */
     uint32_t *light;      /* n: light edges of each row */
+    uint32_t lh_heavy;    /* edges with w >= lh_delta */
 
     /* node split (graph.h:415-522) */
     int32_t level, buckets;

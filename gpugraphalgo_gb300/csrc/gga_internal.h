@@ -31,6 +31,7 @@ struct gga_graph {
     uint32_t maxw;
     double wavg;    /* mean edge weight (1 for an edgeless graph) */
     int symmetric;
+    int wsymmetric; /* every edge's reverse has the same weight: 1 yes, -1 no, 0 not known */
 
     /* node split (graph.h:415-522); arrays live on the device */
     int32_t split_level;

@@ -135,6 +135,7 @@ gga_status gga_graph_get_info(const gga_graph *g, gga_graph_info *info) {
     info->parents_with_children = g->split_level ? g->parents_with_children : 0;
     info->max_weight = g->maxw;
     info->symmetric = g->symmetric;
+    info->wsymmetric = g->wsymmetric;
     return GGA_OK;
 }
 
@@ -485,6 +486,7 @@ static gga_status csr_from_pairs(uint32_t n, const uint32_t *a, const uint32_t *
     run_threads(nt, csr_worker, jobs, sizeof jobs[0]);
     free(tmp); free(toff); free(udeg);
     g->symmetric = 1;
+    g->wsymmetric = 1; /* pair_weight depends on the unordered pair only */
     gga_graph_refresh_stats(g);
     *out = g;
     return GGA_OK;

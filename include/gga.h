@@ -96,6 +96,8 @@ typedef struct gga_graph_info {
     uint32_t max_weight;
     int32_t symmetric;     /* 1 symmetric (generated, or checked on the device), -1 checked: not
                             * symmetric or rows unsorted, 0 not known yet */
+    int32_t wsymmetric;    /* the same, and every edge's reverse has its weight (what a
+                            * pulling SSSP bucket close needs) */
 } gga_graph_info;
 
 /* ---- errors ----------------------------------------------------------- */
@@ -228,6 +230,14 @@ typedef struct gga_params {
      * vertices relax their heavy edges once when the bucket closes);
      * 1 = every near round relaxes all edges.  Distances are the same. */
     uint32_t sssp_light_heavy;
+    /* SSSP bucket close in light/heavy mode.  On graphs whose every edge has
+     * its reverse with the same weight a bucket may close by pulling: each
+     * unsettled vertex takes the smallest d(u) + w over its heavy edges to
+     * settled vertices, instead of the bucket's vertices pushing all their
+     * heavy edges.  0 = pull when the bucket's heavy edges outnumber twice
+     * the unsettled vertices' heavy edges plus n/2; 1 = always push;
+     * 2 = always pull (where allowed).  Distances are the same. */
+    uint32_t sssp_pull;
 } gga_params;
 /* p = NULL returns to the per-graph defaults. */
 gga_status gga_set_params(gga_ctx *ctx, const gga_params *p);
@@ -242,8 +252,10 @@ gga_status gga_autotune(gga_ctx *ctx, gga_graph *g, uint32_t trials, gga_params 
  * and of its per-iteration convergence log (convergence.h:100-159). */
 typedef struct gga_round_trace {
     uint32_t kind;      /* 0 top-down (SSSP: near) round, 1 bottom-up BFS round, 2 SSSP far pass,
-                         * 3 SSSP heavy round (a bucket's heavy edges) */
-    uint32_t items;     /* vertices expanded (kind 0/1) or far-pile entries split (kind 2) */
+                         * 3 SSSP heavy round (a bucket's heavy edges), 4 SSSP pull scan (lists
+                         * the unsettled vertices' heavy edges), 5 SSSP pull round (relaxes them
+                         * from the settled side) */
+    uint32_t items;     /* vertices expanded (kind 0/1/3/5) or far-pile entries split (kind 2) */
     uint32_t edges;     /* edges owned by the expanded vertices */
     uint32_t far_items; /* SSSP: far-pile size when the round started */
     uint32_t ns;        /* round duration (block 0's clock from this round's start to the next's) */

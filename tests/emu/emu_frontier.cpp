@@ -1,10 +1,12 @@
 /* Runs k_frontier (BFS or SSSP, optional bottom-up rounds or light/heavy
  * classes) on NB emulated blocks and compares with the oracle's distances.
- * args: dir NB row sssp iters delta bu alpha beta lh */
+ * args: dir NB row sssp iters delta bu alpha beta lh [pull]
+ * (pull: bucket closes by pull, 0 never, 1 cost rule, 2 always; the test
+ * graphs have equal weights both ways) */
 #include "kernel_frontier.inc"
 template <int BS, bool SSSP>
 int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint32_t alpha, uint32_t beta,
-        uint32_t delta, bool lhm) {
+        uint32_t delta, bool lhm, uint32_t pull) {
     auto off = rd(d + "/off.bin"), col = rd(d + "/col.bin"), wt = rd(d + "/wt.bin"), srcs = rd(d + "/srcs.bin");
     auto want = rd(d + (SSSP ? "/want_sssp.bin" : "/want_bfs.bin"));
     uint32_t n = off.size() - 1, m = col.size(), src = srcs[row];
@@ -39,6 +41,8 @@ int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint
         a.ho0 = hq[3].data(); a.ho1 = hq[4].data(); a.ho2 = hq[5].data();
         a.hb0 = hq[6].data(); a.hb1 = hq[7].data(); a.hb2 = hq[8].data();
         a.huf0 = huf[0].data(); a.huf1 = huf[1].data(); a.huf2 = huf[2].data();
+        a.pull = pull;
+        for (uint32_t e = 0; e < m; ++e) a.heavy_edges += wt[e] >= delta;
     }
     run_grid(NB, BS, [&](int b) {
         switch (b) {
@@ -50,8 +54,8 @@ int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint
     });
     size_t bad = 0;
     for (uint32_t i = 0; i < n; ++i) bad += dist[i] != want[(size_t)row * n + i];
-    printf("frontier sssp=%d lh=%d row=%d iters=%u delta=%u bu=%u err=%u rounds=%u bad=%zu relaxed=%llu\n", (int)SSSP,
-           a.light != nullptr, row, iters, delta, bu, ctl.err, ctl.rounds, bad, ctl.edges_relaxed);
+    printf("frontier sssp=%d lh=%d pull=%u row=%d iters=%u delta=%u bu=%u err=%u rounds=%u bad=%zu relaxed=%llu\n",
+           (int)SSSP, a.light != nullptr, a.pull, row, iters, delta, bu, ctl.err, ctl.rounds, bad, ctl.edges_relaxed);
     return bad != 0 || ctl.err;
 }
 int main(int argc, char **argv) {
@@ -60,5 +64,7 @@ int main(int argc, char **argv) {
     int nb = atoi(argv[2]), row = atoi(argv[3]), sssp = atoi(argv[4]);
     uint32_t iters = atoi(argv[5]), delta = atoi(argv[6]), bu = atoi(argv[7]), al = atoi(argv[8]), be = atoi(argv[9]);
     bool lhm = atoi(argv[10]);
-    return sssp ? run<256, true>(nb, d, row, iters, 0, al, be, delta, lhm) : run<256, false>(nb, d, row, iters, bu, al, be, 0, false);
+    uint32_t pull = argc > 11 ? atoi(argv[11]) : 0;
+    return sssp ? run<256, true>(nb, d, row, iters, 0, al, be, delta, lhm, pull)
+                : run<256, false>(nb, d, row, iters, bu, al, be, 0, false, 0);
 }

@@ -327,3 +327,68 @@ def test_sssp_light_heavy_relaxes_fewer_edges(ctx):
         ctx.reset_params()
     np.testing.assert_array_equal(res[0][0], res[1][0])
     assert res[0][1]["edges_relaxed"] < res[1][1]["edges_relaxed"]
+
+
+@pytest.mark.parametrize("delta", [1, 7, 33, 100])
+def test_sssp_pull_bucket_close_matches_oracle(ctx, delta):
+    """Closing a bucket by pull (each unsettled vertex takes the smallest
+    d(u) + w over its heavy edges to settled vertices) gives the same
+    distances as pushing the bucket's heavy edges: with the cost rule (0),
+    never (1) and at every bucket (2)."""
+    for g in (gga.Graph.rmat(15, 16, seed=41), gga.Graph.grid(96, 80, seed=6)):
+        assert g.info()["wsymmetric"] == 1
+        for s in (int(np.argmax(g.degrees())), 11):
+            want = _oracle_dist(g, "sssp", s)
+            try:
+                for pull in (0, 1, 2):
+                    ctx.set_params(sssp_delta=delta, sssp_pull=pull)
+                    np.testing.assert_array_equal(ctx.sssp(g, s), want, err_msg=f"delta={delta} pull={pull} src={s}")
+            finally:
+                ctx.reset_params()
+
+
+def test_sssp_pull_relaxes_fewer_edges(ctx):
+    """On R-MAT the first bucket holds the hubs: its heavy edges far
+    outnumber the unsettled vertices', so the cost rule pulls there."""
+    g = gga.Graph.rmat(16, 16, seed=8)
+    s = int(np.argmax(g.degrees()))
+    res, kinds = {}, {}
+    try:
+        ctx.trace(True)
+        for pull in (0, 1):
+            ctx.set_params(sssp_delta=32, sssp_pull=pull)
+            res[pull] = ctx.sssp(g, s, stats=True)
+            kinds[pull] = {r["kind"] for r in ctx.last_trace()["rounds"]}
+    finally:
+        ctx.trace(False)
+        ctx.reset_params()
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    assert res[0][1]["edges_relaxed"] < res[1][1]["edges_relaxed"]
+    assert {"pull_scan", "pull"} <= kinds[0]
+    assert "pull" not in kinds[1] and "heavy" in kinds[1]
+
+
+def test_sssp_pull_needs_equal_reverse_weights(ctx):
+    """A graph whose every edge has its reverse, but with another weight,
+    must not pull (the pull reads w(v, u) for w(u, v)): the device check
+    marks it and the bucket closes push, so the distances stay right even
+    with sssp_pull = 2."""
+    off, col, wt = gga.Graph.rmat(13, 8, seed=17).csr()
+    u = np.repeat(np.arange(len(off) - 1, dtype=np.uint32), np.diff(off.astype(np.int64)))
+    wt2 = (wt + (u < col)).astype(np.uint32)
+    g = gga.Graph.from_csr(off, col, wt2)
+    assert g.info()["wsymmetric"] == 0
+    s = int(np.argmax(g.degrees()))
+    try:
+        ctx.set_params(sssp_delta=16, sssp_pull=2)
+        ctx.trace(True)
+        np.testing.assert_array_equal(ctx.sssp(g, s), _oracle_dist(g, "sssp", s))
+        kinds = {r["kind"] for r in ctx.last_trace()["rounds"]}
+    finally:
+        ctx.trace(False)
+        ctx.reset_params()
+    info = g.info()
+    assert info["symmetric"] == 1 and info["wsymmetric"] == -1
+    assert "pull" not in kinds
+    with pytest.raises(gga.GGAError):
+        ctx.set_params(sssp_pull=3)

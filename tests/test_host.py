@@ -154,6 +154,9 @@ def test_rmat_generator_properties():
     pos = np.searchsorted(key[order], rev)
     assert np.array_equal(key[order][pos], rev), "symmetric"
     assert np.array_equal(wt[order][pos], wt), "same weight both ways"
+    info = g.info()
+    assert info["symmetric"] == 1 and info["wsymmetric"] == 1, "known symmetric with equal weights"
+    assert gga.Graph.from_csr(off, col, wt).info()["wsymmetric"] == 0, "user arrays: checked on the device"
     assert wt.min() >= 1 and wt.max() <= 255
     deg = np.diff(off.astype(np.int64))
     assert deg.max() > 20 * deg.mean(), "skewed degrees"
