@@ -420,14 +420,14 @@ __device__ __forceinline__ void pull_scan(const Args &a, uint32_t thr, uint32_t 
  * Block-uniform: every thread runs the same units and checkpoints.
  *
  * PULL (SSSP): the entries are unsettled vertices and their heavy edges;
- * an edge whose other end u is settled (d(u) < thr) offers d(u) + w to the
- * entry's vertex, and every improvement goes to the far pile. */
+ * an edge whose other end u is settled (d(u) < settled) offers d(u) + w to
+ * the entry's vertex. */
 template <int BS, bool SSSP, bool PULL = false>
 __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage &S, uint32_t *t_o, uint32_t *t_b,
                                              uint32_t *t_du, const uint32_t *qv, const uint32_t *qo,
                                              const uint32_t *qb, const uint32_t *uf, uint32_t nitems, uint32_t total,
-                                             uint32_t units, uint32_t round, uint32_t thr, uint32_t nxt,
-                                             uint32_t r3n, uint32_t fp, uint32_t bucket,
+                                             uint32_t units, uint32_t round, uint32_t thr, uint32_t settled,
+                                             uint32_t nxt, uint32_t r3n, uint32_t fp, uint32_t bucket,
                                              unsigned long long &relaxed) {
     const uint32_t tid = threadIdx.x, U = a.unit, G = gridDim.x;
     FrontierCtl *ctl = a.ctl;
@@ -450,12 +450,36 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
         uint32_t ni0 = 0, ncnt = 0;
         if (kn < units) bounds(kn, ni0, ncnt); /* used after this unit */
         const uint32_t ebase = k * U, eend = min(ebase + U, total);
-        for (uint32_t j = tid; j < cnt; j += BS) {
-            const uint32_t i = i0 + j;
-            t_o[j] = __ldcg(qo + i);
-            t_b[j] = __ldcg(qb + i);
-            /* the entry's distance, or in a pull its vertex */
-            if (SSSP) t_du[j] = PULL ? __ldcg(qv + i) : __ldcg(a.dist + __ldcg(qv + i));
+        /* the unit's entries, TB per thread in flight: all entry loads, then
+         * (SSSP) all distance loads, then the stores, so a table of up to
+         * TB x BS entries costs two dependent L2 round trips, not 2 x TB */
+        constexpr uint32_t TB = 5;
+        for (uint32_t j0 = 0; j0 < cnt; j0 += TB * BS) {
+            uint32_t o[TB], b[TB], x[TB];
+#pragma unroll
+            for (uint32_t q = 0; q < TB; ++q) {
+                const uint32_t j = j0 + q * BS + tid;
+                o[q] = b[q] = x[q] = 0;
+                if (j < cnt) {
+                    o[q] = __ldcg(qo + i0 + j);
+                    b[q] = __ldcg(qb + i0 + j);
+                    if (SSSP) x[q] = __ldcg(qv + i0 + j);
+                }
+            }
+            if (SSSP && !PULL) { /* the entry's distance (a pull keeps the vertex) */
+#pragma unroll
+                for (uint32_t q = 0; q < TB; ++q)
+                    if (j0 + q * BS + tid < cnt) x[q] = __ldcg(a.dist + x[q]);
+            }
+#pragma unroll
+            for (uint32_t q = 0; q < TB; ++q) {
+                const uint32_t j = j0 + q * BS + tid;
+                if (j < cnt) {
+                    t_o[j] = o[q];
+                    t_b[j] = b[q];
+                    if (SSSP) t_du[j] = x[q];
+                }
+            }
         }
         __syncthreads();
         constexpr uint32_t PB = STAGE_BATCH;
@@ -497,7 +521,7 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
             if (PULL) { /* the offer d(u) + w to the entry's vertex, from settled u only */
 #pragma unroll
                 for (uint32_t q = 0; q < PB; ++q) {
-                    act[q] = act[q] && probe[q] < thr;
+                    act[q] = act[q] && probe[q] < settled;
                     alt[q] += probe[q];
                     v[q] = tgt[q];
                     probe[q] = NONE;
@@ -537,7 +561,7 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                 if (!SSSP) {
                     a.dist[vq] = aq;
                     nearm |= 1u << q;
-                } else if (!PULL && aq < thr) {
+                } else if (aq < thr) {
                     if (atomicExch(a.stamp + vq, round + 1) != round + 1) nearm |= 1u << q;
                 } else {
                     fmin = min(fmin, aq);
@@ -572,6 +596,38 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
         k = kn;
         i0 = ni0;
         cnt = ncnt;
+    }
+    /* every thread has read the final stage counts before any thread stages
+     * again (a caller may stage right after, as a far pass does) */
+    __syncthreads();
+}
+
+/* Far pass (SSSP): split pile fp with the new threshold thr — entries still
+ * at or above it move to pile fq, entries that fell into the new bucket
+ * [thr_old, thr) join the next round's near queue (once, by round stamp),
+ * and entries below thr_old (settled since they were piled) are dropped.
+ * Block-uniform; the caller publishes the last stage. */
+template <int BS>
+__device__ __forceinline__ void split_pile(const Args &a, Ctrl &C, const Stage &S, uint32_t fp, uint32_t fq,
+                                           uint32_t fc, uint32_t thr, uint32_t thr_old, uint32_t round,
+                                           uint32_t nxt, uint32_t r3n, uint32_t bucket) {
+    const uint32_t tid = threadIdx.x;
+    const uint64_t gthreads = (uint64_t)gridDim.x * BS;
+    const uint32_t *fin = sel3(fp, a.far0, a.far1, a.far2);
+    for (uint64_t base = (uint64_t)blockIdx.x * BS; base < fc; base += gthreads) {
+        const uint64_t i = base + tid;
+        if (i < fc) {
+            const uint32_t v = __ldcg(fin + i);
+            const uint32_t d = __ldcg(a.dist + v);
+            if (d >= thr) {
+                atomicMin(&C.fmin, d);
+                stage_far(a, C, S.sf, v);
+            } else {
+                atomicAnd(a.farbits + (v >> 5), ~(1u << (v & 31)));
+                if (d >= thr_old && atomicExch(a.stamp + v, round + 1) != round + 1) stage_near(a, C, S.sv, v);
+            }
+        }
+        checkpoint<BS, true>(a, C, S, nxt, r3n, fq, bucket, BS);
     }
 }
 
@@ -700,12 +756,40 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
         if (blockIdx.x == 0 && tid == 0) {
             ctl->qctr[(round + 2) % 3] = 0;
         }
+        /* Next bucket (SSSP): the threshold rises by delta (to `lowest` +
+         * delta), a new pile takes the far entries, and the lists and piles
+         * that rotate out are cleared.  Block 0 clears the pile after fq (read
+         * by the previous far pass, a barrier ago; written by the next, a
+         * barrier ahead) and the heavy list after the new bucket's (expanded
+         * two buckets ago). */
+        auto open_bucket = [&](uint32_t lowest) -> uint32_t {
+            thr = lowest > NONE - a.delta ? NONE : lowest + a.delta;
+            ++bucket;
+            heavy_done = false;
+            const uint32_t fq = fp == 2 ? 0 : fp + 1;
+            if (blockIdx.x == 0 && tid == 0) {
+                const uint32_t dead = fq == 2 ? 0 : fq + 1;
+                ctl->far_count[dead] = 0;
+                ctl->far_min[dead] = NONE;
+                ctl->far_phases++;
+                ctl->hctr[(bucket + 1) % 3] = 0;
+            }
+            return fq;
+        };
+        /* end of a round that wrote far pushes and pile entries to pile fq */
+        auto publish_far = [&](uint32_t fq) {
+            checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fq, bucket, 1);
+            if (SSSP && tid == 0 && C.fmin != NONE) {
+                atomicMin(&ctl->far_min[fq], C.fmin);
+                C.fmin = NONE;
+            }
+        };
         if (units == 0) {
             pulling = false;
             if (lh && !heavy_done && hunits > 0) {
                 /* ---- bucket closes: its vertices' distances are final, so
                  * their heavy edges (w >= delta, results >= thr) are relaxed
-                 * once, all into the far pile */
+                 * once */
                 heavy_done = true;
                 hsettled += htot;
                 /* by pull when the unsettled vertices' heavy edges (plus a
@@ -722,63 +806,31 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
                     if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
                     continue;
                 }
+                /* pushed, in the same round as the far pass that opens the
+                 * next bucket: results below the new threshold join its
+                 * near queue, the rest the new pile */
                 trace_round(a, round, 3, hn, htot, fc);
-                expand_units<BS, SSSP>(a, C, S, t_o, t_b, t_du, sel3(hl, a.hv0, a.hv1, a.hv2),
-                                       sel3(hl, a.ho0, a.ho1, a.ho2), sel3(hl, a.hb0, a.hb1, a.hb2),
-                                       sel3(hl, a.huf0, a.huf1, a.huf2), hn, htot, hunits, round, 0u, nxt, r3n, fp, bucket, relaxed);
-                checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, 1);
-                if (tid == 0 && C.fmin != NONE) {
-                    atomicMin(&ctl->far_min[fp], C.fmin);
-                    C.fmin = NONE;
-                }
+                const uint32_t thr_old = thr, hl_old = hl;
+                const uint32_t fq = open_bucket(thr);
+                expand_units<BS, SSSP>(a, C, S, t_o, t_b, t_du, sel3(hl_old, a.hv0, a.hv1, a.hv2),
+                                       sel3(hl_old, a.ho0, a.ho1, a.ho2), sel3(hl_old, a.hb0, a.hb1, a.hb2),
+                                       sel3(hl_old, a.huf0, a.huf1, a.huf2), hn, htot, hunits, round, thr, 0u, nxt,
+                                       r3n, fq, bucket, relaxed);
+                split_pile<BS>(a, C, S, fp, fq, fc, thr, thr_old, round, nxt, r3n, bucket);
+                publish_far(fq);
                 if (a.trace && tid == 0) busy += clock64() - t_round;
                 if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+                fp = fq;
                 continue;
             }
             if (!SSSP || fc == 0) break;
-            /* ---- near queue drained: raise the threshold and split the far
-             * pile into the next round's near queue and the next pile */
+            /* ---- near queue drained and nothing left to close: open the
+             * next bucket at the lowest piled distance and split the pile */
             const uint32_t thr_old = thr;
-            const uint32_t lowest = max(thr, fm);
-            thr = lowest > NONE - a.delta ? NONE : lowest + a.delta;
-            ++bucket;
-            heavy_done = false;
-            const uint32_t fq = fp == 2 ? 0 : fp + 1; /* pile that keeps the far items */
-            if (blockIdx.x == 0 && tid == 0) {
-                /* three piles rotate: the one after fq was read by the
-                 * previous far pass (a barrier ago) and is written by the
-                 * next one (a barrier ahead), so it can be cleared now */
-                const uint32_t dead = fq == 2 ? 0 : fq + 1;
-                ctl->far_count[dead] = 0;
-                ctl->far_min[dead] = NONE;
-                ctl->far_phases++;
-                /* heavy lists rotate by bucket the same way: the one after
-                 * the new bucket's was expanded two buckets ago */
-                ctl->hctr[(bucket + 1) % 3] = 0;
-            }
+            const uint32_t fq = open_bucket(max(thr, fm));
             trace_round(a, round, 2, fc, 0, fc);
-            const uint32_t *fin = sel3(fp, a.far0, a.far1, a.far2);
-            for (uint64_t base = (uint64_t)blockIdx.x * BS; base < fc; base += gthreads) {
-                const uint64_t i = base + tid;
-                if (i < fc) {
-                    const uint32_t v = __ldcg(fin + i);
-                    const uint32_t d = __ldcg(a.dist + v);
-                    if (d >= thr) {
-                        atomicMin(&C.fmin, d);
-                        stage_far(a, C, S.sf, v);
-                    } else {
-                        atomicAnd(a.farbits + (v >> 5), ~(1u << (v & 31)));
-                        if (d >= thr_old && atomicExch(a.stamp + v, round + 1) != round + 1)
-                            stage_near(a, C, S.sv, v);
-                    }
-                }
-                checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fq, bucket, BS);
-            }
-            checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fq, bucket, 1);
-            if (tid == 0 && C.fmin != NONE) {
-                atomicMin(&ctl->far_min[fq], C.fmin);
-                C.fmin = NONE;
-            }
+            split_pile<BS>(a, C, S, fp, fq, fc, thr, thr_old, round, nxt, r3n, bucket);
+            publish_far(fq);
             if (a.trace && tid == 0) busy += clock64() - t_round;
             if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
             fp = fq;
@@ -798,29 +850,29 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
             }
         }
         if (SSSP && pulling) {
-            /* ---- second half of a pulling bucket close */
+            /* ---- second half of a pulling bucket close, in the same round
+             * as the far pass that opens the next bucket: offers from
+             * vertices settled below the old threshold, results below the
+             * new one to its near queue, the rest to the new pile */
             pulling = false;
             trace_round(a, round, 5, nitems, total, fc);
+            const uint32_t thr_old = thr;
+            const uint32_t fq = open_bucket(thr);
             expand_units<BS, SSSP, true>(a, C, S, t_o, t_b, t_du, sel(cur, a.qv0, a.qv1), sel(cur, a.qo0, a.qo1),
                                          sel(cur, a.qb0, a.qb1), sel(cur, a.uf0, a.uf1), nitems, total, units, round,
-                                         thr, nxt, r3n, fp, bucket, relaxed);
-            checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, 1);
-            if (tid == 0 && C.fmin != NONE) {
-                atomicMin(&ctl->far_min[fp], C.fmin);
-                C.fmin = NONE;
-            }
+                                         thr, thr_old, nxt, r3n, fq, bucket, relaxed);
+            split_pile<BS>(a, C, S, fp, fq, fc, thr, thr_old, round, nxt, r3n, bucket);
+            publish_far(fq);
             if (a.trace && tid == 0) busy += clock64() - t_round;
             if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+            fp = fq;
             continue;
         }
         trace_round(a, round, 0, nitems, total, fc);
         expand_units<BS, SSSP>(a, C, S, t_o, t_b, t_du, sel(cur, a.qv0, a.qv1), sel(cur, a.qo0, a.qo1),
-                               sel(cur, a.qb0, a.qb1), sel(cur, a.uf0, a.uf1), nitems, total, units, round, thr, nxt, r3n, fp, bucket, relaxed);
-        checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, 1);
-        if (SSSP && tid == 0 && C.fmin != NONE) {
-            atomicMin(&ctl->far_min[fp], C.fmin);
-            C.fmin = NONE;
-        }
+                               sel(cur, a.qb0, a.qb1), sel(cur, a.uf0, a.uf1), nitems, total, units, round, thr, 0u,
+                               nxt, r3n, fp, bucket, relaxed);
+        publish_far(fp);
         if (a.trace && tid == 0) busy += clock64() - t_round;
         if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
     }

@@ -3,7 +3,8 @@
  * kernels' own source text can run on the host against the oracle.
  *
  * Every CUDA thread is a std::thread; __syncthreads is a per-block
- * std::barrier; warp collectives (ballot, shuffles) exchange values through a
+ * std::barrier that also checks every thread arrived from the same call
+ * site; warp collectives (ballot, shuffles) exchange values through a
  * per-warp barrier, so a collective reached by only part of a warp hangs the
  * emulation instead of passing silently.  Shared-memory statics become
  * per-block instances through a BLK template parameter that
@@ -42,7 +43,25 @@ int g_line[8][1024];
 static std::barrier<> *g_block_bars[8];
 struct WarpCtx { std::barrier<> *bar; uint64_t slot[32]; };
 static WarpCtx *g_warps[8];
-inline void sync_threads_impl(int l) { MARKL(l); g_block_bars[blockIdx.x]->arrive_and_wait(); MARKL(-l); }
+/* Every thread of a block must meet each __syncthreads at the same call
+ * site; a thread that reaches another one (a barrier skipped or taken twice
+ * on one path) stops the emulation with both source lines.  Slots alternate
+ * by barrier phase, so thread 0 cannot overwrite the slot being checked. */
+static int g_arrive_line[8][2][1024];
+thread_local unsigned g_sync_phase;
+inline void sync_threads_impl(int l) {
+    MARKL(l);
+    const unsigned p = g_sync_phase++ & 1u;
+    g_arrive_line[blockIdx.x][p][threadIdx.x] = l;
+    g_block_bars[blockIdx.x]->arrive_and_wait();
+    const int l0 = g_arrive_line[blockIdx.x][p][0];
+    if (l0 != l) {
+        printf("BARRIER MISMATCH block %u thread %u at line %d, thread 0 at line %d\n", blockIdx.x, threadIdx.x, l, l0);
+        fflush(stdout);
+        _exit(4);
+    }
+    MARKL(-l);
+}
 #define __syncthreads() sync_threads_impl(__LINE__)
 inline WarpCtx &wc() { return g_warps[blockIdx.x][threadIdx.x / 32]; }
 template <class T> inline T xchg_all(T v, std::function<T(WarpCtx &, unsigned)> f) {

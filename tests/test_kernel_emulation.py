@@ -3,8 +3,10 @@
 tests/emu/gen_kernels.py turns a kernel file (frontier.cu, sssp32.cu,
 msbfs.cu, batch.cu) into host C++ and tests/emu/prelude.h emulates the CUDA
 constructs it uses: one host thread per CUDA thread, real barriers for
-__syncthreads and for warp collectives (so a collective reached by part of a
-warp hangs here instead of passing), host atomics, and grid barriers between
+__syncthreads (which also check that every thread of the block arrived from
+the same call site) and for warp collectives (so a collective reached by
+part of a warp hangs here instead of passing), host atomics, and grid
+barriers between
 2-4 emulated blocks that interleave freely.  Each case checks bit-exact
 distances against the oracle (the reference's serial BFS/SSSP,
 graph.h:115-184) and that the kernel's error word stays clear.  This is how
