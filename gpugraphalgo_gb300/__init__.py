@@ -60,6 +60,32 @@ def _ptr(a: np.ndarray):
     return C.c_void_p(a.ctypes.data)
 
 
+class _HostBlock:
+    """Page-locked host memory from gga_host_alloc, freed with its last array."""
+
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        _check(N.load().gga_host_alloc(nbytes, C.byref(p)), "host_alloc")
+        self.ptr = p.value
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            N.load().gga_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.uint32) -> np.ndarray:
+    """An uninitialised numpy array in page-locked host memory, so copies to
+    and from the GPU run asynchronously at full bandwidth."""
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape))
+    nbytes = max(1, count * dt.itemsize)
+    blk = _HostBlock(nbytes)
+    raw = (C.c_char * nbytes).from_address(blk.ptr)
+    raw._gga_block = blk  # the array's base keeps the block alive
+    return np.frombuffer(raw, dt, count).reshape(shape)
+
+
 def _algo(a) -> int:
     return ALGOS[a] if isinstance(a, str) else int(a)
 
@@ -334,6 +360,21 @@ class Context:
             f"solve({algo}, src={src}, {variant})",
         )
         return (out, s.as_dict()) if stats else out
+
+    def solve_many(self, graph: Graph, algo, srcs: Sequence[int], out=None, stats: bool = False):
+        """One frontier-engine traversal per source, back to back, each
+        result copied out while the next runs (gga_solve_many).  out: an
+        (len(srcs), n) uint32 array — page-locked (pinned_empty) for the
+        copies to overlap — or any object with a ``data_ptr()``; row i is
+        srcs[i]'s distances.  stats: one dict per source."""
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        if out is None:
+            out = np.empty((len(s), graph.n), np.uint32)
+        ptr = C.c_void_p(out.data_ptr()) if hasattr(out, "data_ptr") else _ptr(out)
+        st = (N.Stats * max(1, len(s)))()
+        _check(N.load().gga_solve_many(self._h, graph.handle, _algo(algo), len(s), _ptr(s), ptr, st),
+               f"solve_many({algo}, {len(s)} sources)")
+        return (out, [st[i].as_dict() for i in range(len(s))]) if stats else out
 
     def bfs(self, graph: Graph, src: int, variant="auto", **kw):
         return self.solve(graph, BFS, src, variant, **kw)

@@ -151,6 +151,9 @@ SIGNATURES = {
     "gga_bfs": (C.c_int, [P, P, u32, C.c_int, P, C.POINTER(Stats)]),
     "gga_sssp": (C.c_int, [P, P, u32, C.c_int, P, C.POINTER(Stats)]),
     "gga_solve": (C.c_int, [P, P, C.c_int, u32, C.c_int, P, C.POINTER(Stats)]),
+    "gga_solve_many": (C.c_int, [P, P, C.c_int, u32, P, P, C.POINTER(Stats)]),
+    "gga_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
+    "gga_host_free": (None, [P]),
     "gga_set_params": (C.c_int, [P, C.POINTER(Params)]),
     "gga_get_params": (C.c_int, [P, C.POINTER(Params)]),
     "gga_autotune": (C.c_int, [P, P, u32, C.POINTER(Params)]),

@@ -60,6 +60,18 @@ void gga_ctx_destroy(gga_ctx *c) {
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
     ctx_batch_release(c);
+    ManyScratch &m = c->many;
+    if (m.copy) cudaStreamSynchronize(m.copy);
+    for (int i = 0; i < ManyScratch::RING; ++i) {
+        cudaFree(m.buf[i]);
+        if (m.ready[i]) cudaEventDestroy(m.ready[i]);
+        if (m.copied[i]) cudaEventDestroy(m.copied[i]);
+    }
+    for (cudaEvent_t e : m.ev) cudaEventDestroy(e);
+    cudaFreeHost(m.hctl);
+    cudaFree(m.acc);
+    cudaFreeHost(m.hacc);
+    if (m.copy) cudaStreamDestroy(m.copy);
     frontier_scratch_free(&c->fs);
     cudaFree(c->dflag);
     cudaFreeHost(c->hflag);
@@ -305,6 +317,39 @@ gga_status ctx_validate_solve(const gga_graph *g, gga_algo algo, uint32_t src) {
     return GGA_OK;
 }
 
+/* What the frontier engine walks for one solve: the split or unsplit view,
+ * SSSP's light-first rows, and whether bucket closes may pull.  Runs the
+ * once-per-graph device checks and builds the light/heavy order on first
+ * use; sizes the scratch. */
+struct FrontierPlan {
+    GraphView v;
+    LightHeavy lh;
+    bool use_split = false;
+};
+
+static gga_status frontier_plan(gga_ctx *c, gga_graph *g, const gga_params &p, bool sssp, FrontierPlan *out) {
+    const DevGraph *d = dev_graph_of(g);
+    gga_status s;
+    out->use_split = d->level != 0 && p.use_split;
+    if (!sssp && !out->use_split && p.bfs_direction == 0 && d->symmetric == 0 &&
+        (s = dev_graph_check_symmetric(g, c->dflag + 40, c->hflag + 40, c->st)))
+        return s;
+    out->v = dev_graph_view(d, out->use_split);
+    if (sssp && !out->use_split && p.sssp_delta && p.sssp_light_heavy == 0) {
+        if ((s = dev_graph_light_heavy(g, p.sssp_delta, c->st))) return s;
+        /* pulling bucket closes need every edge's reverse with its weight */
+        if (p.sssp_pull != 1 && (d->symmetric == 0 || d->wsymmetric == 0) &&
+            (s = dev_graph_check_symmetric(g, c->dflag + 40, c->hflag + 40, c->st)))
+            return s;
+        out->v.col = d->lcol;
+        out->v.wt = d->lwt;
+        out->lh.light = d->light;
+        out->lh.heavy_edges = d->lh_heavy;
+        out->lh.pull = p.sssp_pull == 1 || d->wsymmetric <= 0 ? 0u : (p.sssp_pull == 2 ? 2u : 1u);
+    }
+    return frontier_scratch_ensure(&c->fs, out->v.n > d->n ? out->v.n : d->n, d->m);
+}
+
 gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_variant variant,
                      uint32_t *dist_out, gga_stats *stats) {
     const double t0 = gga_now_ms();
@@ -324,28 +369,12 @@ gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_
     memset(&st, 0, sizeof st);
 
     if (variant == GGA_VARIANT_AUTO || variant == GGA_VARIANT_FRONTIER) {
-        const bool use_split = split && p.use_split;
-        if (!sssp && !use_split && p.bfs_direction == 0 && d->symmetric == 0 &&
-            (s = dev_graph_check_symmetric(g, c->dflag + 40, c->hflag + 40, c->st)))
-            return s;
-        GraphView v = dev_graph_view(d, use_split);
-        LightHeavy lh;
-        if (sssp && !use_split && p.sssp_delta && p.sssp_light_heavy == 0) {
-            if ((s = dev_graph_light_heavy(g, p.sssp_delta, c->st))) return s;
-            /* pulling bucket closes need every edge's reverse with its weight */
-            if (p.sssp_pull != 1 && (d->symmetric == 0 || d->wsymmetric == 0) &&
-                (s = dev_graph_check_symmetric(g, c->dflag + 40, c->hflag + 40, c->st)))
-                return s;
-            v.col = d->lcol;
-            v.wt = d->lwt;
-            lh.light = d->light;
-            lh.heavy_edges = d->lh_heavy;
-            lh.pull = p.sssp_pull == 1 || d->wsymmetric <= 0 ? 0u : (p.sssp_pull == 2 ? 2u : 1u);
-        }
-        if ((s = frontier_scratch_ensure(&c->fs, v.n > d->n ? v.n : d->n, d->m))) return s;
+        FrontierPlan fp;
+        if ((s = frontier_plan(c, g, p, sssp, &fp))) return s;
+        const bool use_split = fp.use_split;
         FrontierResult r;
-        s = frontier_run(&c->fs, v, use_split ? d->first : nullptr, src, sssp, p, c->sms, c->st, c->ev[0], c->ev[1], &r,
-                         c->trace_on, lh);
+        s = frontier_run(&c->fs, fp.v, use_split ? d->first : nullptr, src, sssp, p, c->sms, c->st, c->ev[0], c->ev[1],
+                         &r, c->trace_on, fp.lh);
         if (s) return s;
         if (c->trace_on) {
             const uint32_t nr = r.rounds < TRACE_ROUNDS ? r.rounds : TRACE_ROUNDS;
@@ -423,6 +452,129 @@ gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_
     st.total_ms = gga_now_ms() - t0;
     if (stats) *stats = st;
     return GGA_OK;
+}
+
+/* Buffers of gga_solve_many for n sources of `words`-vertex results. */
+static gga_status many_reserve(gga_ctx *c, size_t words, uint32_t n) {
+    ManyScratch &m = c->many;
+    if (!m.copy) {
+        GGA_CK(cudaStreamCreateWithFlags(&m.copy, cudaStreamNonBlocking));
+        for (int i = 0; i < ManyScratch::RING; ++i) {
+            GGA_CK(cudaEventCreateWithFlags(&m.ready[i], cudaEventDisableTiming));
+            GGA_CK(cudaEventCreateWithFlags(&m.copied[i], cudaEventDisableTiming));
+        }
+    }
+    if (m.buf_words < words) {
+        for (int i = 0; i < ManyScratch::RING; ++i) {
+            cudaFree(m.buf[i]);
+            m.buf[i] = nullptr;
+        }
+        m.buf_words = 0;
+        for (int i = 0; i < ManyScratch::RING; ++i) GGA_CK(cudaMalloc((void **)&m.buf[i], words * sizeof(uint32_t)));
+        m.buf_words = words;
+    }
+    if (m.cap < n) {
+        cudaFreeHost(m.hctl);
+        cudaFree(m.acc);
+        cudaFreeHost(m.hacc);
+        m.hctl = nullptr;
+        m.acc = m.hacc = nullptr;
+        m.cap = 0;
+        GGA_CK(cudaMallocHost((void **)&m.hctl, (size_t)n * sizeof(FrontierCtl)));
+        GGA_CK(cudaMalloc((void **)&m.acc, (size_t)n * 2 * sizeof(unsigned long long)));
+        GGA_CK(cudaMallocHost((void **)&m.hacc, (size_t)n * 2 * sizeof(unsigned long long)));
+        m.cap = n;
+    }
+    while (m.ev.size() < 2 * (size_t)n) {
+        cudaEvent_t e;
+        GGA_CK(cudaEventCreate(&e));
+        m.ev.push_back(e);
+    }
+    return GGA_OK;
+}
+
+gga_status gga_solve_many(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t n, const uint32_t *srcs,
+                          uint32_t *dist_out, gga_stats *stats) {
+    const double t0 = gga_now_ms();
+    if (!c || !g || (n && (!srcs || !dist_out))) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    gga_status s;
+    for (uint32_t i = 0; i < n; ++i)
+        if ((s = ctx_validate_solve(g, algo, srcs[i]))) return s;
+    if (n == 0) return GGA_OK;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if ((s = ctx_activate(c))) return s;
+    if ((s = dev_graph_ensure(g, c->device, c->st))) return s;
+    const DevGraph *d = dev_graph_of(g);
+    const gga_params p = effective_params(c, g);
+    const bool sssp = algo == GGA_SSSP;
+    FrontierPlan fp;
+    if ((s = frontier_plan(c, g, p, sssp, &fp))) return s;
+    if ((s = many_reserve(c, d->n ? d->n : 1, n))) return s;
+    ManyScratch &m = c->many;
+    const bool reached = stats && !p.skip_reached;
+    const size_t bytes = (size_t)d->n * sizeof(uint32_t);
+    if (reached) GGA_CK(cudaMemsetAsync(m.acc, 0, (size_t)n * 2 * sizeof(unsigned long long), c->st));
+    std::vector<FrontierResult> r(n);
+    for (uint32_t i = 0; i < n && s == GGA_OK; ++i) {
+        const int slot = (int)(i % ManyScratch::RING);
+        /* the slot's previous result has reached the host */
+        if (i >= (uint32_t)ManyScratch::RING && (s = gga_cuda_check(cudaStreamWaitEvent(c->st, m.copied[slot], 0))))
+            break;
+        s = frontier_run(&c->fs, fp.v, fp.use_split ? d->first : nullptr, srcs[i], sssp, p, c->sms, c->st,
+                         m.ev[2 * i], m.ev[2 * i + 1], &r[i], false, fp.lh, &m.hctl[i]);
+        if (s) break;
+        uint32_t *res = m.buf[slot];
+        if (fp.use_split) k_gather_parents<<<ctx_grid(c, d->n, 256), 256, 0, c->st>>>(c->fs.dist, d->first, d->n, res);
+        else if (bytes) s = gga_cuda_check(cudaMemcpyAsync(res, c->fs.dist, bytes, cudaMemcpyDeviceToDevice, c->st));
+        if (reached && s == GGA_OK) k_reached<<<ctx_grid(c, d->n, 256), 256, 0, c->st>>>(res, d->off, d->n, m.acc + 2 * i);
+        if (s == GGA_OK) s = gga_cuda_check(cudaGetLastError());
+        if (s == GGA_OK) s = gga_cuda_check(cudaEventRecord(m.ready[slot], c->st));
+        if (s == GGA_OK) s = gga_cuda_check(cudaStreamWaitEvent(m.copy, m.ready[slot], 0));
+        if (s == GGA_OK && bytes)
+            s = gga_cuda_check(cudaMemcpyAsync(dist_out + (size_t)i * d->n, res, bytes, cudaMemcpyDefault, m.copy));
+        if (s == GGA_OK) s = gga_cuda_check(cudaEventRecord(m.copied[slot], m.copy));
+    }
+    if (s == GGA_OK && reached)
+        s = gga_cuda_check(cudaMemcpyAsync(m.hacc, m.acc, (size_t)n * 2 * sizeof(unsigned long long),
+                                           cudaMemcpyDeviceToHost, c->st));
+    /* drain both streams even after an error, so no copy outlives the call */
+    gga_status w = dev_wait(c->st, 60.0 + n);
+    gga_status w2 = dev_wait(m.copy, 60.0);
+    if (s) return s;
+    if (w) return w;
+    if (w2) return w2;
+    for (uint32_t i = 0; i < n; ++i)
+        if ((s = frontier_verdict(m.hctl[i]))) return s;
+    if (stats) {
+        const double each = (gga_now_ms() - t0) / n;
+        for (uint32_t i = 0; i < n; ++i) {
+            gga_stats &st = stats[i];
+            memset(&st, 0, sizeof st);
+            st.iterations = m.hctl[i].rounds;
+            st.kernel_launches = r[i].launches + (fp.use_split ? 1 : 0) + (reached ? 1 : 0);
+            st.edges_relaxed = m.hctl[i].edges_relaxed;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, m.ev[2 * i], m.ev[2 * i + 1]);
+            st.kernel_ms = ms;
+            if (reached) {
+                st.vertices_reached = m.hacc[2 * i];
+                st.edges_reached = m.hacc[2 * i + 1];
+            }
+            st.total_ms = each;
+        }
+    }
+    return GGA_OK;
+}
+
+gga_status gga_host_alloc(size_t bytes, void **out) {
+    if (!out) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    GGA_CK(cudaMallocHost(out, bytes ? bytes : 1));
+    return GGA_OK;
+}
+
+void gga_host_free(void *p) {
+    if (p) cudaFreeHost(p);
 }
 
 gga_status gga_bfs(gga_ctx *c, gga_graph *g, uint32_t src, gga_variant variant, uint32_t *dist_out, gga_stats *stats) {

@@ -9,6 +9,22 @@
 
 struct BatchScratch;
 
+/* Working state of gga_solve_many (created on first use): a ring of result
+ * buffers, so a finished traversal's distances are copied to the host on a
+ * second stream while the next traversal runs. */
+struct ManyScratch {
+    static constexpr int RING = 3;
+    cudaStream_t copy = nullptr;
+    uint32_t *buf[RING] = {};
+    size_t buf_words = 0;
+    cudaEvent_t ready[RING] = {}, copied[RING] = {};
+    std::vector<cudaEvent_t> ev;      /* two per source: kernel start and end */
+    FrontierCtl *hctl = nullptr;      /* pinned: each launch's control block */
+    unsigned long long *acc = nullptr; /* device: reached vertices and edges, two per source */
+    unsigned long long *hacc = nullptr; /* pinned mirror */
+    uint32_t cap = 0;                 /* sources hctl / acc hold */
+};
+
 struct gga_ctx {
     int device = 0;
     int sms = 0;
@@ -25,6 +41,7 @@ struct gga_ctx {
     uint32_t *heavy = nullptr; /* CDP heavy-vertex list */
     uint32_t heavy_cap = 0;
     BatchScratch *batch = nullptr;
+    ManyScratch many;
     bool trace_on = false;
     std::vector<uint32_t> trace_rounds; /* 5 words per round of the last traced solve */
     std::vector<uint32_t> trace_cta;    /* busy kilocycles per CTA */

@@ -975,7 +975,8 @@ gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m) {
 
 gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_t *first, uint32_t src,
                         bool sssp, const gga_params &p, int sms, cudaStream_t st, cudaEvent_t ev0,
-                        cudaEvent_t ev1, FrontierResult *res, bool trace, const LightHeavy &lh) {
+                        cudaEvent_t ev1, FrontierResult *res, bool trace, const LightHeavy &lh,
+                        FrontierCtl *hctl_async) {
     Args a;
     memset(&a, 0, sizeof a);
     if (trace) {
@@ -1035,10 +1036,28 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     }
     if (r) return r;
     if (ev1) GGA_CK(cudaEventRecord(ev1, st));
+    if (res) {
+        res->launches = 1;
+        res->nblocks = a.nblocks;
+    }
+    if (hctl_async) { /* the caller waits, then calls frontier_verdict */
+        GGA_CK(cudaMemcpyAsync(hctl_async, s->ctl, sizeof(FrontierCtl), cudaMemcpyDeviceToHost, st));
+        return GGA_OK;
+    }
     GGA_CK(cudaMemcpyAsync(s->hctl, s->ctl, sizeof(FrontierCtl), cudaMemcpyDeviceToHost, st));
     gga_status w = dev_wait(st, 60.0);
     if (w) return w;
-    const FrontierCtl h = *s->hctl;
+    if ((w = frontier_verdict(*s->hctl))) return w;
+    if (res) {
+        res->rounds = s->hctl->rounds;
+        res->edges_relaxed = s->hctl->edges_relaxed;
+        res->kernel_ms = 0;
+        if (ev0 && ev1) cudaEventElapsedTime(&res->kernel_ms, ev0, ev1);
+    }
+    return GGA_OK;
+}
+
+gga_status frontier_verdict(const FrontierCtl &h) {
     if (h.err == GGA_DEV_TIMEOUT)
         return gga_fail(GGA_ERR_TIMEOUT, "frontier grid barrier timed out after %u rounds", h.rounds);
     if (h.err == GGA_DEV_OVERFLOW) return gga_fail(GGA_ERR_CUDA, "frontier queue overflow (internal error)");
@@ -1052,14 +1071,6 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
                         h.diag[0], h.diag[1], h.diag[2], h.diag[3], h.diag[4], h.diag[5], h.diag[6], h.diag[7],
                         h.diag[8], h.diag[9], h.diag[10], h.diag[11], h.diag[12], h.diag[13], h.diag[14], h.diag[15]);
     if (h.err != GGA_DEV_OK) return gga_fail(GGA_ERR_CUDA, "frontier kernel error %u", h.err);
-    if (res) {
-        res->rounds = h.rounds;
-        res->launches = 1;
-        res->edges_relaxed = h.edges_relaxed;
-        res->kernel_ms = 0;
-        res->nblocks = a.nblocks;
-        if (ev0 && ev1) cudaEventElapsedTime(&res->kernel_ms, ev0, ev1);
-    }
     return GGA_OK;
 }
 

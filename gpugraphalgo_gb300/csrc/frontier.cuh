@@ -69,7 +69,13 @@ struct LightHeavy {
  * unsplit view.  `lh.light` (SSSP, unsplit, delta > 0): light edges per row,
  * with view.col / view.wt in light-first row order; turns on
  * delta-stepping's light/heavy edge classes.  Distances land in s->dist
- * (view ids). */
+ * (view ids).  With hctl_async the call only queues the launch and the copy
+ * of its control block into *hctl_async (pinned) on `st`: the caller waits
+ * for the stream, checks the block with frontier_verdict and reads rounds
+ * and edges_relaxed from it (res gets launches and nblocks only). */
 gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_t *first, uint32_t src,
                         bool sssp, const gga_params &p, int sms, cudaStream_t st, cudaEvent_t ev0,
-                        cudaEvent_t ev1, FrontierResult *res, bool trace = false, const LightHeavy &lh = {});
+                        cudaEvent_t ev1, FrontierResult *res, bool trace = false, const LightHeavy &lh = {},
+                        FrontierCtl *hctl_async = nullptr);
+/* GGA_OK, or the error a finished launch's control block records. */
+gga_status frontier_verdict(const FrontierCtl &h);

@@ -16,6 +16,12 @@
                             cudaGetErrorString(e_));                                       \
     } while (0)
 
+/* GGA_OK, or GGA_ERR_CUDA with the error's text (for code that must not
+ * return early). */
+static inline gga_status gga_cuda_check(cudaError_t e) {
+    return e == cudaSuccess ? GGA_OK : gga_fail(GGA_ERR_CUDA, "%s", cudaGetErrorString(e));
+}
+
 /* Device-resident graph (one per gga_graph).  The unsplit CSR is 0-based;
  * the split view is the reference's NodeSplit result re-based to 0
  * (s_off[k] = psrc[k] - 1 for k < ns). */

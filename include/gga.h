@@ -200,6 +200,21 @@ gga_status gga_sssp(gga_ctx *ctx, gga_graph *g, uint32_t src, gga_variant varian
 gga_status gga_solve(gga_ctx *ctx, gga_graph *g, gga_algo algo, uint32_t src,
                      gga_variant variant, uint32_t *dist_out, gga_stats *stats);
 
+/* n single-source traversals of g on the frontier engine, one after
+ * another; row i of dist_out (n rows of nodes_orig uint32, host or device
+ * memory) receives source srcs[i]'s distances, copied on a second stream
+ * while the next traversal runs.  Distances and per-source stats are those
+ * of n gga_solve calls with GGA_VARIANT_FRONTIER (stats: NULL or n entries;
+ * total_ms is the call's wall time / n).  With pageable host memory each
+ * copy blocks the host, so use gga_host_alloc memory for the overlap.  No
+ * counterpart in the reference, whose executables run one source per
+ * process (bfs_sssp.cu:149-330). */
+gga_status gga_solve_many(gga_ctx *ctx, gga_graph *g, gga_algo algo, uint32_t n, const uint32_t *srcs,
+                          uint32_t *dist_out, gga_stats *stats);
+/* Page-locked host memory, e.g. for gga_solve_many's dist_out. */
+gga_status gga_host_alloc(size_t bytes, void **out);
+void gga_host_free(void *p);
+
 /* Frontier-engine parameters (picked by gga_autotune when not set). */
 typedef struct gga_params {
     uint32_t block_threads;  /* CTA size: 256, 512 or 1024 */

@@ -392,3 +392,48 @@ def test_sssp_pull_needs_equal_reverse_weights(ctx):
     assert "pull" not in kinds
     with pytest.raises(gga.GGAError):
         ctx.set_params(sssp_pull=3)
+
+
+@pytest.mark.parametrize("algo", ["bfs", "sssp"])
+def test_solve_many_matches_single_solves(ctx, algo):
+    """gga_solve_many: back-to-back traversals with the copies on a second
+    stream give each source's single-solve distances and stats, into pinned
+    or pageable host memory, on split and unsplit graphs."""
+    for g in (gga.Graph.rmat(14, 16, seed=12), gga.Graph.grid(64, 50, seed=3)):
+        srcs = [int(np.argmax(g.degrees())), 0, 17, 5, 0, 999 % g.n, 33]  # repeats and more than the ring
+        pinned = gga.pinned_empty((len(srcs), g.n))
+        got, st = ctx.solve_many(g, algo, srcs, out=pinned, stats=True)
+        assert got is pinned
+        page = ctx.solve_many(g, algo, srcs)
+        for i, s in enumerate(srcs):
+            want, ws = ctx.solve(g, algo, s, "frontier", stats=True)
+            np.testing.assert_array_equal(got[i], want, err_msg=f"src #{i}={s}")
+            np.testing.assert_array_equal(page[i], want)
+            assert st[i]["vertices_reached"] == ws["vertices_reached"]
+            assert st[i]["edges_reached"] == ws["edges_reached"]
+            assert st[i]["iterations"] == ws["iterations"] and st[i]["kernel_ms"] > 0
+        np.testing.assert_array_equal(got[0], _oracle_dist(g, algo, srcs[0]))
+    gs = gga.Graph.rmat(12, 8, seed=4)
+    gs.cudaCopy(ctx)
+    gs.NodeSplit(ctx, 4)
+    try:
+        srcs = [0, 3, 100, 7]
+        got = ctx.solve_many(gs, algo, srcs)
+        for i, s in enumerate(srcs):
+            np.testing.assert_array_equal(got[i], _oracle_dist(gs, algo, s))
+    finally:
+        gs.NodeSplit(ctx, 0)
+
+
+def test_solve_many_edges(ctx):
+    g = gga.Graph.rmat(10, 8, seed=2)
+    assert ctx.solve_many(g, "bfs", []).shape == (0, g.n)
+    with pytest.raises(gga.GGAError) as ex:
+        ctx.solve_many(g, "sssp", [0, g.n])
+    assert ex.value.status == gga.ERR_INVALID_ARG
+    torch = pytest.importorskip("torch")
+    out = torch.empty((3, g.n), dtype=torch.int32, device="cuda")
+    ctx.solve_many(g, "sssp", [1, 2, 3], out=out)
+    got = out.cpu().numpy().view(np.uint32)
+    for i, s in enumerate([1, 2, 3]):
+        np.testing.assert_array_equal(got[i], _oracle_dist(g, "sssp", s))
