@@ -77,6 +77,7 @@ class Params(C.Structure):
         ("bfs_beta", u32),
         ("sssp_light_heavy", u32),
         ("sssp_pull", u32),
+        ("sssp_tail", u32),
     ]
 
     def as_dict(self):

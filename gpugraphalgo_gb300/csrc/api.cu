@@ -642,7 +642,8 @@ gga_status gga_autotune(gga_ctx *c, gga_graph *g, uint32_t trials, gga_params *c
             GGA_CK(cudaMalloc((void **)&tmp, (size_t)g->n * sizeof(uint32_t)));
         }
         const uint32_t base = best.sssp_delta;
-        const uint32_t deltas[] = {base / 4 ? base / 4 : 1, base / 2 ? base / 2 : 1, base, base * 2, base * 4, 0};
+        const uint32_t deltas[] = {base / 4 ? base / 4 : 1, base / 2 ? base / 2 : 1, base * 3 / 4 ? base * 3 / 4 : 1,
+                                   base, base * 3 / 2, base * 2, base * 4, 0};
         const uint32_t sizes[] = {256, 512};
         double best_ms = 1e30;
         gga_params saved = c->params;

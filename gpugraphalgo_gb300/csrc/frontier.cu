@@ -77,6 +77,10 @@ struct Args {
      * 1 when the cost rule picks it, 2 always */
     uint32_t pull;
     uint32_t heavy_edges; /* edges with w >= delta */
+    /* SSSP: when a bucket opens with at most this many far-pile entries, the
+     * threshold goes to infinity and the rest runs as one label-correcting
+     * frontier over whole rows (0: never) */
+    uint32_t tail_at;
 };
 
 /* Round record (block 0, thread 0) when tracing. */
@@ -126,6 +130,7 @@ struct Ctrl {
     uint32_t nn, fn, fmin;   /* staged near / far counts, smallest far distance */
     uint32_t base_i, base_e; /* flush allocation */
     uint32_t nitems, total, fc, fm;
+    uint32_t full; /* SSSP tail: near entries cover whole rows, no heavy lists */
     uint32_t hbase_i, hbase_e, hn, htot; /* heavy list: flush allocation, size at round start */
     uint32_t ws[32];         /* block-scan scratch */
     unsigned long long ws64[32];
@@ -182,7 +187,7 @@ __device__ __forceinline__ void flush_near(const Args &a, Ctrl &C, uint32_t *sv,
                                            uint32_t r3n, uint32_t bucket) {
     if (nn == 0) return;
     const uint32_t tid = threadIdx.x;
-    const bool lh = a.light != nullptr; /* the same in every thread */
+    const bool lh = a.light != nullptr && !C.full; /* the same in every thread */
     const uint32_t hl = bucket % 3;
     const uint32_t chunk = (nn + BS - 1) / BS;
     const uint32_t j0 = min(tid * chunk, nn), j1 = min(j0 + chunk, nn);
@@ -673,6 +678,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
         C.nn = 0;
         C.fn = 0;
         C.fmin = NONE;
+        C.full = 0;
         if (blockIdx.x == 0) {
             ctl->far_min[0] = NONE;
             ctl->far_min[1] = NONE;
@@ -709,6 +715,8 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
     uint32_t bucket = 0;          /* SSSP: far passes so far (same value in every block) */
     bool heavy_done = false;      /* this bucket's heavy list was expanded (or pulled) */
     bool pulling = false;         /* this round's queue is a pull list */
+    bool tail = false;            /* SSSP: buckets ended, label-correcting from here */
+    uint32_t fpeak = 0;           /* SSSP: largest far pile seen at a round start */
     uint64_t hsettled = 0;        /* heavy edges of the closed buckets' vertices */
     bool bottom_up = false;       /* BFS direction of the current round */
     uint64_t unexplored = a.m;    /* edges of vertices not yet reached (same value in every block) */
@@ -744,6 +752,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
         }
         __syncthreads();
         const uint32_t nitems = C.nitems, total = C.total, fc = C.fc, fm = C.fm, hn = C.hn, htot = C.htot;
+        fpeak = max(fpeak, fc);
         const uint32_t units = min((uint32_t)(((uint64_t)total + U - 1) / U), a.ucap);
         const uint32_t hunits = min((uint32_t)(((uint64_t)htot + U - 1) / U), a.ucap);
         __syncthreads(); /* C is rewritten below */
@@ -764,6 +773,18 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
          * two buckets ago). */
         auto open_bucket = [&](uint32_t lowest) -> uint32_t {
             thr = lowest > NONE - a.delta ? NONE : lowest + a.delta;
+            if (!tail && fc <= a.tail_at && fc < fpeak) {
+                /* the pile is small and shrinking (opening buckets now drains
+                 * it faster than relaxations fill it): no more buckets.  Every
+                 * later improvement joins the near queue and expands its whole
+                 * row, so no heavy list is needed (C.full is read after the
+                 * next barrier).  On R-MAT the vertices left are low-degree and
+                 * mostly final already, so the label-correcting rounds redo
+                 * almost nothing while the tail's ~5 rounds per bucket go. */
+                tail = true;
+                thr = NONE;
+                if (tid == 0) C.full = 1;
+            }
             ++bucket;
             heavy_done = false;
             const uint32_t fq = fp == 2 ? 0 : fp + 1;
@@ -1008,6 +1029,7 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
                         MIN_UNIT, MAX_UNIT);
     a.scap = bs * (STAGE_BATCH + 1); /* < BS staged after a checkpoint, + one batch */
     a.delta = p.sssp_delta;
+    if (sssp && a.delta && p.sssp_tail != 1) a.tail_at = view.n / (p.sssp_tail ? p.sssp_tail : 4u);
     a.bu = !sssp && view.cc == nullptr && view.symmetric && p.bfs_direction == 0;
     if (sssp && lh.light && a.delta) {
         a.light = lh.light;

@@ -253,6 +253,12 @@ typedef struct gga_params {
      * the unsettled vertices' heavy edges plus n/2; 1 = always push;
      * 2 = always pull (where allowed).  Distances are the same. */
     uint32_t sssp_pull;
+    /* SSSP near-far tail: once a bucket opens with at most n / k far-pile
+     * entries and the pile smaller than the largest it has been, the
+     * threshold goes to infinity and the remaining vertices run as one
+     * label-correcting frontier over whole rows (no more buckets).  0 = k of
+     * 4, 1 = never, k > 1 = that k.  Distances are the same. */
+    uint32_t sssp_tail;
 } gga_params;
 /* p = NULL returns to the per-graph defaults. */
 gga_status gga_set_params(gga_ctx *ctx, const gga_params *p);

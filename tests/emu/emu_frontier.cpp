@@ -1,12 +1,13 @@
 /* Runs k_frontier (BFS or SSSP, optional bottom-up rounds or light/heavy
  * classes) on NB emulated blocks and compares with the oracle's distances.
- * args: dir NB row sssp iters delta bu alpha beta lh [pull]
+ * args: dir NB row sssp iters delta bu alpha beta lh [pull [tail]]
  * (pull: bucket closes by pull, 0 never, 1 cost rule, 2 always; the test
- * graphs have equal weights both ways) */
+ * graphs have equal weights both ways; tail: buckets end once one opens
+ * with at most this many far-pile entries, 0 never) */
 #include "kernel_frontier.inc"
 template <int BS, bool SSSP>
 int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint32_t alpha, uint32_t beta,
-        uint32_t delta, bool lhm, uint32_t pull) {
+        uint32_t delta, bool lhm, uint32_t pull, uint32_t tail) {
     auto off = rd(d + "/off.bin"), col = rd(d + "/col.bin"), wt = rd(d + "/wt.bin"), srcs = rd(d + "/srcs.bin");
     auto want = rd(d + (SSSP ? "/want_sssp.bin" : "/want_bfs.bin"));
     uint32_t n = off.size() - 1, m = col.size(), src = srcs[row];
@@ -26,6 +27,7 @@ int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint
     a.ctl = &ctl; a.cap = cap; a.ucap = ucap; a.src = src; a.iters = iters; a.unit = BS * iters; a.scap = BS * 9;
     a.delta = delta; a.nblocks = NB; a.max_rounds = 4 * n + 4096; a.timeout_ns = 60000000000ull;
     a.bu = bu; a.alpha = alpha; a.beta = beta;
+    if (SSSP && delta) a.tail_at = tail;
     std::vector<uint32_t> lcol(m + 4), lwt(m + 4), light(n + 1), hstamp(cap), hq[9], huf[3];
     for (auto &x : hq) x.assign(cap, 0);
     for (auto &x : huf) x.assign(ucap, 0);
@@ -64,7 +66,7 @@ int main(int argc, char **argv) {
     int nb = atoi(argv[2]), row = atoi(argv[3]), sssp = atoi(argv[4]);
     uint32_t iters = atoi(argv[5]), delta = atoi(argv[6]), bu = atoi(argv[7]), al = atoi(argv[8]), be = atoi(argv[9]);
     bool lhm = atoi(argv[10]);
-    uint32_t pull = argc > 11 ? atoi(argv[11]) : 0;
-    return sssp ? run<256, true>(nb, d, row, iters, 0, al, be, delta, lhm, pull)
-                : run<256, false>(nb, d, row, iters, bu, al, be, 0, false, 0);
+    uint32_t pull = argc > 11 ? atoi(argv[11]) : 0, tail = argc > 12 ? atoi(argv[12]) : 0;
+    return sssp ? run<256, true>(nb, d, row, iters, 0, al, be, delta, lhm, pull, tail)
+                : run<256, false>(nb, d, row, iters, bu, al, be, 0, false, 0, 0);
 }

@@ -437,3 +437,34 @@ def test_solve_many_edges(ctx):
     got = out.cpu().numpy().view(np.uint32)
     for i, s in enumerate([1, 2, 3]):
         np.testing.assert_array_equal(got[i], _oracle_dist(g, "sssp", s))
+
+
+@pytest.mark.parametrize("tail", [0, 1, 2, 64])
+def test_sssp_tail_matches_oracle(ctx, tail):
+    """Ending the buckets early (the rest as one label-correcting frontier
+    over whole rows) gives the same distances, with and without light/heavy
+    classes and pulled bucket closes."""
+    for g in (gga.Graph.rmat(15, 16, seed=41), gga.Graph.grid(96, 80, seed=6)):
+        for s in (int(np.argmax(g.degrees())), 11):
+            want = _oracle_dist(g, "sssp", s)
+            try:
+                for delta, lh, pull in ((16, 0, 0), (33, 0, 2), (100, 1, 1), (1, 0, 1)):
+                    ctx.set_params(sssp_delta=delta, sssp_tail=tail, sssp_light_heavy=lh, sssp_pull=pull)
+                    np.testing.assert_array_equal(ctx.sssp(g, s), want,
+                                                  err_msg=f"tail={tail} delta={delta} lh={lh} pull={pull} src={s}")
+            finally:
+                ctx.reset_params()
+
+
+def test_sssp_tail_cuts_rounds(ctx):
+    g = gga.Graph.rmat(16, 16, seed=8)
+    s = int(np.argmax(g.degrees()))
+    res = {}
+    try:
+        for tail in (0, 1):
+            ctx.set_params(sssp_delta=16, sssp_tail=tail)
+            res[tail] = ctx.sssp(g, s, stats=True)
+    finally:
+        ctx.reset_params()
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    assert res[0][1]["iterations"] < res[1][1]["iterations"]

@@ -77,20 +77,22 @@ def _run(emu, kernel, *args):
 
 
 # graph, blocks, source row, sssp, unit_iters, delta, bottom-up, alpha, beta, light/heavy,
-# pulling bucket closes (0 never, 1 cost rule, 2 always)
+# pulling bucket closes (0 never, 1 cost rule, 2 always), far-pile size that ends the buckets
 FRONTIER = [
-    ("r10", 4, 0, 0, 8, 0, 1, 15, 18, 0, 0),
-    ("r10", 3, 3, 0, 2, 0, 0, 15, 18, 0, 0),
-    ("grid", 4, 2, 0, 16, 0, 1, 1000, 1000, 0, 0),
-    ("r10", 4, 0, 1, 4, 33, 0, 15, 18, 1, 0),
-    ("r10", 2, 9, 1, 2, 64, 0, 15, 18, 1, 1),
-    ("grid", 4, 1, 1, 8, 100, 0, 15, 18, 1, 0),
-    ("grid", 3, 4, 1, 16, 0, 0, 15, 18, 0, 0),
-    ("r10", 4, 7, 1, 4, 1, 0, 15, 18, 1, 0),
-    ("r10", 4, 0, 1, 4, 33, 0, 15, 18, 1, 2),
-    ("grid", 3, 1, 1, 8, 100, 0, 15, 18, 1, 2),
-    ("r10", 2, 7, 1, 2, 1, 0, 15, 18, 1, 2),
-    ("r10", 4, 11, 1, 4, 20, 0, 15, 18, 1, 1),
+    ("r10", 4, 0, 0, 8, 0, 1, 15, 18, 0, 0, 0),
+    ("r10", 3, 3, 0, 2, 0, 0, 15, 18, 0, 0, 0),
+    ("grid", 4, 2, 0, 16, 0, 1, 1000, 1000, 0, 0, 0),
+    ("r10", 4, 0, 1, 4, 33, 0, 15, 18, 1, 0, 0),
+    ("r10", 2, 9, 1, 2, 64, 0, 15, 18, 1, 1, 64),
+    ("grid", 4, 1, 1, 8, 100, 0, 15, 18, 1, 0, 30),
+    ("grid", 3, 4, 1, 16, 0, 0, 15, 18, 0, 0, 0),
+    ("r10", 4, 7, 1, 4, 1, 0, 15, 18, 1, 0, 0),
+    ("r10", 4, 0, 1, 4, 33, 0, 15, 18, 1, 2, 0),
+    ("grid", 3, 1, 1, 8, 100, 0, 15, 18, 1, 2, 0),
+    ("r10", 2, 7, 1, 2, 1, 0, 15, 18, 1, 2, 200),
+    ("r10", 4, 11, 1, 4, 20, 0, 15, 18, 1, 1, 64),
+    ("r10", 4, 3, 1, 4, 8, 0, 15, 18, 1, 1, 1024),
+    ("grid", 4, 5, 1, 4, 50, 0, 15, 18, 0, 0, 100),
 ]
 
 
