@@ -411,7 +411,9 @@ def test_solve_many_matches_single_solves(ctx, algo):
             np.testing.assert_array_equal(page[i], want)
             assert st[i]["vertices_reached"] == ws["vertices_reached"]
             assert st[i]["edges_reached"] == ws["edges_reached"]
-            assert st[i]["iterations"] == ws["iterations"] and st[i]["kernel_ms"] > 0
+            assert st[i]["kernel_ms"] > 0
+            if algo == "bfs":  # BFS rounds are the levels; SSSP's depend on relaxation timing
+                assert st[i]["iterations"] == ws["iterations"]
         np.testing.assert_array_equal(got[0], _oracle_dist(g, algo, srcs[0]))
     gs = gga.Graph.rmat(12, 8, seed=4)
     gs.cudaCopy(ctx)
