@@ -11,10 +11,10 @@
  *   - expansion is EDGE balanced: every queued vertex carries the exclusive
  *     offset of its edge range in the round's concatenated edge list, and
  *     the list is cut into fixed units of U = block_threads * unit_iters
- *     edges.  A CTA takes a unit by atomic ticket, loads the unit's queue
- *     entries into shared memory and walks the unit with consecutive threads
- *     on consecutive edges (coalesced), so a 10^5-degree R-MAT hub is spread
- *     over many CTAs like any other edges;
+ *     edges.  Units are dealt round-robin to the CTAs; a CTA loads its
+ *     unit's queue entries into shared memory and walks the unit with
+ *     consecutive threads on consecutive edges (coalesced), so a
+ *     10^5-degree R-MAT hub is spread over many CTAs like any other edges;
  *   - pushes are staged per CTA in shared memory (shared atomics only) and
  *     published once per unit with ONE 64-bit atomicAdd that allocates queue
  *     slots and edge offsets together; the same flush marks the next round's
@@ -426,7 +426,10 @@ __device__ __forceinline__ void pull_scan(const Args &a, uint32_t thr, uint32_t 
  *
  * PULL (SSSP): the entries are unsettled vertices and their heavy edges;
  * an edge whose other end u is settled (d(u) < settled) offers d(u) + w to
- * the entry's vertex. */
+ * the entry's vertex.  The offers meet in shared memory first (one shared
+ * atomicMin per edge into the entry's slot of t_best, which follows t_du),
+ * and each entry then makes one global atomicMin, instead of one per edge
+ * with a vertex's edges contending for its word. */
 template <int BS, bool SSSP, bool PULL = false>
 __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage &S, uint32_t *t_o, uint32_t *t_b,
                                              uint32_t *t_du, const uint32_t *qv, const uint32_t *qo,
@@ -436,6 +439,7 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                                              unsigned long long &relaxed) {
     const uint32_t tid = threadIdx.x, U = a.unit, G = gridDim.x;
     FrontierCtl *ctl = a.ctl;
+    uint32_t *t_best = t_du + (U + 1); /* PULL: smallest offer per entry */
     /* entries [i0, i0 + cnt) hold unit k's edges (every thread reads the
      * same two boundary words) */
     auto bounds = [&](uint32_t k, uint32_t &i0, uint32_t &cnt) {
@@ -483,6 +487,7 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                     t_o[j] = o[q];
                     t_b[j] = b[q];
                     if (SSSP) t_du[j] = x[q];
+                    if (PULL) t_best[j] = NONE;
                 }
             }
         }
@@ -510,7 +515,7 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                         v[q] = __ldg(a.col + ei);
                         if (PULL) {
                             alt[q] = __ldg(a.wt + ei);
-                            tgt[q] = t_du[lo];
+                            tgt[q] = lo;
                         } else {
                             alt[q] = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
                         }
@@ -523,14 +528,11 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
 #pragma unroll
             for (uint32_t q = 0; q < PB; ++q)
                 probe[q] = act[q] ? (SSSP ? __ldcg(a.dist + v[q]) : __ldcg(a.bits + (v[q] >> 5))) : 0u;
-            if (PULL) { /* the offer d(u) + w to the entry's vertex, from settled u only */
+            if (PULL) { /* the offer d(u) + w to the entry's slot, from settled u only */
 #pragma unroll
-                for (uint32_t q = 0; q < PB; ++q) {
-                    act[q] = act[q] && probe[q] < settled;
-                    alt[q] += probe[q];
-                    v[q] = tgt[q];
-                    probe[q] = NONE;
-                }
+                for (uint32_t q = 0; q < PB; ++q)
+                    if (act[q] && probe[q] < settled) atomicMin(t_best + tgt[q], probe[q] + alt[q]);
+                continue;
             }
             /* updates in phases, so a thread's atomics for its PB edges are in
              * flight together instead of one dependent pair after another:
@@ -597,6 +599,20 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                     }
             }
         }
+        if (PULL) { /* each entry's best offer, once */
+            __syncthreads();
+            for (uint32_t j = tid; j < cnt; j += BS) {
+                const uint32_t best = t_best[j], vq = t_du[j];
+                if (best == NONE || best >= atomicMin(a.dist + vq, best)) continue;
+                if (best < thr) {
+                    if (atomicExch(a.stamp + vq, round + 1) != round + 1) stage_near(a, C, S.sv, vq);
+                } else {
+                    atomicMin(&C.fmin, best);
+                    const uint32_t bit = 1u << (vq & 31);
+                    if (!(atomicOr(a.farbits + (vq >> 5), bit) & bit)) stage_far(a, C, S.sf, vq);
+                }
+            }
+        }
         if (tid == 0) relaxed += eend - ebase;
         k = kn;
         i0 = ni0;
@@ -656,7 +672,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
     const uint32_t U = a.unit, SC = a.scap;
     const bool lh = SSSP && a.light != nullptr;
     uint32_t *t_o = dyn, *t_b = dyn + (U + 1), *t_du = dyn + 2 * (U + 1);
-    uint32_t *stage = dyn + (SSSP ? 3u : 2u) * (U + 1);
+    uint32_t *stage = dyn + (SSSP ? 4u : 2u) * (U + 1);
     Stage S;
     S.sv = stage;
     S.sf = stage + SC;
@@ -908,7 +924,7 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
 
 template <int BS, bool SSSP>
 size_t dyn_smem(uint32_t unit, uint32_t scap) {
-    return ((size_t)(unit + 1) * (SSSP ? 3 : 2) + (size_t)scap * (SSSP ? 2 : 1)) * sizeof(uint32_t);
+    return ((size_t)(unit + 1) * (SSSP ? 4 : 2) + (size_t)scap * (SSSP ? 2 : 1)) * sizeof(uint32_t);
 }
 
 template <int BS, bool SSSP>
