@@ -447,18 +447,25 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
         const uint32_t i1 = k + 1 < units ? min(__ldcg(uf + k + 1), nitems - 1) : nitems - 1;
         cnt = i1 >= i0 ? min(i1 - i0 + 1, U + 1) : 1u;
     };
-    uint32_t k = blockIdx.x, i0 = 0, cnt = 0;
-    if (k < units) bounds(k, i0, cnt);
+    /* A round with fewer units than CTAs cuts each unit into SU parts of
+     * U / SU edges (SU a power of two dividing iters, SU x units <= G), so
+     * more CTAs share its edges and its pushes; a CTA then takes one part
+     * (the unit's whole table, the part's edges). */
+    uint32_t SU = 1;
+    while (units * (SU * 2) <= G && a.iters % (SU * 2) == 0) SU *= 2;
+    const uint32_t vunits = units * SU, its = a.iters / SU, esub = U / SU;
+    uint32_t k = blockIdx.x, i0 = 0, cnt = 0; /* k: part index */
+    if (k < vunits) bounds(k / SU, i0, cnt);
     for (;;) {
         __syncthreads(); /* previous unit's table reads and staging done */
         const uint32_t nn = C.nn, fn = SSSP ? C.fn : 0u;
         if (nn >= BS) flush_near<BS>(a, C, S.sv, nn, nxt, r3n, bucket);
         if (SSSP && fn >= BS) flush_far<BS>(a, C, S.sf, fn, fp);
-        if (k >= units) break;
+        if (k >= vunits) break;
         const uint32_t kn = k + G;
         uint32_t ni0 = 0, ncnt = 0;
-        if (kn < units) bounds(kn, ni0, ncnt); /* used after this unit */
-        const uint32_t ebase = k * U, eend = min(ebase + U, total);
+        if (kn < vunits) bounds(kn / SU, ni0, ncnt); /* used after this unit */
+        const uint32_t ebase = (k / SU) * U + (k % SU) * esub, eend = min(ebase + esub, total);
         /* the unit's entries, TB per thread in flight: all entry loads, then
          * (SSSP) all distance loads, then the stores, so a table of up to
          * TB x BS entries costs two dependent L2 round trips, not 2 x TB */
@@ -493,14 +500,14 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
         }
         __syncthreads();
         constexpr uint32_t PB = STAGE_BATCH;
-        for (uint32_t it0 = 0; it0 < a.iters; it0 += PB) {
+        for (uint32_t it0 = 0; it0 < its; it0 += PB) {
             if (it0) checkpoint<BS, SSSP>(a, C, S, nxt, r3n, fp, bucket, BS);
             uint32_t v[PB], alt[PB], probe[PB], tgt[PB];
             bool act[PB];
 #pragma unroll
             for (uint32_t q = 0; q < PB; ++q) {
                 const uint32_t e = ebase + (it0 + q) * BS + tid;
-                act[q] = it0 + q < a.iters && e < eend;
+                act[q] = it0 + q < its && e < eend;
                 v[q] = 0;
                 alt[q] = 0;
                 tgt[q] = 0;
