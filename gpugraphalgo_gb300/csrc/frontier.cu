@@ -281,11 +281,11 @@ __device__ __forceinline__ void checkpoint(const Args &a, Ctrl &C, const Stage &
 /* One bottom-up BFS round (Beamer, Asanovic, Patterson, SC 2012): every
  * unvisited vertex looks through its neighbours for one at level `round`
  * (dist == round marks the frontier exactly: later levels are round + 1 or
- * unset) and stops at the first.  A warp owns one 32-vertex word of the
- * visited bitmap per step, lane i vertex 32w + i; the warp's finds are
- * written back as one word and appended to the next round's queue with one
- * packed 64-bit atomicAdd, so the queue has the same format as after a
- * top-down round.  Needs every edge's reverse (a symmetric graph).  The loop
+ * unset) and stops at the first.  A warp owns two 32-vertex words of the
+ * visited bitmap per step, lane i vertices 32w + i of each; the warp's
+ * finds are written back as whole words and appended to the next round's
+ * queue with one packed 64-bit atomicAdd, so the queue has the same format
+ * as after a top-down round.  Needs every edge's reverse (a symmetric graph).  The loop
  * trip count is warp-uniform; the per-lane neighbour scan reconverges before
  * the ballot. */
 template <int BS>
@@ -297,56 +297,89 @@ __device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, u
     const uint32_t nwords = (a.n + 31) / 32;
     uint32_t *qv = sel(nxt, a.qv0, a.qv1), *qo = sel(nxt, a.qo0, a.qo1), *qb = sel(nxt, a.qb0, a.qb1);
     uint32_t *uf = sel(nxt, a.uf0, a.uf1);
-    for (uint64_t w = gw; w < nwords; w += nw) {
-        const uint32_t vw = __ldcg(a.bits + w);
-        const uint32_t v = (uint32_t)w * 32u + lane;
-        bool found = false;
-        uint32_t b = 0, d = 0;
-        if (v < a.n && !(vw & (1u << lane))) {
-            b = __ldg(a.off + v);
-            const uint32_t e1 = __ldg(a.off + v + 1);
-            d = e1 - b;
-            for (uint32_t e = b; e < e1 && !found; e += 4) {
-                uint32_t u[4];
+    /* NW words per warp step: their loads and neighbour scans are in flight
+     * together, and their finds share one queue allocation */
+    constexpr uint32_t NW = 2;
+    static_assert(NW == 2, "the queue allocation below combines exactly two words");
+    for (uint64_t w0 = gw * NW; w0 < nwords; w0 += nw * NW) {
+        uint32_t vw[NW], v[NW], b[NW], e1[NW], cur[NW];
+        bool open[NW], found[NW];
 #pragma unroll
-                for (uint32_t q = 0; q < 4; ++q) u[q] = e + q < e1 ? __ldg(a.col + e + q) : NONE;
+        for (uint32_t k = 0; k < NW; ++k) {
+            const uint64_t wk = w0 + k;
+            vw[k] = wk < nwords ? __ldcg(a.bits + wk) : FULL;
+            v[k] = (uint32_t)wk * 32u + lane;
+            open[k] = wk < nwords && v[k] < a.n && !(vw[k] & (1u << lane));
+            found[k] = false;
+            b[k] = e1[k] = 0;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < NW; ++k)
+            if (open[k]) {
+                b[k] = __ldg(a.off + v[k]);
+                e1[k] = __ldg(a.off + v[k] + 1);
+            }
+#pragma unroll
+        for (uint32_t k = 0; k < NW; ++k) cur[k] = b[k];
+        for (;;) { /* per lane; the lanes reconverge before the ballots */
+            bool act[NW], any = false;
+#pragma unroll
+            for (uint32_t k = 0; k < NW; ++k) {
+                act[k] = open[k] && !found[k] && cur[k] < e1[k];
+                any |= act[k];
+            }
+            if (!any) break;
+            uint32_t u[NW][4];
+#pragma unroll
+            for (uint32_t k = 0; k < NW; ++k)
+#pragma unroll
+                for (uint32_t q = 0; q < 4; ++q) u[k][q] = act[k] && cur[k] + q < e1[k] ? __ldg(a.col + cur[k] + q) : NONE;
+#pragma unroll
+            for (uint32_t k = 0; k < NW; ++k) {
 #pragma unroll
                 for (uint32_t q = 0; q < 4; ++q)
-                    if (u[q] != NONE && __ldcg(a.dist + u[q]) == round) found = true;
-                relaxed += min(4u, e1 - e);
+                    if (u[k][q] != NONE && __ldcg(a.dist + u[k][q]) == round) found[k] = true;
+                if (act[k]) {
+                    relaxed += min(4u, e1[k] - cur[k]);
+                    cur[k] += 4;
+                }
             }
         }
-        const uint32_t fm = __ballot_sync(FULL, found);
-        if (fm == 0) continue; /* warp-uniform */
-        if (found) a.dist[v] = round + 1;
-        if (lane == 0) a.bits[w] = vw | fm; /* this warp is the word's only writer this round */
-        const uint32_t dd = found ? d : 0u;
-        uint32_t incl = dd;
+        uint32_t fm[NW], dd[NW], incl[NW];
 #pragma unroll
-        for (int k = 1; k < 32; k <<= 1) {
-            const uint32_t y = __shfl_up_sync(FULL, incl, k);
-            if (lane >= (uint32_t)k) incl += y;
+        for (uint32_t k = 0; k < NW; ++k) fm[k] = __ballot_sync(FULL, found[k]);
+        if ((fm[0] | fm[1]) == 0) continue; /* warp-uniform */
+#pragma unroll
+        for (uint32_t k = 0; k < NW; ++k) {
+            if (found[k]) a.dist[v[k]] = round + 1;
+            /* this warp is the word's only writer this round */
+            if (lane == 0 && fm[k]) a.bits[w0 + k] = vw[k] | fm[k];
+            dd[k] = found[k] ? e1[k] - b[k] : 0u;
+            incl[k] = dd[k];
         }
-        const uint32_t wtot = __shfl_sync(FULL, incl, 31);
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+#pragma unroll
+            for (uint32_t k = 0; k < NW; ++k) {
+                const uint32_t y = __shfl_up_sync(FULL, incl[k], s);
+                if (lane >= (uint32_t)s) incl[k] += y;
+            }
+        }
+        const uint32_t tot0 = __shfl_sync(FULL, incl[0], 31), tot1 = __shfl_sync(FULL, incl[1], 31);
+        const uint32_t cnt0 = (uint32_t)__popc(fm[0]), cnt1 = (uint32_t)__popc(fm[1]);
         unsigned long long old = 0;
         if (lane == 0)
-            old = atomicAdd(&a.ctl->qctr[r3n], ((unsigned long long)__popc(fm) << 32) | (unsigned long long)wtot);
+            old = atomicAdd(&a.ctl->qctr[r3n],
+                            ((unsigned long long)(cnt0 + cnt1) << 32) | (unsigned long long)(tot0 + tot1));
         old = __shfl_sync(FULL, old, 0);
-        if (found) {
-            const uint32_t idx = (uint32_t)(old >> 32) + (uint32_t)__popc(fm & lanemask_lt());
-            const uint32_t o = (uint32_t)old + incl - dd;
-            if (idx < a.cap) {
-                qv[idx] = v;
-                qo[idx] = o;
-                qb[idx] = b;
-                for (uint64_t k = ((uint64_t)o + a.unit - 1) / a.unit; k * a.unit < (uint64_t)o + dd; ++k) {
-                    if (k < a.ucap) uf[k] = idx;
-                    else set_err(a.ctl, GGA_DEV_OVERFLOW_UNITS);
-                }
-            } else {
-                set_err(a.ctl, GGA_DEV_OVERFLOW);
+        /* word 0's finds first, then word 1's */
+#pragma unroll
+        for (uint32_t k = 0; k < NW; ++k)
+            if (found[k]) {
+                const uint32_t idx = (uint32_t)(old >> 32) + (k ? cnt0 : 0u) + (uint32_t)__popc(fm[k] & lanemask_lt());
+                const uint32_t o = (uint32_t)old + (k ? tot0 : 0u) + incl[k] - dd[k];
+                put_entry(a, idx, o, v[k], b[k], dd[k], qv, qo, qb, uf);
             }
-        }
     }
 }
 
@@ -465,7 +498,8 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
         const uint32_t kn = k + G;
         uint32_t ni0 = 0, ncnt = 0;
         if (kn < vunits) bounds(kn / SU, ni0, ncnt); /* used after this unit */
-        const uint32_t ebase = (k / SU) * U + (k % SU) * esub, eend = min(ebase + esub, total);
+        /* a last unit's later parts may start past the round's last edge */
+        const uint32_t ebase = (k / SU) * U + (k % SU) * esub, eend = max(ebase, min(ebase + esub, total));
         /* the unit's entries, TB per thread in flight: all entry loads, then
          * (SSSP) all distance loads, then the stores, so a table of up to
          * TB x BS entries costs two dependent L2 round trips, not 2 x TB */
