@@ -213,7 +213,7 @@ gga_params ctx_default_params(const gga_graph *g) {
     gga_params p;
     memset(&p, 0, sizeof p);
     p.block_threads = 256;
-    p.unit_iters = 0; /* per algorithm: 8 for BFS, 4 for SSSP */
+    p.unit_iters = 0; /* per algorithm: 4096 edges per unit for BFS, 4 per thread for SSSP */
     const double wavg = g->wavg > 0 ? g->wavg : 1.0; /* computed once when the graph is built */
     const double davg = g->n ? (double)g->m / g->n : 1.0;
     /* bucket width ~ a few average weights over the average degree */

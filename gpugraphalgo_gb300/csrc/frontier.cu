@@ -44,6 +44,7 @@ constexpr uint32_t NONE = 0xffffffffu;
 constexpr uint32_t MIN_UNIT = 512;  /* smallest edges-per-unit the buffers are sized for */
 constexpr uint32_t MAX_UNIT = 4096; /* largest edges-per-unit (shared-memory bound) */
 constexpr uint32_t STAGE_BATCH = 4; /* edges per thread in flight between staging checkpoints */
+constexpr uint32_t BU_WORDS = 4;    /* bottom-up BFS: visited-bitmap words per warp step */
 
 struct Args {
     const uint32_t *off, *col, *wt, *cc;
@@ -281,8 +282,8 @@ __device__ __forceinline__ void checkpoint(const Args &a, Ctrl &C, const Stage &
 /* One bottom-up BFS round (Beamer, Asanovic, Patterson, SC 2012): every
  * unvisited vertex looks through its neighbours for one at level `round`
  * (dist == round marks the frontier exactly: later levels are round + 1 or
- * unset) and stops at the first.  A warp owns two 32-vertex words of the
- * visited bitmap per step, lane i vertices 32w + i of each; the warp's
+ * unset) and stops at the first.  A warp owns BU_WORDS 32-vertex words of
+ * the visited bitmap per step, lane i vertices 32w + i of each; the warp's
  * finds are written back as whole words and appended to the next round's
  * queue with one packed 64-bit atomicAdd, so the queue has the same format
  * as after a top-down round.  Needs every edge's reverse (a symmetric graph).  The loop
@@ -299,8 +300,7 @@ __device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, u
     uint32_t *uf = sel(nxt, a.uf0, a.uf1);
     /* NW words per warp step: their loads and neighbour scans are in flight
      * together, and their finds share one queue allocation */
-    constexpr uint32_t NW = 2;
-    static_assert(NW == 2, "the queue allocation below combines exactly two words");
+    constexpr uint32_t NW = BU_WORDS;
     for (uint64_t w0 = gw * NW; w0 < nwords; w0 += nw * NW) {
         uint32_t vw[NW], v[NW], b[NW], e1[NW], cur[NW];
         bool open[NW], found[NW];
@@ -345,10 +345,13 @@ __device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, u
                 }
             }
         }
-        uint32_t fm[NW], dd[NW], incl[NW];
+        uint32_t fm[NW], dd[NW], incl[NW], fany = 0;
 #pragma unroll
-        for (uint32_t k = 0; k < NW; ++k) fm[k] = __ballot_sync(FULL, found[k]);
-        if ((fm[0] | fm[1]) == 0) continue; /* warp-uniform */
+        for (uint32_t k = 0; k < NW; ++k) {
+            fm[k] = __ballot_sync(FULL, found[k]);
+            fany |= fm[k];
+        }
+        if (fany == 0) continue; /* warp-uniform */
 #pragma unroll
         for (uint32_t k = 0; k < NW; ++k) {
             if (found[k]) a.dist[v[k]] = round + 1;
@@ -365,19 +368,23 @@ __device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, u
                 if (lane >= (uint32_t)s) incl[k] += y;
             }
         }
-        const uint32_t tot0 = __shfl_sync(FULL, incl[0], 31), tot1 = __shfl_sync(FULL, incl[1], 31);
-        const uint32_t cnt0 = (uint32_t)__popc(fm[0]), cnt1 = (uint32_t)__popc(fm[1]);
+        /* the words' finds in word order: entries before word k, edges before it */
+        uint32_t pc[NW], pe[NW], allc = 0, alle = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < NW; ++k) {
+            pc[k] = allc;
+            pe[k] = alle;
+            allc += (uint32_t)__popc(fm[k]);
+            alle += __shfl_sync(FULL, incl[k], 31);
+        }
         unsigned long long old = 0;
-        if (lane == 0)
-            old = atomicAdd(&a.ctl->qctr[r3n],
-                            ((unsigned long long)(cnt0 + cnt1) << 32) | (unsigned long long)(tot0 + tot1));
+        if (lane == 0) old = atomicAdd(&a.ctl->qctr[r3n], ((unsigned long long)allc << 32) | (unsigned long long)alle);
         old = __shfl_sync(FULL, old, 0);
-        /* word 0's finds first, then word 1's */
 #pragma unroll
         for (uint32_t k = 0; k < NW; ++k)
             if (found[k]) {
-                const uint32_t idx = (uint32_t)(old >> 32) + (k ? cnt0 : 0u) + (uint32_t)__popc(fm[k] & lanemask_lt());
-                const uint32_t o = (uint32_t)old + (k ? tot0 : 0u) + incl[k] - dd[k];
+                const uint32_t idx = (uint32_t)(old >> 32) + pc[k] + (uint32_t)__popc(fm[k] & lanemask_lt());
+                const uint32_t o = (uint32_t)old + pe[k] + incl[k] - dd[k];
                 put_entry(a, idx, o, v[k], b[k], dd[k], qv, qo, qb, uf);
             }
     }
@@ -1075,9 +1082,10 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     a.ucap = s->ucap;
     a.src = src;
     const uint32_t bs = p.block_threads ? p.block_threads : 256;
-    /* measured on R-MAT 22 (GB300): BFS is fastest with 2048-edge units,
-     * SSSP with 1024-edge units (one batch of edges per thread per unit) */
-    a.iters = p.unit_iters ? p.unit_iters : (sssp ? 4 : 8);
+    /* measured on R-MAT 22 (GB300): BFS is fastest with the largest units
+     * (4096 edges), SSSP with 1024-edge units (one batch of edges per
+     * thread per unit) */
+    a.iters = p.unit_iters ? p.unit_iters : (sssp ? 4 : MAX_UNIT / bs);
     if (a.iters < 2 || a.iters > 16)
         return gga_fail(GGA_ERR_INVALID_ARG, "unit_iters must be in [2, 16] (got %u)", a.iters);
     a.unit = bs * a.iters;

@@ -218,7 +218,8 @@ void gga_host_free(void *p);
 /* Frontier-engine parameters (picked by gga_autotune when not set). */
 typedef struct gga_params {
     uint32_t block_threads;  /* CTA size: 256, 512 or 1024 */
-    uint32_t unit_iters;     /* edges per work unit = block_threads x this (2..16; 0 = 8 for BFS, 4 for SSSP) */
+    uint32_t unit_iters;     /* edges per work unit = block_threads x this (2..16; 0 = 4096 / block_threads for
+                              * BFS, 4 for SSSP) */
     uint32_t sssp_delta;     /* near-far bucket width (0 = plain improved-vertex frontier) */
     uint32_t use_split;      /* expand over the node-split graph when one exists */
     uint32_t blocks_per_sm;  /* persistent grid = SMs x this (0 = occupancy maximum) */
