@@ -681,19 +681,31 @@ __device__ __forceinline__ void split_pile(const Args &a, Ctrl &C, const Stage &
                                            uint32_t fc, uint32_t thr, uint32_t thr_old, uint32_t round,
                                            uint32_t nxt, uint32_t r3n, uint32_t bucket) {
     const uint32_t tid = threadIdx.x;
-    const uint64_t gthreads = (uint64_t)gridDim.x * BS;
+    /* PE entries per thread per step, their loads in flight together; a
+     * step stages at most PE x BS, within the stage's room after a
+     * checkpoint (scap >= BS x (STAGE_BATCH + 1)) */
+    constexpr uint32_t PE = STAGE_BATCH;
+    const uint64_t gstep = (uint64_t)gridDim.x * BS * PE;
     const uint32_t *fin = sel3(fp, a.far0, a.far1, a.far2);
-    for (uint64_t base = (uint64_t)blockIdx.x * BS; base < fc; base += gthreads) {
-        const uint64_t i = base + tid;
-        if (i < fc) {
-            const uint32_t v = __ldcg(fin + i);
-            const uint32_t d = __ldcg(a.dist + v);
-            if (d >= thr) {
-                atomicMin(&C.fmin, d);
-                stage_far(a, C, S.sf, v);
+    for (uint64_t base = (uint64_t)blockIdx.x * BS * PE; base < fc; base += gstep) {
+        uint32_t v[PE], d[PE];
+#pragma unroll
+        for (uint32_t q = 0; q < PE; ++q) {
+            const uint64_t i = base + q * BS + tid;
+            v[q] = i < fc ? __ldcg(fin + i) : NONE;
+        }
+#pragma unroll
+        for (uint32_t q = 0; q < PE; ++q) d[q] = v[q] != NONE ? __ldcg(a.dist + v[q]) : 0u;
+#pragma unroll
+        for (uint32_t q = 0; q < PE; ++q) {
+            if (v[q] == NONE) continue;
+            if (d[q] >= thr) {
+                atomicMin(&C.fmin, d[q]);
+                stage_far(a, C, S.sf, v[q]);
             } else {
-                atomicAnd(a.farbits + (v >> 5), ~(1u << (v & 31)));
-                if (d >= thr_old && atomicExch(a.stamp + v, round + 1) != round + 1) stage_near(a, C, S.sv, v);
+                atomicAnd(a.farbits + (v[q] >> 5), ~(1u << (v[q] & 31)));
+                if (d[q] >= thr_old && atomicExch(a.stamp + v[q], round + 1) != round + 1)
+                    stage_near(a, C, S.sv, v[q]);
             }
         }
         checkpoint<BS, true>(a, C, S, nxt, r3n, fq, bucket, BS);
