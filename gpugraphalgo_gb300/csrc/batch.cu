@@ -287,11 +287,14 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
                 const uint32_t nr = ld_relaxed_u32(&st->nr[r3]);
                 const uint32_t fc = min(ld_relaxed_u32(&st->fc[fp]), Q.n);
                 const uint32_t fm = ld_relaxed_u32(&st->fmin[fp]);
+                const uint32_t fpk = ld_relaxed_u32(&st->fpeak[par]);
                 old = thr;
                 const bool split = nr == 0 && fc > 0 && !cool;
                 if (split) {
                     const uint32_t lowest = max(thr, fm);
                     thr = lowest > NONE - Q.delta ? NONE : lowest + Q.delta;
+                    /* a small and shrinking pile: no more buckets */
+                    if (fc <= Q.tail_at && fc < fpk) thr = NONE;
                     fcount = fc;
                 }
                 tgt = split ? fp ^ 1u : fp;
@@ -300,6 +303,7 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
                     st->thr[par ^ 1] = thr;
                     st->fp[par ^ 1] = tgt;
                     st->cool[par ^ 1] = split ? 1u : 0u;
+                    st->fpeak[par ^ 1] = max(fpk, fc);
                     st->nr[(round + 2) % 3] = 0; /* read two rounds ago, counted from next round */
                     if (cool) {                  /* the pile split last round is free again */
                         st->fc[fp ^ 1] = 0;
@@ -497,6 +501,7 @@ __global__ void k_mq_inject(MqArgs a, MqQuery *qt, const uint32_t *list, uint32_
             st->thr[par] = Q->algo == GGA_SSSP && Q->delta ? Q->delta : NONE;
             st->fp[par] = 0;
             st->cool[par] = 0;
+            st->fpeak[0] = st->fpeak[1] = 0;
             st->nr[round % 3] = d ? 1u : 0u;
         }
         if (!d) continue;
@@ -829,6 +834,7 @@ gga_status gga_multi_solve(gga_ctx *c, uint32_t nq, const gga_query *queries, gg
         r.algo = q.algo;
         r.src = q.src;
         r.delta = q.algo == GGA_SSSP ? ctx_default_params(q.graph).sssp_delta : 0;
+        r.tail_at = r.delta ? d->n / 4 : 0;
         mq_state_layout(&r, b->pool + at);
         at += mq_state_words(d->n, q.algo);
         slots[i] = i;

@@ -22,7 +22,11 @@ struct MqQuery {
     uint32_t src;
     uint32_t start_round; /* round in which the source is expanded */
     uint32_t delta;       /* SSSP bucket width (0: Bellman-Ford order) */
-    uint32_t pad[2];
+    /* SSSP: once the query's near queue drains with at most this many far-pile
+     * entries, below the largest pile it has had, its buckets end and the
+     * rest runs label-correcting (threshold infinity); 0 = never */
+    uint32_t tail_at;
+    uint32_t pad;
 };
 
 /* Per-query counters and bucket state of the batch kernel.  Counters are
@@ -35,7 +39,7 @@ struct MqQstate {
     uint32_t thr[2];  /* near threshold */
     uint32_t fp[2];   /* pile that far pushes go to */
     uint32_t cool[2]; /* 1: split a pile in the previous round */
-    uint32_t pad;
+    uint32_t fpeak[2]; /* largest far pile seen */
 };
 
 /* Control block of the batch kernel; persists across superstep launches

@@ -2,7 +2,9 @@
  * new queries injected before each (0 = all at once), finished queries
  * detected by their queue entries and far-pile items (k_mq_count).
  * Queries: the first 16 sources of srcs.bin, algorithm from algos.bin, SSSP
- * bucket width `delta` (0 = Bellman-Ford order).  args: dir NB per stagger delta */
+ * bucket width `delta` (0 = Bellman-Ford order).  args: dir NB per stagger delta [tail]
+ * (tail: a query's buckets end once its pile is at most this size and
+ * shrinking; 0 never) */
 #include "kernel_mq.inc"
 int NB;
 void launch(MqArgs a) {
@@ -16,6 +18,7 @@ int main(int argc, char **argv) {
     std::string d = argv[1];
     NB = atoi(argv[2]);
     const uint32_t per = atoi(argv[3]), stagger = atoi(argv[4]), delta = atoi(argv[5]);
+    const uint32_t tail = argc > 6 ? atoi(argv[6]) : 0;
     auto off = rd(d + "/off.bin"), col = rd(d + "/col.bin"), wt = rd(d + "/wt.bin"), srcs = rd(d + "/srcs.bin"),
          algos = rd(d + "/algos.bin"), want = rd(d + "/want_mix.bin");
     const uint32_t n = off.size() - 1, m = col.size(), nq = algos.size();
@@ -48,6 +51,7 @@ int main(int argc, char **argv) {
             memset(&Q, 0, sizeof Q);
             Q.off = off.data(); Q.col = col.data(); Q.wt = wt.data(); Q.n = n; Q.m = m;
             Q.algo = algos[t]; Q.src = srcs[t]; Q.delta = Q.algo == GGA_SSSP ? delta : 0;
+            Q.tail_at = Q.delta ? tail : 0;
             Q.dist = dist[t].data(); Q.aux = aux[t].data();
             Q.fbits = fb[t].data(); Q.pile0 = p0[t].data(); Q.pile1 = p1[t].data();
             std::fill(dist[t].begin(), dist[t].end(), 1000000000u);

@@ -111,14 +111,17 @@ def test_msbfs_kernel_text(emu, case):
     _run(emu, "msbfs", *case)
 
 
-# graph, blocks, rounds per launch, queries admitted per launch, SSSP delta
+# graph, blocks, rounds per launch, queries admitted per launch, SSSP delta, pile size that ends a
+# query's buckets
 MQ = [
-    ("r10", 4, 1000000, 0, 0),
-    ("r10", 4, 1000000, 0, 33),
-    ("grid", 4, 1000000, 0, 100),
-    ("r10", 3, 2, 3, 16),
-    ("grid", 4, 5, 1, 300),
-    ("grid", 3, 3, 2, 1),
+    ("r10", 4, 1000000, 0, 0, 0),
+    ("r10", 4, 1000000, 0, 33, 0),
+    ("grid", 4, 1000000, 0, 100, 0),
+    ("r10", 3, 2, 3, 16, 0),
+    ("grid", 4, 5, 1, 300, 0),
+    ("grid", 3, 3, 2, 1, 0),
+    ("r10", 4, 1000000, 0, 16, 256),
+    ("grid", 3, 3, 2, 50, 120),
 ]
 
 
