@@ -263,8 +263,9 @@ def _timed(fn, reps):
 def batch_section(gga, ctx):
     """Batched queries in one launch against the same queries one at a time.
 
-    Both sides copy every distance vector to host memory (the user-facing
-    call); kernel-only rates come from the library's CUDA events."""
+    Both sides copy every distance vector to page-locked host memory (the
+    user-facing call); kernel-only rates come from the library's CUDA
+    events."""
     res = {}
     g = gga.Graph.rmat(20, 16, 0.57, 0.19, 0.19, seed=4, wmin=1, wmax=255)
     g.cudaCopy(ctx)
@@ -273,12 +274,21 @@ def batch_section(gga, ctx):
     s64 = [int(x) for x in rng.choice(cand, 64, replace=False)]
     s32 = s64[:32]
 
-    def singles(qs):
-        outs, kms = [], 0.0
+    # every output (batched and one-at-a-time) lands in page-locked host
+    # rows allocated here, outside the timed calls
+    def rows(sizes):
+        block = gga.pinned_empty(int(sum(sizes)))
+        out, at = [], 0
+        for n in sizes:
+            out.append(block[at:at + n])
+            at += n
+        return out
+
+    def singles(qs, outs):
+        kms = 0.0
         t0 = time.perf_counter()
-        for gg, algo, s in qs:
-            o, st = ctx.solve(gg, algo, s, stats=True)
-            outs.append(o)
+        for (gg, algo, s), o in zip(qs, outs):
+            _, st = ctx.solve(gg, algo, s, out=o, stats=True)
             kms += st["kernel_ms"]
         return outs, time.perf_counter() - t0, kms
 
@@ -291,14 +301,16 @@ def batch_section(gga, ctx):
                      "batch_ms": bwall * 1e3, "gteps_kernel": er / (bst["kernel_ms"] * 1e-3) / 1e9 if bst["kernel_ms"] else None,
                      "rounds": bst["iterations"], "edges_relaxed": bst["edges_relaxed"], "edges_reached": er}
 
-    ctx.msbfs(g, s64)
-    (bo, bst), bw = _timed(lambda: ctx.msbfs(g, s64, stats=True), 3)
-    so, sw, sk = singles([(g, "bfs", s) for s in s64])
+    b64, o64 = gga.pinned_empty((64, g.n)), rows([g.n] * 64)
+    ctx.msbfs(g, s64, out=b64)
+    (bo, bst), bw = _timed(lambda: ctx.msbfs(g, s64, stats=True, out=b64), 3)
+    so, sw, sk = singles([(g, "bfs", s) for s in s64], o64)
     record("msbfs64_rmat20", 64, list(bo), bst, bw, so, sw, sk, bst["edges_reached"])
 
-    ctx.sssp_batch(g, s32)
-    (bo, bst), bw = _timed(lambda: ctx.sssp_batch(g, s32, stats=True), 3)
-    so, sw, sk = singles([(g, "sssp", s) for s in s32])
+    b32 = b64[:32]
+    ctx.sssp_batch(g, s32, out=b32)
+    (bo, bst), bw = _timed(lambda: ctx.sssp_batch(g, s32, stats=True, out=b32), 3)
+    so, sw, sk = singles([(g, "sssp", s) for s in s32], o64[:32])
     record("sssp32_rmat20", 32, list(bo), bst, bw, so, sw, sk, bst["edges_reached"])
 
     gs = [gga.Graph.rmat(sc, 16, 0.57, 0.19, 0.19, seed=10 + i, wmin=1, wmax=255) for i, sc in enumerate(range(12, 21))]
@@ -310,9 +322,10 @@ def batch_section(gga, ctx):
         r = np.random.default_rng(100 + j)
         for s in r.choice(np.nonzero(gg.degrees() > 0)[0], 8, replace=False):
             qs += [(gg, "bfs", int(s)), (gg, "sssp", int(s))]
-    ctx.multi_solve(qs)
-    (bo, bst), bw = _timed(lambda: ctx.multi_solve(qs, stats=True), 3)
-    so, sw, sk = singles(qs)
+    mb, mo = rows([gg.n for gg, _, _ in qs]), rows([gg.n for gg, _, _ in qs])
+    ctx.multi_solve(qs, outs=mb)
+    (bo, bst), bw = _timed(lambda: ctx.multi_solve(qs, stats=True, outs=mb), 3)
+    so, sw, sk = singles(qs, mo)
     record("mixed16x8_bfs+sssp", len(qs), bo, bst, bw, so, sw, sk, bst["edges_reached"])
     res["mixed16x8_bfs+sssp"]["graphs"] = "R-MAT 12..20 ef16 seeds 10-18, grids 256..2048 seeds 19-25"
     return res

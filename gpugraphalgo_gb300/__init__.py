@@ -60,6 +60,11 @@ def _ptr(a: np.ndarray):
     return C.c_void_p(a.ctypes.data)
 
 
+def _out_ptr(out):
+    """Address of an output buffer: a numpy array or an object with data_ptr()."""
+    return C.c_void_p(out.data_ptr()) if hasattr(out, "data_ptr") else _ptr(out)
+
+
 class _HostBlock:
     """Page-locked host memory from gga_host_alloc, freed with its last array."""
 
@@ -400,29 +405,39 @@ class Context:
                             "edges": r.edges, "far_items": r.far_items, "us": r.ns / 1e3} for r in rounds[: nr.value]],
                 "cta_kcycles": cta[: nb.value]}
 
-    def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False):
+    def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False, out=None):
+        """Up to 64 BFS sources in one bit-packed launch; out: optional
+        (len(srcs), n) uint32 array (pinned_empty for the fastest copy) or an
+        object with ``data_ptr()``."""
         s = np.ascontiguousarray(srcs, dtype=np.uint32)
-        out = np.empty((len(s), graph.n), np.uint32)
+        if out is None:
+            out = np.empty((len(s), graph.n), np.uint32)
         st = N.Stats()
-        _check(N.load().gga_msbfs(self._h, graph.handle, len(s), _ptr(s), _ptr(out), C.byref(st)), "msbfs")
+        _check(N.load().gga_msbfs(self._h, graph.handle, len(s), _ptr(s), _out_ptr(out), C.byref(st)), "msbfs")
         return (out, st.as_dict()) if stats else out
 
-    def sssp_batch(self, graph: Graph, srcs: Sequence[int], stats: bool = False):
+    def sssp_batch(self, graph: Graph, srcs: Sequence[int], stats: bool = False, out=None):
+        """Up to 32 SSSP sources in one launch; out as for msbfs."""
         s = np.ascontiguousarray(srcs, dtype=np.uint32)
-        out = np.empty((len(s), graph.n), np.uint32)
+        if out is None:
+            out = np.empty((len(s), graph.n), np.uint32)
         st = N.Stats()
-        _check(N.load().gga_sssp_batch(self._h, graph.handle, len(s), _ptr(s), _ptr(out), C.byref(st)), "sssp_batch")
+        _check(N.load().gga_sssp_batch(self._h, graph.handle, len(s), _ptr(s), _out_ptr(out), C.byref(st)),
+               "sssp_batch")
         return (out, st.as_dict()) if stats else out
 
-    def multi_solve(self, queries, stats: bool = False):
-        """queries: list of (graph, algo, src) -> list of distance arrays."""
-        outs = [np.empty(g.n, np.uint32) for g, _, _ in queries]
+    def multi_solve(self, queries, stats: bool = False, outs=None):
+        """queries: list of (graph, algo, src) -> list of distance arrays.
+        outs: optional list of one output array (or ``data_ptr()`` object)
+        per query."""
+        if outs is None:
+            outs = [np.empty(g.n, np.uint32) for g, _, _ in queries]
         arr = (N.Query * len(queries))()
         for i, (g, a, s) in enumerate(queries):
             arr[i].graph = g.handle.value
             arr[i].algo = _algo(a)
             arr[i].src = s
-            arr[i].dist_out = outs[i].ctypes.data
+            arr[i].dist_out = _out_ptr(outs[i]).value
         st = N.Stats()
         _check(N.load().gga_multi_solve(self._h, len(queries), arr, C.byref(st)), "multi_solve")
         return (outs, st.as_dict()) if stats else outs
