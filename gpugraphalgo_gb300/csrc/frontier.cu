@@ -35,6 +35,8 @@
  */
 #include <stdio.h>
 #include <string.h>
+#include <mutex>
+
 
 #include "frontier.cuh"
 
@@ -987,17 +989,30 @@ size_t dyn_smem(uint32_t unit, uint32_t scap) {
     return ((size_t)(unit + 1) * (SSSP ? 4 : 2) + (size_t)scap * (SSSP ? 2 : 1)) * sizeof(uint32_t);
 }
 
+/* Resident CTAs per SM for this instance and shared-memory size; the first
+ * call per size also raises the instance's dynamic shared-memory limit, so
+ * later launches make no driver calls before the launch itself (the time
+ * between the start event and the kernel is host time). */
 template <int BS, bool SSSP>
 int occupancy(size_t smem) {
-    static int occ[8];
-    static size_t occ_smem[8];
+    constexpr int SLOTS = 16;
+    static int occ[SLOTS], occ_dev[SLOTS];
+    static size_t occ_smem[SLOTS];
     static int used = 0;
+    static std::mutex mu;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> lk(mu);
     for (int i = 0; i < used; ++i)
-        if (occ_smem[i] == smem) return occ[i];
+        if (occ_smem[i] == smem && occ_dev[i] == dev) return occ[i];
+    if (cudaFuncSetAttribute(k_frontier<BS, SSSP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return 0;
     int v = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_frontier<BS, SSSP>, BS, smem) != cudaSuccess) v = 0;
-    if (used < 8) {
+    if (used < SLOTS && v > 0) { /* a full cache only costs the calls above again */
         occ[used] = v;
+        occ_dev[used] = dev;
         occ_smem[used] = smem;
         ++used;
     }
@@ -1007,7 +1022,6 @@ int occupancy(size_t smem) {
 template <int BS, bool SSSP>
 gga_status launch(Args &a, const gga_params &p, int sms, cudaStream_t st) {
     const size_t smem = dyn_smem<BS, SSSP>(a.unit, a.scap);
-    GGA_CK(cudaFuncSetAttribute(k_frontier<BS, SSSP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = occupancy<BS, SSSP>(smem);
     if (occ <= 0) return gga_fail(GGA_ERR_CUDA, "frontier kernel: zero occupancy (unit %u)", a.unit);
     int per_sm = p.blocks_per_sm ? (int)p.blocks_per_sm : occ;
@@ -1196,7 +1210,6 @@ gga_status frontier_verdict(const FrontierCtl &h) {
  * make that first call before any stream capture begins.
  * ------------------------------------------------------------------------ */
 
-#include <mutex>
 
 #define NOALLOC_MAX_NODES (1u << 18) /* 262,144 vertices */
 #define NOALLOC_MAX_EDGES (1u << 23) /* 8,388,608 directed edges */
