@@ -578,6 +578,9 @@ def run_gga(args, dist: Dist):
         g.cudaCopy(ctx)
 
     if not args.no_batch and dist.rank == 0:
+        # both sides of the batched comparisons use each graph's own defaults,
+        # not the parameters tuned for the R-MAT-22 step above
+        ctx.reset_params()
         try:
             out["batched"] = batch_section(gga, ctx)
         except Exception as e:  # reported, not fatal

@@ -833,7 +833,7 @@ gga_status gga_multi_solve(gga_ctx *c, uint32_t nq, const gga_query *queries, gg
         r.m = d->m;
         r.algo = q.algo;
         r.src = q.src;
-        r.delta = q.algo == GGA_SSSP ? ctx_default_params(q.graph).sssp_delta : 0;
+        r.delta = q.algo == GGA_SSSP ? ctx_profile_delta(q.graph) : 0;
         r.tail_at = r.delta ? d->n / 4 : 0;
         mq_state_layout(&r, b->pool + at);
         at += mq_state_words(d->n, q.algo);

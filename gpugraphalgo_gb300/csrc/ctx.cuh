@@ -50,6 +50,9 @@ struct gga_ctx {
 
 gga_status ctx_activate(gga_ctx *c);
 gga_params ctx_default_params(const gga_graph *g);
+/* SSSP bucket width from g's degree profile (never 0): the batch engines'
+ * width, whose rounds are shared by many queries. */
+uint32_t ctx_profile_delta(const gga_graph *g);
 gga_status ctx_validate_solve(const gga_graph *g, gga_algo algo, uint32_t src);
 gga_status ctx_finish_output(gga_ctx *c, const DevGraph *d, const uint32_t *dev_out, uint32_t *dist_out,
                              gga_stats *stats);

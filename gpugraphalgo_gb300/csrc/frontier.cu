@@ -995,19 +995,23 @@ size_t dyn_smem(uint32_t unit, uint32_t scap) {
  * between the start event and the kernel is host time). */
 template <int BS, bool SSSP>
 int occupancy(size_t smem) {
-    constexpr int SLOTS = 16;
+    constexpr int SLOTS = 16, DEVS = 64;
     static int occ[SLOTS], occ_dev[SLOTS];
     static size_t occ_smem[SLOTS];
+    static size_t attr[DEVS]; /* the limit set on each device (it only grows) */
     static int used = 0;
     static std::mutex mu;
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= DEVS) return 0;
     std::lock_guard<std::mutex> lk(mu);
+    if (smem > attr[dev]) {
+        if (cudaFuncSetAttribute(k_frontier<BS, SSSP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return 0;
+        attr[dev] = smem;
+    }
     for (int i = 0; i < used; ++i)
         if (occ_smem[i] == smem && occ_dev[i] == dev) return occ[i];
-    if (cudaFuncSetAttribute(k_frontier<BS, SSSP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-        return 0;
     int v = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_frontier<BS, SSSP>, BS, smem) != cudaSuccess) v = 0;
     if (used < SLOTS && v > 0) { /* a full cache only costs the calls above again */

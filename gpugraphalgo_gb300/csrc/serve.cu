@@ -290,7 +290,7 @@ gga_status gga_server_create(gga_ctx *c, uint32_t ngraphs, gga_graph *const *gra
     for (uint32_t i = 0; i < ngraphs; ++i) {
         sv->graphs.push_back(graphs[i]);
         sv->dgraphs.push_back(dev_graph_of(graphs[i]));
-        sv->delta.push_back(ctx_default_params(graphs[i]).sssp_delta);
+        sv->delta.push_back(ctx_profile_delta(graphs[i]));
         max_n = std::max<uint64_t>(max_n, graphs[i]->n);
         max_m = std::max<uint64_t>(max_m, graphs[i]->m);
     }
