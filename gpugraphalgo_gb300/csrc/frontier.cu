@@ -47,6 +47,7 @@ constexpr uint32_t MIN_UNIT = 512;  /* smallest edges-per-unit the buffers are s
 constexpr uint32_t MAX_UNIT = 4096; /* largest edges-per-unit (shared-memory bound) */
 constexpr uint32_t STAGE_BATCH = 4; /* edges per thread in flight between staging checkpoints */
 constexpr uint32_t BU_WORDS = 4;    /* bottom-up BFS: visited-bitmap words per warp step */
+constexpr uint32_t BU_NBRS = 4;     /* bottom-up BFS: neighbours a lane checks per vertex per step */
 
 struct Args {
     const uint32_t *off, *col, *wt, *cc;
@@ -331,19 +332,21 @@ __device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, u
                 any |= act[k];
             }
             if (!any) break;
-            uint32_t u[NW][4];
+            constexpr uint32_t NB = BU_NBRS;
+            uint32_t u[NW][NB];
 #pragma unroll
             for (uint32_t k = 0; k < NW; ++k)
 #pragma unroll
-                for (uint32_t q = 0; q < 4; ++q) u[k][q] = act[k] && cur[k] + q < e1[k] ? __ldg(a.col + cur[k] + q) : NONE;
+                for (uint32_t q = 0; q < NB; ++q)
+                    u[k][q] = act[k] && cur[k] + q < e1[k] ? __ldg(a.col + cur[k] + q) : NONE;
 #pragma unroll
             for (uint32_t k = 0; k < NW; ++k) {
 #pragma unroll
-                for (uint32_t q = 0; q < 4; ++q)
+                for (uint32_t q = 0; q < NB; ++q)
                     if (u[k][q] != NONE && __ldcg(a.dist + u[k][q]) == round) found[k] = true;
                 if (act[k]) {
-                    relaxed += min(4u, e1[k] - cur[k]);
-                    cur[k] += 4;
+                    relaxed += min(NB, e1[k] - cur[k]);
+                    cur[k] += NB;
                 }
             }
         }
