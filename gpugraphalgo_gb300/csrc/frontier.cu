@@ -463,11 +463,13 @@ __device__ __forceinline__ void pull_scan(const Args &a, uint32_t thr, uint32_t 
  * and gives consecutive edges to consecutive threads.  Units hold equal edge
  * counts, so the static deal balances like a ticket counter would, without
  * an atomic on the path, and the next unit's bounds load while the current
- * one is expanded.  Each thread handles PB edges at a time in three passes
- * (edge loads, then distance/bitmap probes, then updates), so PB independent
- * memory chains are in flight per thread instead of one.  Improvements at or
- * above thr go to the far pile (thr = 0 sends all of them there).
- * Block-uniform: every thread runs the same units and checkpoints.
+ * one is expanded; a round with fewer units than CTAs splits each unit into
+ * parts.  Each thread handles PB edges at a time in three passes (edge
+ * loads, then distance/bitmap probes, then updates), so PB independent
+ * memory chains are in flight per thread instead of one.  SSSP improvements
+ * below thr join the next round's near queue, the rest the far pile fp.
+ * Block-uniform: every thread runs the same units and checkpoints, and the
+ * last barrier follows the final stage-count read.
  *
  * PULL (SSSP): the entries are unsettled vertices and their heavy edges;
  * an edge whose other end u is settled (d(u) < settled) offers d(u) + w to
