@@ -221,7 +221,9 @@ typedef struct gga_params {
     uint32_t unit_iters;     /* edges per work unit = block_threads x this (2..16; 0 = 4096 / block_threads for
                               * BFS, 4 for SSSP) */
     uint32_t sssp_delta;     /* near-far bucket width (0 = plain improved-vertex frontier) */
-    uint32_t use_split;      /* expand over the node-split graph when one exists */
+    uint32_t use_split;      /* 1: the frontier engine expands over the node-split graph when one exists;
+                              * 0 (default): over the unsplit CSR, which its edge-balanced units need
+                              * no split for (same distances, faster) */
     uint32_t blocks_per_sm;  /* persistent grid = SMs x this (0 = occupancy maximum) */
     /* CDP variants: heavy-vertex threshold as bfs_sssp.cu:224-236 derives it
      * (level > 0: ceil(maxdeg/level); level < 0: histogram rule with buckets) */

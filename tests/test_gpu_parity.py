@@ -77,6 +77,12 @@ def test_split_graph_all_variants_match_reference(golden, ctx):
                 for v in ("frontier", "topo_atomic", "topo_plain"):
                     got = ctx.solve(g, algo, int(src), v)
                     assert digest(got) == drec["sha256"], (name, key, dkey, v)
+                try:  # the frontier engine over the split view too
+                    ctx.set_params(use_split=1)
+                    got = ctx.solve(g, algo, int(src), "frontier")
+                    assert digest(got) == drec["sha256"], (name, key, dkey, "frontier/split view")
+                finally:
+                    ctx.reset_params()
         g.NodeSplit(ctx, 0)
 
 
@@ -128,6 +134,11 @@ def test_random_rmat_against_oracle(ctx, seed):
         want = _oracle_dist(g, algo, srcs[0])
         for v in ("frontier", "topo_plain", "cdp_atomic"):
             np.testing.assert_array_equal(ctx.solve(g, algo, srcs[0], v), want)
+        try:
+            ctx.set_params(use_split=1)
+            np.testing.assert_array_equal(ctx.solve(g, algo, srcs[0], "frontier"), want)
+        finally:
+            ctx.reset_params()
 
 
 def test_grid_deep_against_oracle(ctx):
@@ -195,6 +206,11 @@ def test_source_is_split_parent(golden, ctx):
         if src == "0":
             for v in ("frontier", "topo_atomic", "topo_plain"):
                 assert digest(ctx.solve(g, algo, 0, v)) == rec["sha256"]
+            try:  # the split source as the frontier engine's split view sees it
+                ctx.set_params(use_split=1)
+                assert digest(ctx.solve(g, algo, 0, "frontier")) == rec["sha256"]
+            finally:
+                ctx.reset_params()
 
 
 def test_cdp_modes_and_fallback(ctx):
@@ -420,10 +436,13 @@ def test_solve_many_matches_single_solves(ctx, algo):
     gs.NodeSplit(ctx, 4)
     try:
         srcs = [0, 3, 100, 7]
-        got = ctx.solve_many(gs, algo, srcs)
-        for i, s in enumerate(srcs):
-            np.testing.assert_array_equal(got[i], _oracle_dist(gs, algo, s))
+        for us in (0, 1):
+            ctx.set_params(use_split=us)
+            got = ctx.solve_many(gs, algo, srcs)
+            for i, s in enumerate(srcs):
+                np.testing.assert_array_equal(got[i], _oracle_dist(gs, algo, s), err_msg=f"use_split={us}")
     finally:
+        ctx.reset_params()
         gs.NodeSplit(ctx, 0)
 
 
