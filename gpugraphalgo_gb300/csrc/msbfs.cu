@@ -23,7 +23,18 @@
  *
  * One edge read serves every source whose frontier contains u, so a vertex
  * reached by all 64 sources in the same level is expanded once instead of 64
- * times.  Levels equal those of 64 single-source BFS runs (the reference's
+ * times.
+ *
+ * On symmetric graphs a level whose frontier edges exceed m / 4 expands
+ * bottom-up instead (the multi-source form of Beamer's rule; measured on
+ * GB300 with 64 sources, R-MAT 22: 7.98 -> 4.92 ms, R-MAT 20: 1.65 -> 1.52
+ * ms, while m / 16 was several times slower, since a vertex stops only once
+ * it has every source's bit): every vertex
+ * not yet seen by all sources ORs its neighbours' `seen` masks until it has
+ * every source, and the bits it lacked are exactly the sources reaching it
+ * at level L + 1 (a neighbour seen by source s at level <= L means level
+ * L + 1, as the vertex was not reached by level L).  `seen` is only written
+ * in settle, so the masks read are those of level L.  Levels equal those of 64 single-source BFS runs (the reference's
  * BFS levels, K/graph.h:115-149 serial and K/cudaKernels.h:285-344 device),
  * on the unsplit graph: splitting a vertex does not change any level.
  */
@@ -41,6 +52,7 @@ constexpr uint32_t MB_UNIT = MB_BS * MB_ITERS;
 constexpr uint32_t MB_BATCH = 4;
 constexpr uint32_t MB_SCAP = MB_BS * (MB_BATCH + 1);
 constexpr unsigned FULL = 0xffffffffu;
+constexpr uint32_t NONE = 0xffffffffu;
 
 struct MsCtl {
     GridBarrier bar;
@@ -65,6 +77,8 @@ struct MsArgs {
     MsCtl *ctl;
     uint32_t ucap, nblocks, max_levels;
     unsigned long long timeout_ns;
+    uint32_t bu;              /* symmetric graph: bottom-up levels allowed */
+    unsigned long long all;   /* the mask of every source */
 };
 
 struct MsCtrl {
@@ -89,6 +103,81 @@ __device__ __forceinline__ void ms_checkpoint(const MsArgs &a, MsCtrl &C, uint32
     __syncthreads();
     if (threadIdx.x == 0) C.nn = 0;
     __syncthreads();
+}
+
+/* One bottom-up expansion of level L: a warp takes 2 x 32 consecutive
+ * vertices per step (lane i vertices 64w + i and 64w + 32 + i), each lane
+ * ORs its vertices' neighbours' seen masks, 4 per vertex per step, until the
+ * vertex has every source; vertices that gained bits get them in nxt (this
+ * lane is their only writer this level) and join the next candidate list
+ * through one warp-aggregated atomicAdd.  Trip counts are warp-uniform; the
+ * per-lane scans reconverge before the ballots. */
+__device__ __forceinline__ void ms_bottom_up(const MsArgs &a, uint32_t np, unsigned long long &relaxed) {
+    constexpr uint32_t NV = 2, NB = 4;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t gw = ((uint64_t)blockIdx.x * MB_BS + threadIdx.x) >> 5, nw = ((uint64_t)gridDim.x * MB_BS) >> 5;
+    const uint64_t steps = ((uint64_t)a.n + 32 * NV - 1) / (32 * NV);
+    for (uint64_t w = gw; w < steps; w += nw) {
+        uint32_t v[NV], cur[NV], e1[NV];
+        unsigned long long sv[NV], acc[NV];
+        bool open[NV];
+#pragma unroll
+        for (uint32_t k = 0; k < NV; ++k) {
+            const uint64_t vk = w * 32 * NV + 32 * k + lane;
+            v[k] = (uint32_t)vk;
+            sv[k] = vk < a.n ? __ldcg(a.seen + vk) : a.all;
+            acc[k] = 0;
+            open[k] = sv[k] != a.all;
+            cur[k] = e1[k] = 0;
+            if (open[k]) {
+                cur[k] = __ldg(a.off + vk);
+                e1[k] = __ldg(a.off + vk + 1);
+            }
+        }
+        for (;;) {
+            bool act[NV], any = false;
+#pragma unroll
+            for (uint32_t k = 0; k < NV; ++k) {
+                act[k] = open[k] && cur[k] < e1[k] && (acc[k] | sv[k]) != a.all;
+                any |= act[k];
+            }
+            if (!any) break;
+            uint32_t u[NV][NB];
+#pragma unroll
+            for (uint32_t k = 0; k < NV; ++k)
+#pragma unroll
+                for (uint32_t q = 0; q < NB; ++q) u[k][q] = act[k] && cur[k] + q < e1[k] ? __ldg(a.col + cur[k] + q) : NONE;
+#pragma unroll
+            for (uint32_t k = 0; k < NV; ++k) {
+#pragma unroll
+                for (uint32_t q = 0; q < NB; ++q)
+                    if (u[k][q] != NONE) acc[k] |= __ldcg(a.seen + u[k][q]);
+                if (act[k]) {
+                    relaxed += min(NB, e1[k] - cur[k]);
+                    cur[k] += NB;
+                }
+            }
+        }
+        uint32_t fm[NV], cnt = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < NV; ++k) {
+            const bool found = open[k] && (acc[k] & ~sv[k]) != 0;
+            if (found) a.nxt[v[k]] = acc[k] & ~sv[k];
+            fm[k] = __ballot_sync(FULL, found);
+            cnt += (uint32_t)__popc(fm[k]);
+        }
+        if (cnt == 0) continue; /* warp-uniform */
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&a.ctl->cand[np], cnt);
+        base = __shfl_sync(FULL, base, 0);
+#pragma unroll
+        for (uint32_t k = 0, before = 0; k < NV; before += (uint32_t)__popc(fm[k]), ++k)
+            if ((fm[k] >> lane) & 1u) {
+                const uint32_t idx = base + before + (uint32_t)__popc(fm[k] & lanemask_lt());
+                if (idx < a.n) a.cand[idx] = v[k];
+                else ms_err(a.ctl, GGA_DEV_OVERFLOW);
+            }
+    }
 }
 
 __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
@@ -181,6 +270,12 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
             ctl->cand[p] = 0;  /* read at the start of settle(L), appended in expand(L+1) */
             ctl->xctr[np] = 0; /* read in expand(L-1), appended in settle(L+1) */
         }
+        /* direction of this level, from counters every block read alike */
+        if (a.bu && (uint64_t)total * 4 > a.m) {
+            ms_bottom_up(a, np, relaxed);
+            if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+            continue;
+        }
         for (;;) {
             if (tid == 0) {
                 const uint32_t k = atomicAdd(&ctl->work[p], 1u);
@@ -249,7 +344,10 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
         ms_checkpoint(a, C, sc, np, 1);
         if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
     }
-    if (tid == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);
+    /* every thread of every block leaves the level loop at the same point;
+     * top-down counts sit in thread 0, bottom-up counts in every lane */
+    for (int d = 16; d > 0; d >>= 1) relaxed += __shfl_down_sync(FULL, relaxed, d);
+    if (lane == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);
     if (blockIdx.x == 0 && tid == 0) ctl->levels = L;
 }
 
@@ -419,6 +517,8 @@ gga_status gga_msbfs(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *sr
     if ((s = ctx_activate(c))) return s;
     if ((s = dev_graph_ensure(g, c->device, c->st))) return s;
     const DevGraph *d = dev_graph_of(g);
+    /* bottom-up levels need every edge's reverse (checked once per graph) */
+    if (d->symmetric == 0 && (s = dev_graph_check_symmetric(g, c->dflag + 40, c->hflag + 40, c->st))) return s;
     BatchScratch *b = ctx_batch(c);
     if (!b) return gga_fail(GGA_ERR_NO_MEMORY, "batch scratch");
     if (!b->ms) {
@@ -454,6 +554,8 @@ gga_status gga_msbfs(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *sr
     a.nblocks = (uint32_t)m->nblocks;
     a.max_levels = d->n + 1;
     a.timeout_ns = 4000000000ull;
+    a.bu = d->symmetric > 0 ? 1u : 0u;
+    a.all = nsrc == 64 ? ~0ull : (1ull << nsrc) - 1;
 
     GGA_CK(cudaMemsetAsync(m->ctl, 0, sizeof(MsCtl), c->st));
     GGA_CK(cudaMemsetAsync(m->seen, 0, (size_t)d->n * 8, c->st));

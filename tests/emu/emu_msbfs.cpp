@@ -1,4 +1,5 @@
-/* Runs k_msbfs for the first nsrc sources.  args: dir NB nsrc */
+/* Runs k_msbfs for the first nsrc sources.  args: dir NB nsrc [bu]
+ * (bu: bottom-up levels allowed; the test graphs are symmetric) */
 #include "kernel_msbfs.inc"
 int main(int argc, char **argv) {
     if (argc < 4) return 3;
@@ -17,6 +18,8 @@ int main(int argc, char **argv) {
     a.cand = cand.data(); a.xv = xv.data(); a.xo = xo.data(); a.xb = xb.data(); a.xf = xf.data(); a.uf = uf.data();
     a.dist = dist.data(); a.ns = nsrc; a.ctl = &ctl; a.ucap = ucap; a.nblocks = NB; a.max_levels = n + 1;
     a.timeout_ns = 60000000000ull;
+    a.bu = argc > 4 ? atoi(argv[4]) : 0;
+    a.all = nsrc == 64 ? ~0ull : (1ull << nsrc) - 1;
     for (uint32_t s = 0; s < nsrc; ++s) { /* k_ms_sources */
         const uint32_t v = srcs[s];
         if (atomicOr(a.nxt + v, 1ull << s) == 0) a.cand[ctl.cand[0]++] = v;
@@ -27,6 +30,7 @@ int main(int argc, char **argv) {
     size_t bad = 0;
     for (uint32_t s = 0; s < nsrc; ++s)
         for (uint32_t v = 0; v < n; ++v) bad += dist[(size_t)v * nsrc + s] != want[(size_t)s * n + v];
-    printf("msbfs NB=%d nsrc=%u err=%u levels=%u bad=%zu relaxed=%llu\n", NB, nsrc, ctl.err, ctl.levels, bad, ctl.edges_relaxed);
+    printf("msbfs NB=%d nsrc=%u bu=%u err=%u levels=%u bad=%zu relaxed=%llu\n", NB, nsrc, a.bu, ctl.err, ctl.levels, bad,
+           ctl.edges_relaxed);
     return bad != 0 || ctl.err;
 }

@@ -106,7 +106,9 @@ def test_sssp32_kernel_text(emu, case):
     _run(emu, "sssp32", *case)
 
 
-@pytest.mark.parametrize("case", [("r10", 4, 64), ("grid", 2, 7)], ids=lambda c: "-".join(map(str, c)))
+# graph, blocks, sources, bottom-up levels allowed
+@pytest.mark.parametrize("case", [("r10", 4, 64, 0), ("grid", 2, 7, 0), ("r10", 4, 64, 1), ("r10", 3, 5, 1),
+                                  ("grid", 4, 33, 1)], ids=lambda c: "-".join(map(str, c)))
 def test_msbfs_kernel_text(emu, case):
     _run(emu, "msbfs", *case)
 
