@@ -240,7 +240,7 @@ typedef struct gga_params {
      * rule, on symmetric graphs walked unsplit; 1 = top-down only.  Levels
      * are the same either way. */
     uint32_t bfs_direction;
-    uint32_t bfs_alpha; /* go bottom-up when frontier edges x alpha > unexplored edges (0 = 15) */
+    uint32_t bfs_alpha; /* go bottom-up when frontier edges x alpha > unexplored edges (0 = 8) */
     uint32_t bfs_beta;  /* go back top-down when frontier vertices x beta < n (0 = 18) */
     /* SSSP edge classes: 0 = delta-stepping light/heavy split when
      * sssp_delta > 0 on the unsplit graph (rows reordered light-first once
