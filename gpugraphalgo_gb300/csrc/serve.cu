@@ -209,7 +209,7 @@ void server_loop(gga_server *s) {
                 q.algo = rq.algo;
                 q.src = rq.src;
                 q.delta = rq.algo == GGA_SSSP ? s->delta[rq.graph] : 0;
-                q.tail_at = q.delta ? d->n / 4 : 0;
+                q.tail_at = q.delta && (uint64_t)d->m >= 8ull * d->n ? d->n / 4 : 0;
                 mq_state_layout(&q, s->pool + off);
                 hq.push_back(q);
                 hslots.push_back(slot);
