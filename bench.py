@@ -301,17 +301,30 @@ def batch_section(gga, ctx):
                      "batch_ms": bwall * 1e3, "gteps_kernel": er / (bst["kernel_ms"] * 1e-3) / 1e9 if bst["kernel_ms"] else None,
                      "rounds": bst["iterations"], "edges_relaxed": bst["edges_relaxed"], "edges_reached": er}
 
+    def reference_kernel(name, algo, srcs, batch_out, k=3):
+        """The same queries through the reference's own kernel (topology-driven
+        Bellman-Ford with atomicMin, the "na_" build), one launch sequence per
+        query with the result copied to host: a sample of k queries."""
+        t0 = time.perf_counter()
+        outs = [ctx.solve(g, algo, s, "topo_atomic", out=o64[i]) for i, s in enumerate(srcs[:k])]
+        dt = time.perf_counter() - t0
+        res[name]["reference_kernel_one_at_a_time"] = {
+            "qps": k / dt, "sample_queries": k, "batch_speedup": res[name]["batch_qps"] / (k / dt),
+            "identical": bool(all(np.array_equal(a, b) for a, b in zip(outs, batch_out)))}
+
     b64, o64 = gga.pinned_empty((64, g.n)), rows([g.n] * 64)
     ctx.msbfs(g, s64, out=b64)
     (bo, bst), bw = _timed(lambda: ctx.msbfs(g, s64, stats=True, out=b64), 3)
     so, sw, sk = singles([(g, "bfs", s) for s in s64], o64)
     record("msbfs64_rmat20", 64, list(bo), bst, bw, so, sw, sk, bst["edges_reached"])
+    reference_kernel("msbfs64_rmat20", "bfs", s64, bo)
 
     b32 = b64[:32]
     ctx.sssp_batch(g, s32, out=b32)
     (bo, bst), bw = _timed(lambda: ctx.sssp_batch(g, s32, stats=True, out=b32), 3)
     so, sw, sk = singles([(g, "sssp", s) for s in s32], o64[:32])
     record("sssp32_rmat20", 32, list(bo), bst, bw, so, sw, sk, bst["edges_reached"])
+    reference_kernel("sssp32_rmat20", "sssp", s32, bo)
 
     gs = [gga.Graph.rmat(sc, 16, 0.57, 0.19, 0.19, seed=10 + i, wmin=1, wmax=255) for i, sc in enumerate(range(12, 21))]
     gs += [gga.Graph.grid(w, w, 0.05, 0.001, seed=19 + i, wmin=1, wmax=1000)
