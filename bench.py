@@ -379,13 +379,24 @@ def serving_section(gga, ctx, seconds: float, device: int):
         ctx.solve(graphs[gi], al, s, out=ring[k % W][: ns[gi]])
     ctx.synchronize()
     seq_qps = len(seq) / (time.perf_counter() - t0)
+    # the reference's own kernel (topology-driven Bellman-Ford, "na_"), one
+    # query at a time, on the first queries of the same mix (at most ~5 s)
+    t0, nref = time.perf_counter(), 0
+    for gi, al, s in seq[:8]:
+        ctx.solve(graphs[gi], al, s, "topo_atomic", out=ring[nref % W][: ns[gi]])
+        nref += 1
+        if time.perf_counter() - t0 > 5.0:
+            break
+    ctx.synchronize()
+    ref_qps = nref / (time.perf_counter() - t0)
 
     srv = gga.Server(ctx, graphs, mem_cap_bytes=60 << 30, max_slots=256)
     old_switch = sys.getswitchinterval()
     sys.setswitchinterval(0.0002)  # the submitting and the waiting thread share the GIL
     out = {"graphs": "R-MAT 16/18/20/21 ef16 seeds 30-33, grids 512/1024/1536/2048 seeds 34-37 (5% deleted, w 1..1000)",
            "mix": "70% BFS / 30% SSSP, uniform graph and source", "mem_cap_bytes": 60 << 30, "max_slots": 256,
-           "superstep_rounds": 8, "sequential_qps": seq_qps, "rates": []}
+           "superstep_rounds": 8, "sequential_qps": seq_qps,
+           "reference_kernel_sequential": {"qps": ref_qps, "sample_queries": nref}, "rates": []}
     try:
         # exactness: served answers equal single-query answers
         chk = draw(24)
@@ -448,6 +459,7 @@ def serving_section(gga, ctx, seconds: float, device: int):
                                  "throttled_submits": throttled, "window": W})
         out["stats"] = srv.stats()
         out["peak_qps_vs_sequential"] = max(r["achieved_qps"] for r in out["rates"]) / seq_qps
+        out["peak_qps_vs_reference_kernel_sequential"] = max(r["achieved_qps"] for r in out["rates"]) / ref_qps
     finally:
         sys.setswitchinterval(old_switch)
         srv.close()
