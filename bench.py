@@ -241,7 +241,8 @@ def run_reference(args, dist: Dist):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"rmat{args.scale}_ef{args.edge_factor}_seed2_bfs_sssp", "sources": args.sources,
+        "config": {"workload": f"rmat{args.scale}_ef{args.edge_factor}_seed2_{args.sources}src_bfs+sssp",
+                   "sources": args.sources,
                    "implementation": "serial in-order Bellman-Ford sweeps (graph.h:115-184), oracle C port",
                    "parallelism": f"{threads} host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},

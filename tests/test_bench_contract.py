@@ -1,0 +1,56 @@
+"""bench.py's reference arm on the CPU: the one JSON line a harness reads,
+from one process and from two gloo ranks (rank 0 alone runs and prints).
+The arm times the oracle's restatement of the reference's serial
+findSerialBFS / findSerialSSSP (graph.h:115-184) on host threads."""
+from __future__ import annotations
+
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ARGS = ["--impl", "reference", "--scale", "10", "--sources", "4", "--steps", "2", "--warmup", "3"]
+
+
+def _json_lines(out: str):
+    return [json.loads(line) for line in out.splitlines() if line.startswith("{")]
+
+
+def _check_line(d, gpus):
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert d["impl"] == "reference"
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert (d["steps"], d["warmup"], d["n_gpus"]) == (2, 3, gpus)
+    assert d["config"]["workload"] == "rmat10_ef16_seed2_4src_bfs+sssp"
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_prints_one_json_line():
+    r = subprocess.run([sys.executable, "bench.py", *ARGS], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _json_lines(r.stdout)
+    assert len(lines) == 1, r.stdout
+    _check_line(lines[0], 1)
+
+
+def test_reference_arm_two_ranks_rank0_prints():
+    pytest.importorskip("torch.distributed")
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", *ARGS, "--gpus", "2"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _json_lines(r.stdout)
+    assert len(lines) == 1, r.stdout
+    _check_line(lines[0], 2)
