@@ -54,3 +54,37 @@ def test_reference_arm_two_ranks_rank0_prints():
     lines = _json_lines(r.stdout)
     assert len(lines) == 1, r.stdout
     _check_line(lines[0], 2)
+
+
+def _dist_rank(rank, port, q):
+    os.environ.update({"RANK": str(rank), "WORLD_SIZE": "2", "LOCAL_RANK": str(rank), "MASTER_ADDR": "127.0.0.1",
+                       "MASTER_PORT": str(port)})
+    sys.path.insert(0, ROOT)
+    import bench
+
+    d = bench.Dist()
+    try:
+        d.barrier()
+        # each replica's own time and units: the job's time is the slowest
+        # rank's, its units the sum over ranks
+        q.put((rank, d.max(1.5 + rank), d.sum(10.0 * (rank + 1))))
+    finally:
+        d.close()
+
+
+def test_replica_timing_reductions_two_gloo_ranks():
+    mp = pytest.importorskip("torch.multiprocessing")
+    pytest.importorskip("torch.distributed")
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_dist_rank, args=(r, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    for p in ps:
+        p.join(300)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=10) for _ in range(2))
+    assert got == [(0, 2.5, 30.0), (1, 2.5, 30.0)]
