@@ -281,6 +281,22 @@ def writeResult(path: str, **fields):
     _check(N.load().gga_write_result_row(path.encode(), C.byref(r)), "writeResult")
 
 
+def combine_clocks(block_cycles, sms: int = 14):
+    """The reference's load-balance estimate of one launch (combineClocks,
+    metrics.h:68-84, with getminIndex / getmaxIndex, metrics.h:1-24): blocks
+    in launch order go to the least-loaded SM (lowest index on ties), and the
+    estimate is the busiest SM's total.  Returns (estimate, SM of each block).
+    The reference sums the estimates of every iteration (bfs_sssp.cu:527-536)
+    with its 14 SMs; pass sms=152 for a GB300."""
+    load = [0] * sms
+    where = []
+    for c in block_cycles:
+        k = min(range(sms), key=lambda j: (load[j], j))
+        where.append(k)
+        load[k] += int(c)
+    return max(load), where
+
+
 class Context:
     """A device context: stream, events and scratch on one GPU."""
 
@@ -401,9 +417,12 @@ class Context:
         _check(N.load().gga_trace_get(self._h, rounds, nr.value, C.byref(nr),
                                       cta.ctypes.data_as(C.POINTER(C.c_uint32)), nb.value, C.byref(nb)), "trace_get")
         kinds = ("near", "bottom_up", "far", "heavy", "pull_scan", "pull")
+        busy = cta[: nb.value]
         return {"rounds": [{"kind": kinds[r.kind] if r.kind < len(kinds) else r.kind, "items": r.items,
                             "edges": r.edges, "far_items": r.far_items, "us": r.ns / 1e3} for r in rounds[: nr.value]],
-                "cta_kcycles": cta[: nb.value]}
+                "cta_kcycles": busy,
+                # busiest CTA over the mean: 1.0 is a perfectly balanced launch
+                "imbalance": float(busy.max() / busy.mean()) if len(busy) and busy.mean() > 0 else None}
 
     def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False, out=None):
         """Up to 64 BFS sources in one bit-packed launch; out: optional

@@ -180,3 +180,15 @@ def test_grid_generator_properties():
 def test_maxweight_rejected_for_sssp_only():
     g = gga.Graph.from_csr([0, 1, 1], [1], [gga.MAX_WEIGHT + 1])
     assert g.info()["max_weight"] == gga.MAX_WEIGHT + 1
+
+
+def test_combine_clocks_matches_reference_rule():
+    """metrics.h:68-84: blocks in order onto the least-loaded SM (first index
+    on ties); the estimate is the busiest SM's total."""
+    import gpugraphalgo_gb300 as gga
+
+    assert gga.combine_clocks([5, 3, 4, 1, 2], sms=2) == (8, [0, 1, 1, 0, 0])
+    assert gga.combine_clocks([1, 1, 1], sms=3) == (1, [0, 1, 2])
+    assert gga.combine_clocks([7] * 14) == (7, list(range(14)))
+    assert gga.combine_clocks([7] * 15)[0] == 14
+    assert gga.combine_clocks([], sms=4) == (0, [])
