@@ -424,6 +424,23 @@ class Context:
                 # busiest CTA over the mean: 1.0 is a perfectly balanced launch
                 "imbalance": float(busy.max() / busy.mean()) if len(busy) and busy.mean() > 0 else None}
 
+    def convergence(self, graph: Graph, algo, src: int, final, variant="topo_atomic"):
+        """Per-iteration convergence of a topology-driven solve against
+        `final` (printConv_rtime, convergence.h:100-159): one dict per relax
+        launch with the vertices still differing and the norm the reference
+        prints.  Returns (records, distances)."""
+        fin = np.ascontiguousarray(final, dtype=np.uint32)
+        if fin.shape != (graph.n,):
+            raise ValueError(f"final: {graph.n} distances expected")
+        out = np.empty(graph.n, np.uint32)
+        cap = min(graph.n + 2, 1 << 20)
+        recs = (N.ConvRecord * cap)()
+        nrec = C.c_uint32()
+        _check(N.load().gga_convergence(self._h, graph.handle, _algo(algo), src, _variant(variant), _ptr(fin), recs,
+                                        cap, C.byref(nrec), _ptr(out)), f"convergence({algo}, src={src}, {variant})")
+        return ([{"iteration": r.iteration, "diff_count": r.diff_count, "norm2": r.norm2}
+                 for r in recs[: min(nrec.value, cap)]], out)
+
     def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False, out=None):
         """Up to 64 BFS sources in one bit-packed launch; out: optional
         (len(srcs), n) uint32 array (pinned_empty for the fastest copy) or an

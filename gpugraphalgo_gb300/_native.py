@@ -60,6 +60,10 @@ class RoundTrace(C.Structure):
     _fields_ = [("kind", u32), ("items", u32), ("edges", u32), ("far_items", u32), ("ns", u32)]
 
 
+class ConvRecord(C.Structure):
+    _fields_ = [("iteration", u32), ("pad", u32), ("diff_count", C.c_uint64), ("norm2", C.c_double)]
+
+
 class Params(C.Structure):
     _fields_ = [
         ("block_threads", u32),
@@ -172,6 +176,7 @@ SIGNATURES = {
     "gga_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
     "gga_server_destroy": (None, [P]),
     "gga_trace_enable": (C.c_int, [P, C.c_int]),
+    "gga_convergence": (C.c_int, [P, P, C.c_int, u32, C.c_int, P, C.POINTER(ConvRecord), u32, C.POINTER(u32), P]),
     "gga_trace_get": (C.c_int, [P, C.POINTER(RoundTrace), u32, C.POINTER(u32), C.POINTER(u32), u32, C.POINTER(u32)]),
 }
 

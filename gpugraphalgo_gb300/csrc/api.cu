@@ -317,7 +317,10 @@ struct TopoResult {
 gga_status topo_run(const DevGraph *d, bool split, gga_variant variant, bool sssp, uint32_t src,
                     uint32_t max_allowed, uint32_t cdp_mode, uint32_t *dist, uint32_t *scratch_heavy,
                     uint32_t *dflag, uint32_t *hflag, int sms, cudaStream_t st, cudaEvent_t *ev,
-                    TopoResult *res);
+                    TopoResult *res, ConvHook *conv);
+
+/* Set by gga_convergence around its gga_solve call (same thread). */
+static thread_local ConvHook *tl_conv = nullptr;
 
 gga_status ctx_validate_solve(const gga_graph *g, gga_algo algo, uint32_t src) {
     if (algo != GGA_BFS && algo != GGA_SSSP) return gga_fail(GGA_ERR_INVALID_ARG, "unknown algorithm %d", (int)algo);
@@ -444,7 +447,7 @@ gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_
         if ((s = frontier_scratch_ensure(&c->fs, v.n > d->n ? v.n : d->n, d->m))) return s;
         TopoResult r;
         s = topo_run(d, split, variant, sssp, src, max_allowed, p.cdp_mode, c->fs.dist, c->heavy, c->dflag, c->hflag,
-                     c->sms, c->st, c->ev, &r);
+                     c->sms, c->st, c->ev, &r, tl_conv);
         if (s) return s;
         st.iterations = r.iterations;
         st.kernel_launches = r.launches;
@@ -463,6 +466,50 @@ gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_
     st.total_ms = gga_now_ms() - t0;
     if (stats) *stats = st;
     return GGA_OK;
+}
+
+gga_status gga_convergence(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_variant variant,
+                           const uint32_t *final_dist, gga_conv_record *records, uint32_t cap, uint32_t *nrec,
+                           uint32_t *dist_out) {
+    if (!c || !g || !final_dist || !nrec || (cap && !records)) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    if (variant != GGA_VARIANT_TOPO_ATOMIC && variant != GGA_VARIANT_TOPO_PLAIN && variant != GGA_VARIANT_CDP_ATOMIC &&
+        variant != GGA_VARIANT_CDP_PLAIN)
+        return gga_fail(GGA_ERR_INVALID_ARG, "convergence logs need a topology-driven variant (got %d)", (int)variant);
+    gga_status s = ctx_validate_solve(g, algo, src);
+    if (s) return s;
+    uint32_t *fin = nullptr;
+    unsigned long long *acc = nullptr;
+    uint32_t *tmp = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        if ((s = ctx_activate(c))) return s;
+        cudaError_t e = cudaMalloc((void **)&fin, (size_t)g->n * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&acc, 2 * sizeof(unsigned long long));
+        if (e == cudaSuccess && !dist_out) e = cudaMalloc((void **)&tmp, (size_t)g->n * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMemcpy(fin, final_dist, (size_t)g->n * sizeof(uint32_t), cudaMemcpyDefault);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(fin);
+            cudaFree(acc);
+            cudaFree(tmp);
+            return gga_fail(GGA_ERR_CUDA, "convergence buffers: %s", cudaGetErrorString(e));
+        }
+    }
+    ConvHook h;
+    h.fin = fin;
+    h.cnt = acc;
+    h.norm = (double *)(acc + 1);
+    h.rec = records;
+    h.cap = cap;
+    h.n = 0;
+    tl_conv = &h;
+    s = gga_solve(c, g, algo, src, variant, dist_out ? dist_out : tmp, nullptr);
+    tl_conv = nullptr;
+    cudaFree(fin);
+    cudaFree(acc);
+    cudaFree(tmp);
+    *nrec = h.n;
+    return s;
 }
 
 /* Buffers of gga_solve_many for n sources of `words`-vertex results. */

@@ -56,6 +56,16 @@ struct DevGraph {
 };
 
 /* The graph a relaxation engine walks: either the unsplit CSR or the split one. */
+/* Convergence log of a topology-driven solve (gga_convergence): after every
+ * relax launch the current distances are compared with `fin`. */
+struct ConvHook {
+    const uint32_t *fin;     /* device: final distances of the original vertices */
+    unsigned long long *cnt; /* device: vertices that differ (one launch) */
+    double *norm;            /* device: sum of the squared differences */
+    gga_conv_record *rec;    /* host: records, room for cap */
+    uint32_t cap, n;         /* n: iterations logged */
+};
+
 struct GraphView {
     const uint32_t *off;
     const uint32_t *col;

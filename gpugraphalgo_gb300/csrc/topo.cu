@@ -20,6 +20,9 @@
  * launch, read `changed`, repeat; launch shape BLOCKSIZE=1024 threads x
  * #SMs x FACTOR blocks (bfs_sssp.cu:145,333-334).
  */
+#include <algorithm>
+#include <math.h>
+
 #include "gga_device.cuh"
 
 namespace {
@@ -188,11 +191,35 @@ struct TopoResult {
     float ktime, sktime;
 };
 
+/* printConv_rtime (convergence.h:100-159) on the device: over the original
+ * vertices u, the current distance of u's parent against fin[u]; the count
+ * of differences and the sum of (fs - fi)^2 taken in 32-bit unsigned
+ * arithmetic, as the reference's foru expression computes it. */
+__global__ void k_conv_compare(const uint32_t *dist, const uint32_t *first, const uint32_t *fin, uint32_t n,
+                               unsigned long long *cnt, double *norm) {
+    unsigned long long c = 0;
+    double sum = 0.0;
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n; u += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t fi = dist[first ? first[u] : u], fs = fin[u];
+        const uint32_t d = fs - fi;
+        sum += (double)(uint32_t)(d * d);
+        c += fs != fi;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        c += __shfl_down_sync(0xffffffffu, c, o);
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+    }
+    if ((threadIdx.x & 31) == 0 && c) {
+        atomicAdd(cnt, c);
+        atomicAdd(norm, sum);
+    }
+}
+
 /* Runs a reference-semantics variant; distances land in `dist` (view ids). */
 gga_status topo_run(const DevGraph *d, bool split, gga_variant variant, bool sssp, uint32_t src,
                     uint32_t max_allowed, uint32_t cdp_mode, uint32_t *dist, uint32_t *scratch_heavy,
                     uint32_t *dflag, uint32_t *hflag, int sms, cudaStream_t st, cudaEvent_t *ev,
-                    TopoResult *res) {
+                    TopoResult *res, ConvHook *conv) {
     const bool cdp = variant == GGA_VARIANT_CDP_ATOMIC || variant == GGA_VARIANT_CDP_PLAIN;
     const bool atomic = variant == GGA_VARIANT_TOPO_ATOMIC || variant == GGA_VARIANT_CDP_ATOMIC;
     const GraphView g = dev_graph_view(d, split && !cdp);
@@ -236,9 +263,32 @@ gga_status topo_run(const DevGraph *d, bool split, gga_variant variant, bool sss
         cudaEventRecord(ev[1], st);
         res->launches++;
         GGA_CK(cudaGetLastError());
+        if (conv) {
+            GGA_CK(cudaMemsetAsync(conv->cnt, 0, sizeof(unsigned long long), st));
+            GGA_CK(cudaMemsetAsync(conv->norm, 0, sizeof(double), st));
+            const uint32_t cb = std::min<uint32_t>((d->n + 255) / 256, (uint32_t)sms * 8);
+            k_conv_compare<<<cb ? cb : 1, 256, 0, st>>>(dist, split && !cdp ? d->first : nullptr, conv->fin, d->n,
+                                                        conv->cnt, conv->norm);
+            GGA_CK(cudaGetLastError());
+            res->launches++;
+        }
         GGA_CK(cudaMemcpyAsync(hflag, dflag, 4 * sizeof(uint32_t) + sizeof(CdpState), cudaMemcpyDeviceToHost, st));
         gga_status w = dev_wait(st, 60.0);
         if (w) return w;
+        if (conv) {
+            unsigned long long hc = 0;
+            double hn = 0.0;
+            GGA_CK(cudaMemcpy(&hc, conv->cnt, sizeof hc, cudaMemcpyDeviceToHost));
+            GGA_CK(cudaMemcpy(&hn, conv->norm, sizeof hn, cudaMemcpyDeviceToHost));
+            if (conv->n < conv->cap) {
+                gga_conv_record &r = conv->rec[conv->n];
+                r.iteration = res->iterations;
+                r.pad = 0;
+                r.diff_count = hc;
+                r.norm2 = sqrt(hn);
+            }
+            conv->n++;
+        }
         cudaEventElapsedTime(&t, ev[0], ev[1]);
         res->ktime += t;
         if (children) {

@@ -295,6 +295,27 @@ gga_status gga_trace_enable(gga_ctx *ctx, int enable);
 gga_status gga_trace_get(gga_ctx *ctx, gga_round_trace *rounds, uint32_t cap, uint32_t *nrounds,
                          uint32_t *cta_kcycles, uint32_t cta_cap, uint32_t *ncta);
 
+/* One iteration of a convergence log. */
+typedef struct gga_conv_record {
+    uint32_t iteration;  /* 1-based relax launch */
+    uint32_t pad;
+    uint64_t diff_count; /* original vertices whose distance differs from the final one */
+    double norm2;        /* sqrt(sum over them of (final - current)^2), the square taken in
+                          * 32-bit unsigned arithmetic as the reference's foru does */
+} gga_conv_record;
+/* Per-iteration convergence of a topology-driven solve, replacing
+ * printConv_rtime (convergence.h:100-159, called after every relax launch at
+ * bfs_sssp.cu:420-424): after each launch the current distances of the
+ * original vertices (the split parents) are compared on the device with
+ * final_dist (host, nodes_orig words, e.g. an earlier solve's answer).
+ * variant: TOPO_ATOMIC, TOPO_PLAIN, CDP_ATOMIC or CDP_PLAIN (the frontier
+ * engine has rounds, not iterations; gga_trace_get covers it).  Up to cap
+ * records are written; *nrec receives the number of iterations run.
+ * dist_out (host or device, may be NULL) receives the solve's answer. */
+gga_status gga_convergence(gga_ctx *ctx, gga_graph *g, gga_algo algo, uint32_t src, gga_variant variant,
+                           const uint32_t *final_dist, gga_conv_record *records, uint32_t cap, uint32_t *nrec,
+                           uint32_t *dist_out);
+
 /* ---- verification and output (myutils.h, L5) ---------------------------- */
 
 /* verifysolution, myutils.h:1-18: number of edges with wt>0 and

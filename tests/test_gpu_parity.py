@@ -489,3 +489,37 @@ def test_sssp_tail_cuts_rounds(ctx):
         ctx.reset_params()
     np.testing.assert_array_equal(res[0][0], res[1][0])
     assert res[0][1]["iterations"] < res[1][1]["iterations"]
+
+
+@pytest.mark.parametrize("variant", ["topo_atomic", "topo_plain", "cdp_atomic"])
+@pytest.mark.parametrize("algo", ["bfs", "sssp"])
+def test_convergence_log(ctx, variant, algo):
+    """printConv_rtime (convergence.h:100-159) after every relax launch: the
+    vertices still differing from the final answer shrink to none, and the
+    reference's norm (squares of 32-bit unsigned differences) is exact."""
+    g = gga.Graph.rmat(11, 8, seed=41)
+    if variant == "topo_plain":
+        g.node_split(ctx, -1, 10)
+    want = _oracle_dist(g, algo, 7)
+    recs, got = ctx.convergence(g, algo, 7, want, variant)
+    np.testing.assert_array_equal(got, want)
+    assert [r["iteration"] for r in recs] == list(range(1, len(recs) + 1))
+    diffs = [r["diff_count"] for r in recs]
+    assert diffs == sorted(diffs, reverse=True) and diffs[-1] == 0 and recs[-1]["norm2"] == 0.0
+    reached = want < gga.INFINITY
+    n = int(reached.sum())
+    # against a final answer off by a known amount the converged state shows it
+    for off, per_vertex in ((1, 1), (-1, 1), (65536, 0), (3, 9)):
+        fin = want.astype(np.int64)
+        fin[reached] += off
+        fin = (fin % (1 << 32)).astype(np.uint32)
+        recs, _ = ctx.convergence(g, algo, 7, fin, variant)
+        assert recs[-1]["diff_count"] == n
+        assert recs[-1]["norm2"] == pytest.approx((n * per_vertex) ** 0.5, rel=1e-12, abs=0)
+
+
+def test_convergence_rejects_frontier(ctx):
+    g = gga.Graph.rmat(8, 4, seed=2)
+    with pytest.raises(gga.GGAError) as ex:
+        ctx.convergence(g, "bfs", 0, np.zeros(g.n, np.uint32), "frontier")
+    assert ex.value.status == gga.ERR_INVALID_ARG
