@@ -192,3 +192,18 @@ def test_combine_clocks_matches_reference_rule():
     assert gga.combine_clocks([7] * 14) == (7, list(range(14)))
     assert gga.combine_clocks([7] * 15)[0] == 14
     assert gga.combine_clocks([], sms=4) == (0, [])
+
+
+def test_combine_clocks_matches_reference_fixture():
+    """Against the reference's own combineClocks (metrics.h:68-84, 14 SMs),
+    run by tests/golden/make_golden_clocks.py."""
+    import json
+    import os
+
+    import gpugraphalgo_gb300 as gga
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "clocks.json")) as f:
+        cases = json.load(f)["cases"]
+    assert len(cases) >= 10
+    for c in cases:
+        assert gga.combine_clocks(c["clocks"]) == (c["estimate"], c["sm"]), len(c["clocks"])
