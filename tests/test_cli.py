@@ -86,3 +86,16 @@ def test_split_sweep_writes_one_row_per_point(tmp_path):
         if r[0].startswith(("na_", "gga_")) and level < 2**31:
             assert int(r[11]) == -(-maxdeg // level)
         assert float(r[14]) > 0 and int(r[12]) >= 1
+
+
+def test_sweep_points_follow_the_reference_driver():
+    """mysc:20-51 runs levels 1..40 (no bucket argument, so the default 10)
+    and then the histogram rule (level -1) with buckets 2, 5, 10, 15."""
+    from gpugraphalgo_gb300 import sweep
+
+    pts = sweep.sweep_points(sweep._levels("1-40"), [2, 5, 10, 15])
+    assert pts == [(i, 10) for i in range(1, 41)] + [(-1, 2), (-1, 5), (-1, 10), (-1, 15)]
+    assert sweep._levels("1-3,7,9-10") == [1, 2, 3, 7, 9, 10]
+    assert sweep._levels("-1") == [-1]
+    assert sweep.VARIANT == {"na": "topo_atomic", "n": "topo_plain", "da": "cdp_atomic", "d": "cdp_plain",
+                             "gga": "frontier"}
