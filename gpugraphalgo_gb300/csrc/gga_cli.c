@@ -30,7 +30,9 @@
  *
  * Differences on purpose: errors return a non-zero exit status with a
  * message instead of exit(-1) / SIGFPE (the histogram rule's division by
- * zero reports GGA_ERR_SPLIT_RULE).
+ * zero reports GGA_ERR_SPLIT_RULE), and the usage check comes before the
+ * device is opened (the reference prints its device lines first,
+ * bfs_sssp.cu:135-152).
  */
 #include <stdio.h>
 #include <stdlib.h>

@@ -99,3 +99,22 @@ def test_sweep_points_follow_the_reference_driver():
     assert sweep._levels("-1") == [-1]
     assert sweep.VARIANT == {"na": "topo_atomic", "n": "topo_plain", "da": "cdp_atomic", "d": "cdp_plain",
                              "gga": "frontier"}
+
+
+@pytest.mark.parametrize("exe", FLAVOURS)
+def test_cli_usage_without_arguments(exe):
+    """The algorithm line (bfs_sssp.cu:106-111), then the usage line and exit
+    status 1 when no graph is given (bfs_sssp.cu:149-152).  The reference
+    prints its device lines in between; this CLI reaches the usage check
+    without touching a device."""
+    r = subprocess.run([os.path.join(BIN, exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    lines = r.stdout.splitlines()
+    assert lines[0] == ("SSSP" if "sssp" in exe else "BFS")
+    assert lines[1].startswith("Usage: ") and lines[1].endswith(" <file>")
+
+
+def test_cli_algorithm_override():
+    r = subprocess.run([os.path.join(BIN, "d_sssp")], capture_output=True, text=True, timeout=60,
+                       env={**os.environ, "GGA_ALGO": "bfs"})
+    assert r.returncode == 1 and r.stdout.splitlines()[0] == "BFS"
