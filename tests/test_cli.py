@@ -118,3 +118,18 @@ def test_cli_algorithm_override():
     r = subprocess.run([os.path.join(BIN, "d_sssp")], capture_output=True, text=True, timeout=60,
                        env={**os.environ, "GGA_ALGO": "bfs"})
     assert r.returncode == 1 and r.stdout.splitlines()[0] == "BFS"
+
+
+def test_conv_log_format_matches_reference_lines():
+    """conv.vi lines as convergence.h:84-134 writes them: a header after
+    three blank lines and an 88-dash rule, `Iteration:` with the iteration
+    left-aligned in 3 columns and the norm printed like a C++ stream double,
+    and the footer."""
+    from gpugraphalgo_gb300 import conv
+
+    assert conv.header(-1, 1234, "rmat20.gr", "SSSP") == "\n\n\n" + "-" * 88 + "\nDist_Level_-1_MaxDeg_1234_rmat20.gr_SSSP\n"
+    assert conv.iteration_line(1, 123456.789, 42) == "Iteration:1   = 123457(42)\n"
+    assert conv.iteration_line(12, 0.0, 0) == "Iteration:12  = 0(0)\n"
+    assert conv.iteration_line(1234, 1.5e-7, 3) == "Iteration:1234 = 1.5e-07(3)\n"
+    assert conv.iteration_line(7, 65536.0 ** 2, 1) == "Iteration:7   = 4.29497e+09(1)\n"
+    assert conv.footer(17, 254) == "Total Iteration : 17     Max Dist : 254\n" + "-" * 88 + "\n"
