@@ -133,3 +133,22 @@ def test_conv_log_format_matches_reference_lines():
     assert conv.iteration_line(1234, 1.5e-7, 3) == "Iteration:1234 = 1.5e-07(3)\n"
     assert conv.iteration_line(7, 65536.0 ** 2, 1) == "Iteration:7   = 4.29497e+09(1)\n"
     assert conv.footer(17, 254) == "Total Iteration : 17     Max Dist : 254\n" + "-" * 88 + "\n"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flavour", ["na", "d"])
+def test_conv_tool_writes_a_converging_log(tmp_path, flavour):
+    g = gga.Graph.rmat(10, 8, seed=3)
+    gr = str(tmp_path / "rmat10.gr")
+    g.save_gr(gr)
+    from gpugraphalgo_gb300 import conv
+
+    out = tmp_path / "conv.vi"
+    assert conv.main([gr, "--flavour", flavour, "--algo", "sssp", "--level", "2", "--out", str(out)]) == 0
+    lines = out.read_text().split("\n")
+    assert lines[:3] == ["", "", ""] and lines[3] == "-" * 88
+    assert lines[4] == f"Dist_Level_2_MaxDeg_{g.info()['maxdeg']}_rmat10.gr_SSSP"
+    its = [x for x in lines if x.startswith("Iteration:")]
+    assert its and its[-1].endswith(" = 0(0)")
+    want = oracle.serial_distances(*g.csr(), "sssp", 0)
+    assert f"Total Iteration : {len(its)}     Max Dist : {int(want[want < gga.INFINITY].max())}" in lines
