@@ -3,11 +3,11 @@
 The reference's ENABLE_IT_DIST + ENABLE_RTIME_DIST build copies the distances
 back after every relax launch and appends to conv.vi: a header naming the
 split level, maximum degree, graph and algorithm (printConv_rtime_init,
-convergence.h:84-91, called at bfs_sssp.cu:247-249), one line per iteration
+convergence.h:81-90, called at bfs_sssp.cu:247-249), one line per iteration
 with the norm of the difference to the serial answer and the count of
-differing vertices (printConv_rtime, convergence.h:100-134, called at
+differing vertices (printConv_rtime, convergence.h:100-159, called at
 bfs_sssp.cu:420-424), and a footer with the iteration count and the largest
-distance (printConv_rtime_final, convergence.h:92-99, bfs_sssp.cu:510-517).
+distance (printConv_rtime_final, convergence.h:91-99, bfs_sssp.cu:510-517).
 
 Here the per-iteration figures come from gga_convergence, computed on the
 device; the final answer is the frontier engine's (bit-identical to the

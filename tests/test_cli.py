@@ -121,7 +121,7 @@ def test_cli_algorithm_override():
 
 
 def test_conv_log_format_matches_reference_lines():
-    """conv.vi lines as convergence.h:84-134 writes them: a header after
+    """conv.vi lines as convergence.h:81-159 writes them: a header after
     three blank lines and an 88-dash rule, `Iteration:` with the iteration
     left-aligned in 3 columns and the norm printed like a C++ stream double,
     and the footer."""
