@@ -13,18 +13,27 @@ value    GTEPS = sum of E_r over the step's traversals / device time of the
          step (CUDA events on the library's stream around K steps); E_r is
          the out-degree sum of reached vertices, directed edges counted once.
 e2e      the same metric through the C ABI with HOST buffers: every step
-         re-uploads the pinned CSR and copies each distance vector back.
+         drops the device copy, re-uploads the pinned CSR, rebuilds what the
+         engine derives from it and copies each distance vector back; the
+         per-phase breakdown is in the line.
 roofline the dominant persistent kernel: algorithmic bytes per launch
          (BFS 8*E_r + 20*V_r, SSSP 12*E_r + 20*V_r) / its mean launch time
          against the measured HBM copy bandwidth.
 cpu_baseline  the oracle (C restatement of the reference's serial
-         findSerialBFS/SSSP, graph.h:115-184) on the host cores, one source
-         per thread, on a bounded sample of the same workload.
+         findSerialBFS/SSSP, graph.h:115-184) on the host cores, every thread
+         taking the next traversal, on a bounded sample of the same workload;
+         plus the single-source latency on one core.
+parity   the GPU distances of that sample (the timed step's own call and
+         parameters) against the oracle's, bit for bit, plus verifysolution;
+         likewise the 4096^2 grid configuration (grid4096: GTEPS, roofline,
+         parity against an exact FIFO-BFS / Dijkstra checker).  Any mismatch
+         makes the run exit non-zero after printing its line.
 
 --impl reference times that CPU path alone (the reference's implementation of
-the path; it has no other runnable form on this machine) on the same metric.
-Multi-GPU: launched with torchrun, every rank runs an independent replica of
-the workload on its own GPU with its own sources ("scaling": "weak").
+the path; it has no other runnable form on this machine) on the same metric,
+without loading the GPU library.  Multi-GPU: launched with torchrun, every
+rank runs an independent replica of the workload on its own GPU with its own
+sources ("scaling": "weak").
 """
 from __future__ import annotations
 
@@ -63,6 +72,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--autotune-trials", type=int, default=1)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-query and serving sections")
+    ap.add_argument("--no-grid", action="store_true", help="skip the 4096^2 grid section")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="offered-load duration per Poisson rate")
     return ap.parse_args()
 
@@ -160,15 +170,32 @@ class ClockSampler:
 
 # ------------------------------------------------------------ workload
 
+RMAT_ABC = (0.57, 0.19, 0.19)
+
+
+def pick_sources(deg, count: int, rank: int):
+    """`count` distinct random sources of degree > 0 (the same list for the
+    GPU arm and the CPU arm of one rank)."""
+    rng = np.random.default_rng(2 + 1000 * rank)
+    cand = np.nonzero(np.asarray(deg) > 0)[0]
+    return [int(x) for x in rng.choice(cand, size=count, replace=False)]
+
+
 def make_workload(args, rank: int):
     import gpugraphalgo_gb300 as gga
 
-    g = gga.Graph.rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, seed=2, wmin=1, wmax=255)
-    deg = g.degrees()
-    rng = np.random.default_rng(2 + 1000 * rank)
-    cand = np.nonzero(deg > 0)[0]
-    srcs = [int(x) for x in rng.choice(cand, size=args.sources, replace=False)]
-    return g, srcs
+    g = gga.Graph.rmat(args.scale, args.edge_factor, *RMAT_ABC, seed=2, wmin=1, wmax=255)
+    return g, pick_sources(g.degrees(), args.sources, rank)
+
+
+def workload_config(args, n: int, m: int, maxdeg: int, world: int) -> dict:
+    """The workload both arms run (the same dict in both lines)."""
+    return {"workload": f"rmat{args.scale}_ef{args.edge_factor}_seed2_{args.sources}src_bfs+sssp",
+            "graph": f"R-MAT scale {args.scale} ef {args.edge_factor} a/b/c=.57/.19/.19 seed 2, symmetrised, "
+                     "dedup, ids permuted, weights U[1,255]",
+            "vertices": n, "edges": m, "maxdeg": maxdeg, "sources": args.sources,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (CSR %.2f GB vs 129 MB L2); no flush" % ((4 * (n + 1) + 8 * m) / 1e9)}
 
 
 def algorithmic_bytes(algo: str, er: int, vr: int) -> int:
@@ -187,65 +214,105 @@ def read_traffic(kind: str):
     return None
 
 
-def cpu_baseline(g, srcs, threads: int, budget_sources: int):
-    """Oracle serial BFS/SSSP (the reference's algorithm) on host threads."""
+def measured_peak():
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = json.load(open(pk)).get("hbm_gbs") if os.path.exists(pk) else None
+    return (peak, "measured") if peak else (6800.0, "fallback")
+
+
+# ------------------------------------------------------------ CPU legs (oracle)
+
+def cpu_pass(og, tasks, threads: int, keep: bool = False):
+    """The oracle's serial BFS/SSSP (the reference's findSerialBFS/SSSP,
+    graph.h:115-184) over `tasks` = [(source, algo)], `threads` host threads
+    taking the next task as they finish (ctypes releases the GIL, so the
+    threads run in parallel).  Returns (sum of E_r, wall seconds, distances
+    by (source, algo) when keep)."""
     import oracle
 
-    off, col, wt = g.csr()
-    og = oracle.OracleGraph.from_csr(off, col, wt)
     lib = oracle.load()
-    deg = np.diff(off.astype(np.int64))
-    sample = srcs[:budget_sources]
-    results = {}
+    deg = og.degrees().astype(np.int64)
+    n = len(deg)
+    er, dists = {}, {}
+    lock = threading.Lock()
+    nxt = [0]
 
-    def work(i, s):
-        for algo in ("bfs", "sssp"):
-            d = np.empty(len(off) - 1, np.uint32)
+    def worker():
+        while True:
+            with lock:
+                i = nxt[0]
+                nxt[0] += 1
+            if i >= len(tasks):
+                return
+            s, algo = tasks[i]
+            d = np.empty(n, np.uint32)
             lib.oracle_serial(og._h, 1 if algo == "sssp" else 0, s, oracle._p(d))
-            reach = d < oracle.INF
-            results[(i, algo)] = int(deg[reach].sum())
+            er[i] = int(deg[d < oracle.INF].sum())
+            if keep:
+                dists[(s, algo)] = d
 
     t0 = time.perf_counter()
-    ths = []
-    for i, s in enumerate(sample):
-        th = threading.Thread(target=work, args=(i, s))
+    ths = [threading.Thread(target=worker) for _ in range(max(1, min(threads, len(tasks))))]
+    for th in ths:
         th.start()
-        ths.append(th)
-        if len(ths) >= threads:
-            ths.pop(0).join()
     for th in ths:
         th.join()
-    dt = time.perf_counter() - t0
-    er = sum(results.values())
-    return er / dt / 1e9, dt, len(sample)
+    return sum(er.values()), time.perf_counter() - t0, dists
+
+
+def step_tasks(srcs):
+    """One CPU step: every source's SSSP first (the longer ones), then BFS."""
+    return [(s, "sssp") for s in srcs] + [(s, "bfs") for s in srcs]
+
+
+def latency_1core(og, src: int) -> dict:
+    """Single-source latency of the oracle on one core, per algorithm."""
+    out = {}
+    for algo in ("bfs", "sssp"):
+        _, dt, _ = cpu_pass(og, [(src, algo)], 1)
+        out[algo] = dt
+    return out
 
 
 def run_reference(args, dist: Dist):
-    """--impl reference: the reference's CPU path (oracle port) on host cores."""
+    """--impl reference: the reference's serial CPU path (the oracle's C
+    restatement of findSerialBFS/SSSP) on all host cores.  The workload graph
+    comes from the library's generator compiled into liboracle.so, so this
+    process never loads the GPU library."""
     if dist.rank != 0:
         return None
-    g, srcs = make_workload(args, 0)
+    import oracle
+
+    og = oracle.OracleGraph.gen_rmat(args.scale, args.edge_factor, *RMAT_ABC, seed=2, wmin=1, wmax=255)
+    deg = og.degrees()
+    srcs = pick_sources(deg, args.sources, 0)
     threads = os.cpu_count() or 1
-    per_step = max(2, min(threads, (threads * 6) // max(1, args.steps + args.warmup)))
-    for w in range(args.warmup):
-        cpu_baseline(g, srcs[w * per_step % len(srcs):][:per_step] or srcs[:per_step], threads, per_step)
-    vals, secs = [], 0.0
-    for k in range(args.steps):
+    per_step = min(threads, len(srcs))  # sources per step: every core busy
+
+    def window(k):
         start = (k * per_step) % len(srcs)
-        v, dt, _ = cpu_baseline(g, (srcs[start:] + srcs[:start])[:per_step], threads, per_step)
-        vals.append(v)
+        return (srcs[start:] + srcs[:start])[:per_step]
+
+    for w in range(args.warmup):  # pages the graph in: one BFS per thread
+        cpu_pass(og, [(s, "bfs") for s in window(w)], threads)
+    er_tot, secs = 0, 0.0
+    for k in range(args.steps):
+        er, dt, _ = cpu_pass(og, step_tasks(window(k)), threads)
+        er_tot += er
         secs += dt
-    value = statistics.mean(vals)
-    sample = f"{per_step} sources x (BFS+SSSP) per step, one source per thread, R-MAT-{args.scale}"
+    value = er_tot / secs / 1e9
+    lat = latency_1core(og, srcs[0])
+    dims = og.dims()
+    sample = (f"{per_step} sources x (BFS+SSSP) per step on {threads} threads taking the next traversal as they "
+              f"finish, R-MAT-{args.scale}")
     return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"rmat{args.scale}_ef{args.edge_factor}_seed2_{args.sources}src_bfs+sssp",
-                   "sources": args.sources,
-                   "implementation": "serial in-order Bellman-Ford sweeps (graph.h:115-184), oracle C port",
-                   "parallelism": f"{threads} host threads"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "config": workload_config(args, dims["nnodes"], dims["nedges"], int(np.max(deg)), dist.world),
+        "implementation": "serial in-order Bellman-Ford sweeps (graph.h:115-184), oracle C port, all host threads",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "latency_1core_s": lat},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -302,14 +369,16 @@ def batch_section(gga, ctx):
                      "batch_ms": bwall * 1e3, "gteps_kernel": er / (bst["kernel_ms"] * 1e-3) / 1e9 if bst["kernel_ms"] else None,
                      "rounds": bst["iterations"], "edges_relaxed": bst["edges_relaxed"], "edges_reached": er}
 
-    def reference_kernel(name, algo, srcs, batch_out, k=3):
-        """The same queries through the reference's own kernel (topology-driven
-        Bellman-Ford with atomicMin, the "na_" build), one launch sequence per
-        query with the result copied to host: a sample of k queries."""
+    def topo_reexpression(name, algo, srcs, batch_out, k=3):
+        """The same queries through this library's topology-driven
+        re-expression of the reference's "na_" relaxation (k_topo_relax, which
+        follows M_my_drelax, cudaKernels.h:285-344, over every vertex per
+        iteration; not the reference's kernel compiled unchanged), one launch
+        sequence per query with the result copied to host: k queries."""
         t0 = time.perf_counter()
         outs = [ctx.solve(g, algo, s, "topo_atomic", out=o64[i]) for i, s in enumerate(srcs[:k])]
         dt = time.perf_counter() - t0
-        res[name]["reference_kernel_one_at_a_time"] = {
+        res[name]["topo_reexpression_one_at_a_time"] = {
             "qps": k / dt, "sample_queries": k, "batch_speedup": res[name]["batch_qps"] / (k / dt),
             "identical": bool(all(np.array_equal(a, b) for a, b in zip(outs, batch_out)))}
 
@@ -318,21 +387,31 @@ def batch_section(gga, ctx):
     (bo, bst), bw = _timed(lambda: ctx.msbfs(g, s64, stats=True, out=b64), 3)
     so, sw, sk = singles([(g, "bfs", s) for s in s64], o64)
     record("msbfs64_rmat20", 64, list(bo), bst, bw, so, sw, sk, bst["edges_reached"])
-    reference_kernel("msbfs64_rmat20", "bfs", s64, bo)
+    topo_reexpression("msbfs64_rmat20", "bfs", s64, bo)
 
     b32 = b64[:32]
     ctx.sssp_batch(g, s32, out=b32)
     (bo, bst), bw = _timed(lambda: ctx.sssp_batch(g, s32, stats=True, out=b32), 3)
     so, sw, sk = singles([(g, "sssp", s) for s in s32], o64[:32])
     record("sssp32_rmat20", 32, list(bo), bst, bw, so, sw, sk, bst["edges_reached"])
-    reference_kernel("sssp32_rmat20", "sssp", s32, bo)
+    topo_reexpression("sssp32_rmat20", "sssp", s32, bo)
 
     gs = [gga.Graph.rmat(sc, 16, 0.57, 0.19, 0.19, seed=10 + i, wmin=1, wmax=255) for i, sc in enumerate(range(12, 21))]
     gs += [gga.Graph.grid(w, w, 0.05, 0.001, seed=19 + i, wmin=1, wmax=1000)
            for i, w in enumerate((256, 512, 768, 1024, 1280, 1536, 2048))]
+    # the autotuner picks each graph's parameters (stored on the graph): the
+    # batch uses its bucket width per graph, the one-at-a-time solves the rest
+    picks = []
+    for gg in gs:
+        gg.cudaCopy(ctx)
+        p = ctx.autotune(gg, 1)
+        picks.append({"n": gg.n, "block_threads": p["block_threads"], "sssp_delta": p["sssp_delta"],
+                      "expansion": ("edges_unsplit", "edges_split", "cdp")[p["expansion"]],
+                      "split_level": p["split_level"], "bfs_alpha": p["bfs_alpha"] or 8,
+                      "bfs_beta": p["bfs_beta"] or 18, "batch_delta": p["batch_delta"]})
+    ctx.reset_params()
     qs = []
     for j, gg in enumerate(gs):
-        gg.cudaCopy(ctx)
         r = np.random.default_rng(100 + j)
         for s in r.choice(np.nonzero(gg.degrees() > 0)[0], 8, replace=False):
             qs += [(gg, "bfs", int(s)), (gg, "sssp", int(s))]
@@ -342,6 +421,7 @@ def batch_section(gga, ctx):
     so, sw, sk = singles(qs, mo)
     record("mixed16x8_bfs+sssp", len(qs), bo, bst, bw, so, sw, sk, bst["edges_reached"])
     res["mixed16x8_bfs+sssp"]["graphs"] = "R-MAT 12..20 ef16 seeds 10-18, grids 256..2048 seeds 19-25"
+    res["mixed16x8_bfs+sssp"]["autotuned_per_graph"] = picks
     return res
 
 
@@ -358,7 +438,9 @@ def serving_section(gga, ctx, seconds: float, device: int):
         else:
             gg = gga.Graph.grid(size, size, 0.05, 0.001, seed=seed, wmin=1, wmax=1000)
         gg.cudaCopy(ctx)
+        ctx.autotune(gg, 1)  # per-graph parameters; the server reads each graph's batch bucket width
         graphs.append(gg)
+    ctx.reset_params()
     ns = [gg.n for gg in graphs]
     W = 512
     ring = torch.empty((W, max(ns)), dtype=torch.int32, device=f"cuda:{device}")
@@ -380,8 +462,9 @@ def serving_section(gga, ctx, seconds: float, device: int):
         ctx.solve(graphs[gi], al, s, out=ring[k % W][: ns[gi]])
     ctx.synchronize()
     seq_qps = len(seq) / (time.perf_counter() - t0)
-    # the reference's own kernel (topology-driven Bellman-Ford, "na_"), one
-    # query at a time, on the first queries of the same mix (at most ~5 s)
+    # the topology-driven re-expression of the reference's "na_" relaxation
+    # (k_topo_relax), one query at a time, on the first queries of the same
+    # mix (at most ~5 s)
     t0, nref = time.perf_counter(), 0
     for gi, al, s in seq[:8]:
         ctx.solve(graphs[gi], al, s, "topo_atomic", out=ring[nref % W][: ns[gi]])
@@ -396,8 +479,9 @@ def serving_section(gga, ctx, seconds: float, device: int):
     sys.setswitchinterval(0.0002)  # the submitting and the waiting thread share the GIL
     out = {"graphs": "R-MAT 16/18/20/21 ef16 seeds 30-33, grids 512/1024/1536/2048 seeds 34-37 (5% deleted, w 1..1000)",
            "mix": "70% BFS / 30% SSSP, uniform graph and source", "mem_cap_bytes": 60 << 30, "max_slots": 256,
-           "superstep_rounds": 8, "sequential_qps": seq_qps,
-           "reference_kernel_sequential": {"qps": ref_qps, "sample_queries": nref}, "rates": []}
+           "superstep": "until the first round in which an in-flight query has finished, at most 128 rounds",
+           "sequential_qps": seq_qps,
+           "topo_reexpression_sequential": {"qps": ref_qps, "sample_queries": nref}, "rates": []}
     try:
         # exactness: served answers equal single-query answers
         chk = draw(24)
@@ -460,11 +544,57 @@ def serving_section(gga, ctx, seconds: float, device: int):
                                  "throttled_submits": throttled, "window": W})
         out["stats"] = srv.stats()
         out["peak_qps_vs_sequential"] = max(r["achieved_qps"] for r in out["rates"]) / seq_qps
-        out["peak_qps_vs_reference_kernel_sequential"] = max(r["achieved_qps"] for r in out["rates"]) / ref_qps
+        out["peak_qps_vs_topo_reexpression_sequential"] = max(r["achieved_qps"] for r in out["rates"]) / ref_qps
     finally:
         sys.setswitchinterval(old_switch)
         srv.close()
     return out
+
+
+def grid_section(gga, ctx, peak: float):
+    """The high-diameter configuration: a 4096 x 4096 grid (16.8 M vertices),
+    5% of edges deleted, 0.1% long-range edges, weights U[1,1000], seed 3,
+    source = the corner vertex 0; BFS and SSSP on parameters the autotuner
+    picks for this graph.  Device-timed GTEPS and roofline per algorithm; the
+    distances are kept for the oracle check."""
+    g = gga.Graph.grid(4096, 4096, 0.05, 0.001, seed=3, wmin=1, wmax=1000)
+    g.cudaCopy(ctx)
+    ctx.reset_params()
+    params = ctx.autotune(g, 1)
+    out = {"graph": "4096x4096 grid, 5% edges deleted, +0.1% long-range, w U[1,1000], seed 3",
+           "vertices": g.n, "edges": g.m, "source": 0, "params": {k: params[k] for k in ("block_threads", "sssp_delta")}}
+    res = {}
+    for algo in ("bfs", "sssp"):
+        ctx.set_params(skip_reached=0)
+        d, st = ctx.solve(g, algo, 0, stats=True)
+        ctx.set_params(skip_reached=1)
+        er, vr = st["edges_reached"], st["vertices_reached"]
+        ms = []
+        for _ in range(3):
+            _, st2 = ctx.solve(g, algo, 0, stats=True, keep_on_device=True)
+            ms.append(st2["kernel_ms"])
+        t = statistics.median(ms)
+        byts = algorithmic_bytes(algo, er, vr)
+        out[algo] = {"kernel_ms": t, "gteps": er / (t * 1e-3) / 1e9, "rounds": st["iterations"],
+                     "edges_reached": er, "vertices_reached": vr,
+                     "roofline_frac": byts / (t * 1e-3) / 1e9 / peak, "verify_errors": g.verifysolution(d, algo)}
+        res[algo] = d
+    ctx.reset_params()
+    return g, out, res
+
+
+def parity_check(pairs, check_fn) -> dict:
+    """pairs: {(src, algo): gpu distances}; check_fn(src, algo) -> oracle
+    distances.  Counts traversals whose arrays differ anywhere."""
+    mism, first = 0, None
+    for (s, algo), got in pairs.items():
+        want = check_fn(s, algo)
+        if not np.array_equal(got, want):
+            mism += 1
+            if first is None:
+                bad = np.nonzero(got != want)[0]
+                first = {"source": s, "algo": algo, "vertices_differing": int(len(bad)), "first": int(bad[0])}
+    return {"mismatches": mism, "first_mismatch": first}
 
 
 def run_gga(args, dist: Dist):
@@ -476,7 +606,7 @@ def run_gga(args, dist: Dist):
     info = g.info()
     g.cudaCopy(ctx)
     params = ctx.autotune(g, args.autotune_trials)
-    ctx.set_params(skip_reached=1)
+    tune_report = ctx.autotune_report()
     variant = args.variant
 
     # E_r / V_r per traversal (fixed by graph and source), outside the timing
@@ -531,13 +661,7 @@ def run_gga(args, dist: Dist):
         kinds[algo] = {"bytes_per_launch": byts, "ms_per_launch": per_launch_ms,
                        "achieved_gbs": byts / (per_launch_ms * 1e-3) / 1e9}
     dom = "sssp" if sssp_ms >= bfs_ms else "bfs"
-    peaks = {}
-    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(pk):
-        peaks = json.load(open(pk))
-    peak = peaks.get("hbm_gbs")
-    peak_src = "measured" if peak else "fallback"
-    peak = peak or 6800.0
+    peak, peak_src = measured_peak()
     tpe = read_traffic(dom)
     er_mean = (sssp_er if dom == "sssp" else bfs_er) / len(srcs)
     roofline = {"bound": "hbm", "kernel": f"k_frontier<{params['block_threads']},{'true' if dom == 'sssp' else 'false'}>",
@@ -551,13 +675,9 @@ def run_gga(args, dist: Dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"rmat{args.scale}_ef{args.edge_factor}_seed2_{args.sources}src_bfs+sssp",
-                   "graph": f"R-MAT scale {args.scale} ef {args.edge_factor} a/b/c=.57/.19/.19 seed 2, symmetrised, "
-                            "dedup, ids permuted, weights U[1,255]",
-                   "vertices": info["nodes_orig"], "edges": info["nedges"], "maxdeg": info["maxdeg"],
-                   "sources": args.sources, "parallelism": "replicas" if dist.world > 1 else "single",
-                   "l2": "inputs larger than L2 (CSR %.2f GB vs 129 MB L2); no flush" % ((4 * (info["nodes_orig"] + 1) + 8 * info["nedges"]) / 1e9),
-                   "variant": variant, "params": params, "device": dev["name"], "sms": dev["sms"]},
+        "config": workload_config(args, info["nodes_orig"], info["nedges"], info["maxdeg"], dist.world),
+        "engine": {"variant": variant, "params": params, "device": dev["name"], "sms": dev["sms"],
+                   "autotune_trials_ms": tune_report},
         "bfs_gteps": bfs_er / (bfs_ms * 1e-3) / 1e9,
         "sssp_gteps": sssp_er / (sssp_ms * 1e-3) / 1e9,
         "roofline": roofline,
@@ -565,43 +685,90 @@ def run_gga(args, dist: Dist):
         "clocks": clk,
     }
 
-    # reference algorithm (topology-driven Bellman-Ford, "na_") on the same GPU
+    # the topology-driven re-expression of the reference's "na_" relaxation
+    # (k_topo_relax: every vertex every iteration, host loop) on the same GPU
     try:
-        ta = {}
+        ta = {"what": "k_topo_relax, this library's re-expression of M_my_drelax (cudaKernels.h:285-344) "
+                      "with the host fixed-point loop of bfs_sssp.cu:372-468; not the reference's kernel compiled "
+                      "unchanged"}
         for algo in ("bfs", "sssp"):
             _, st = ctx.solve(g, algo, srcs[0], "topo_atomic", stats=True, keep_on_device=True)
             ta[algo] = {"ms": st["kernel_ms"], "iterations": st["iterations"],
                         "gteps": reach[(algo, srcs[0])][0] / (st["kernel_ms"] * 1e-3) / 1e9}
-        out["reference_algorithm_same_gpu"] = ta
+        out["topo_reexpression_same_gpu"] = ta
     except Exception as e:  # reported, not fatal
-        out["reference_algorithm_same_gpu"] = {"error": str(e)}
+        out["topo_reexpression_same_gpu"] = {"error": str(e)}
 
-    # end to end through the C ABI with host buffers: every step uploads the
-    # CSR again and copies every distance vector to page-locked host rows
-    # (gga_solve_many overlaps each copy with the next traversal)
+    # end to end through the C ABI with host buffers: every step drops the
+    # device copy, uploads the pinned CSR again, rebuilds what the engine
+    # derives from it (gga_graph_prepare) and copies every distance vector to
+    # page-locked host rows (gga_solve_many overlaps each copy with the next
+    # traversal); per-phase wall times are taken with a synchronize between
+    # phases
     if not args.no_e2e:
         g.pin(True)
         hout = {algo: gga.pinned_empty((len(srcs), info["nodes_orig"])) for algo in ("bfs", "sssp")}
         src_list = [int(s) for s in srcs]
+        e2e_steps = max(5, min(args.steps, 10))
+        phases = {"release": 0.0, "upload": 0.0, "prepare": 0.0, "bfs": 0.0, "sssp": 0.0}
+
+        def e2e_warm():  # untimed: first touch of the page-locked output rows
+            for algo in ("bfs", "sssp"):
+                ctx.solve_many(g, algo, src_list, out=hout[algo])
+
+        e2e_warm()
         dist.barrier()
-        e2e_steps = max(1, min(args.steps, 2))
+        ctx.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            ta = time.perf_counter()
             g.release_device()
-            for algo in ("bfs", "sssp"):
-                if variant in ("frontier", "auto"):
-                    ctx.solve_many(g, algo, src_list, out=hout[algo])
-                else:
-                    for i, s in enumerate(src_list):
-                        ctx.solve(g, algo, s, variant, out=hout[algo][i])
+            tb = time.perf_counter()
+            g.cudaCopy(ctx)
+            tc = time.perf_counter()
+            ctx.prepare(g, "bfs")
+            ctx.prepare(g, "sssp")
+            td = time.perf_counter()
+            ctx.solve_many(g, "bfs", src_list, out=hout["bfs"])
+            te = time.perf_counter()
+            ctx.solve_many(g, "sssp", src_list, out=hout["sssp"])
+            tf = time.perf_counter()
+            for k, dt in (("release", tb - ta), ("upload", tc - tb), ("prepare", td - tc), ("bfs", te - td),
+                          ("sssp", tf - te)):
+                phases[k] += dt
         ctx.synchronize()
         dt = time.perf_counter() - t0
         dt_max = dist.max(dt)
         out["e2e"] = {"value": dist.sum(er_step * e2e_steps) / dt_max / 1e9, "unit": UNIT,
                       "h2d_bytes_per_step": 4 * (info["nodes_orig"] + 1) + 8 * info["nedges"],
                       "d2h_bytes_per_step": 4 * info["nodes_orig"] * 2 * len(srcs),
-                      "steps": e2e_steps}
+                      "steps": e2e_steps, "ms_per_step": dt * 1e3 / e2e_steps,
+                      "breakdown_ms_per_step": {k: v * 1e3 / e2e_steps for k, v in phases.items()},
+                      "device_ms_per_step": ms_max / args.steps}
         g.cudaCopy(ctx)
+        ctx.prepare(g, "bfs")
+        ctx.prepare(g, "sssp")
+
+    threads = os.cpu_count() or 1
+    checks = not args.no_cpu_baseline and dist.rank == 0
+    psrc = srcs[:min(threads, len(srcs))]
+    gpu_res = {}
+    if checks:
+        # the timed step's own call and parameters, results to the host
+        for s in psrc:
+            for algo in ("bfs", "sssp"):
+                gpu_res[(s, algo)] = ctx.solve(g, algo, s, variant)
+
+    grid = None
+    if not args.no_grid and dist.rank == 0:
+        try:
+            grid = grid_section(gga, ctx, peak)
+            out["grid4096"] = grid[1]
+        except Exception as e:  # reported, not fatal
+            out["grid4096"] = {"error": repr(e)}
+            grid = None
+        ctx.set_params(**params)
+        ctx.set_params(skip_reached=1)
 
     if not args.no_batch and dist.rank == 0:
         # both sides of the batched comparisons use each graph's own defaults,
@@ -616,11 +783,51 @@ def run_gga(args, dist: Dist):
         except Exception as e:
             out["serving"] = {"error": repr(e)}
 
-    if dist.rank == 0 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        v, dt, ns = cpu_baseline(g, srcs, threads, min(threads, len(srcs)))
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": min(threads, ns), "kind": "port",
-                               "sample": f"{ns} sources x (BFS+SSSP), one source per thread, {dt:.1f} s wall"}
+    parity_ok = True
+    if checks:
+        import oracle
+
+        off, col, wt = g.csr()
+        og = oracle.OracleGraph.from_csr(off, col, wt)
+        del off, col, wt
+        er, dt, odist = cpu_pass(og, step_tasks(psrc), threads, keep=True)
+        out["cpu_baseline"] = {"value": er / dt / 1e9, "unit": UNIT, "cores": min(threads, 2 * len(psrc)),
+                               "kind": "port",
+                               "sample": f"{len(psrc)} sources x (BFS+SSSP) on {threads} threads taking the next "
+                                         f"traversal as they finish, {dt:.1f} s wall",
+                               "latency_1core_s": latency_1core(og, srcs[0])}
+        # parity at the metric's configuration: every compared traversal
+        # bit-exact with the oracle, and no relaxable edge left (verifysolution)
+        p = parity_check(gpu_res, lambda s, a: odist[(s, a)])
+        verr = sum(g.verifysolution(d, a) for (s, a), d in gpu_res.items())
+        out["parity"] = {"graph": f"R-MAT-{args.scale}", "sources": len(psrc), "traversals": len(gpu_res),
+                         "params": "the timed step's (autotuned)", "oracle": "serial sweeps (graph.h:115-184)",
+                         **p, "verify_errors": verr}
+        parity_ok = p["mismatches"] == 0 and verr == 0
+        del odist, og
+        if grid is not None:
+            gg, gout, gres = grid
+            ogg = oracle.OracleGraph.from_csr(*gg.csr())
+            box = {}
+
+            def grid_oracle():
+                for algo in ("bfs", "sssp"):
+                    box[algo] = ogg.shortest(algo, 0)
+
+            th = threading.Thread(target=grid_oracle, daemon=True)
+            t0 = time.perf_counter()
+            th.start()
+            th.join(timeout=300)
+            if th.is_alive():
+                gout["parity"] = {"timeout_s": 300, "checked": sorted(box)}
+                parity_ok = False
+            else:
+                gp = parity_check({(0, a): d for a, d in gres.items()}, lambda s, a: box[a])
+                gout["parity"] = {"oracle": "FIFO BFS / Dijkstra (oracle_shortest; equal to the serial sweeps on "
+                                            "every golden graph)", "oracle_s": time.perf_counter() - t0, **gp,
+                                  "verify_errors": gout["bfs"]["verify_errors"] + gout["sssp"]["verify_errors"]}
+                parity_ok = parity_ok and gp["mismatches"] == 0 and gout["parity"]["verify_errors"] == 0
+    out["parity_ok"] = parity_ok
     ctx.close()
     return out
 
@@ -628,12 +835,18 @@ def run_gga(args, dist: Dist):
 def main():
     args = parse_args()
     dist = Dist()
+    ok = True
     try:
         res = run_reference(args, dist) if args.impl == "reference" else run_gga(args, dist)
         if dist.rank == 0 and res is not None:
             print(json.dumps(res))
+            ok = res.get("parity_ok", True)
     finally:
         dist.close()
+    if not ok:
+        # a fast answer that differs from the oracle is not a result
+        print("bench: GPU distances differ from the oracle (see \"parity\")", file=sys.stderr)
+        sys.exit(1)
 
 
 if __name__ == "__main__":

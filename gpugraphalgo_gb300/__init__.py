@@ -358,10 +358,26 @@ class Context:
         _check(N.load().gga_get_params(self._h, C.byref(p)), "get_params")
         return p.as_dict()
 
+    def prepare(self, graph: Graph, algo):
+        """Upload `graph` if needed and build its once-per-graph derived data
+        for `algo` under the current parameters (gga_graph_prepare)."""
+        _check(N.load().gga_graph_prepare(self._h, graph.handle, _algo(algo)), f"prepare({algo})")
+
     def autotune(self, graph: Graph, trials: int = 0) -> dict:
+        """Per-graph parameters (gga_autotune): stored on `graph` and set on
+        this context.  With trials > 0 the choice comes from timed trials;
+        autotune_report() lists them."""
         p = N.Params()
         _check(N.load().gga_autotune(self._h, graph.handle, trials, C.byref(p)), "autotune")
         return p.as_dict()
+
+    def autotune_report(self) -> dict:
+        """The last autotune's candidates and their times (ms)."""
+        import json
+
+        buf = C.create_string_buffer(1 << 16)
+        _check(N.load().gga_autotune_report(self._h, buf, len(buf)), "autotune_report")
+        return json.loads(buf.value.decode())
 
     def solve(self, graph: Graph, algo, src: int, variant="auto", out=None, stats: bool = False,
               keep_on_device: bool = False):

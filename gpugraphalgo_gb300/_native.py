@@ -82,6 +82,10 @@ class Params(C.Structure):
         ("sssp_light_heavy", u32),
         ("sssp_pull", u32),
         ("sssp_tail", u32),
+        ("expansion", u32),
+        ("split_level", i32),
+        ("split_buckets", i32),
+        ("batch_delta", u32),
     ]
 
     def as_dict(self):
@@ -153,6 +157,7 @@ SIGNATURES = {
     "gga_ctx_synchronize": (C.c_int, [P]),
     "gga_graph_pin": (C.c_int, [P, C.c_int]),
     "gga_graph_release_device": (C.c_int, [P]),
+    "gga_graph_prepare": (C.c_int, [P, P, C.c_int]),
     "gga_bfs": (C.c_int, [P, P, u32, C.c_int, P, C.POINTER(Stats)]),
     "gga_sssp": (C.c_int, [P, P, u32, C.c_int, P, C.POINTER(Stats)]),
     "gga_solve": (C.c_int, [P, P, C.c_int, u32, C.c_int, P, C.POINTER(Stats)]),
@@ -162,6 +167,7 @@ SIGNATURES = {
     "gga_set_params": (C.c_int, [P, C.POINTER(Params)]),
     "gga_get_params": (C.c_int, [P, C.POINTER(Params)]),
     "gga_autotune": (C.c_int, [P, P, u32, C.POINTER(Params)]),
+    "gga_autotune_report": (C.c_int, [P, C.c_char_p, C.c_size_t]),
     "gga_verify": (C.c_int, [P, C.c_int, P, PU64]),
     "gga_write_dist": (C.c_int, [C.c_char_p, P, P]),
     "gga_reached": (C.c_int, [P, P, PU64, PU64]),

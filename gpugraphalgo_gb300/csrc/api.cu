@@ -9,6 +9,7 @@
  * or the reference's host loop (TOPO/CDP variants) -> gather the parents'
  * distances in original order -> one copy to the caller's buffer.
  */
+#include <algorithm>
 #include <mutex>
 #include <stdio.h>
 #include <stdlib.h>
@@ -234,11 +235,22 @@ gga_params ctx_default_params(const gga_graph *g) {
     p.use_split = 0;
     p.cdp_level = 1;
     p.cdp_buckets = 10;
+    p.expansion = 0;
+    p.split_level = 0;
+    p.split_buckets = 10;
+    p.batch_delta = 0xFFFFFFFFu;
     return p;
 }
 
+/* Bucket width of g's queries in the batch engine: the autotuner's pick, else
+ * the degree-profile width. */
+uint32_t ctx_batch_delta(const gga_graph *g) {
+    if (g->has_tuned && g->tuned.batch_delta != 0xFFFFFFFFu) return g->tuned.batch_delta;
+    return ctx_profile_delta(g);
+}
+
 static gga_params effective_params(gga_ctx *c, const gga_graph *g) {
-    gga_params d = ctx_default_params(g);
+    gga_params d = g->has_tuned ? g->tuned : ctx_default_params(g);
     if (!c->params_set) return d;
     gga_params p = c->params;
     if (!p.block_threads) p.block_threads = d.block_threads;
@@ -364,6 +376,20 @@ static gga_status frontier_plan(gga_ctx *c, gga_graph *g, const gga_params &p, b
     return frontier_scratch_ensure(&c->fs, out->v.n > d->n ? out->v.n : d->n, d->m);
 }
 
+gga_status gga_graph_prepare(gga_ctx *c, gga_graph *g, gga_algo algo) {
+    if (!c || !g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    if (algo != GGA_BFS && algo != GGA_SSSP) return gga_fail(GGA_ERR_INVALID_ARG, "unknown algorithm %d", (int)algo);
+    std::lock_guard<std::mutex> lk(c->mu);
+    gga_status s = ctx_activate(c);
+    if (!s) s = dev_graph_ensure(g, c->device, c->st);
+    FrontierPlan fp;
+    gga_params p = effective_params(c, g);
+    if (p.expansion == 1) p.use_split = 1;
+    if (!s) s = frontier_plan(c, g, p, algo == GGA_SSSP, &fp);
+    if (!s) s = dev_wait(c->st, 60.0);
+    return s;
+}
+
 gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_variant variant,
                      uint32_t *dist_out, gga_stats *stats) {
     const double t0 = gga_now_ms();
@@ -376,7 +402,14 @@ gga_status gga_solve(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src, gga_
     if ((s = ctx_activate(c))) return s;
     if ((s = dev_graph_ensure(g, c->device, c->st))) return s;
     const DevGraph *d = dev_graph_of(g);
-    const gga_params p = effective_params(c, g);
+    gga_params p = effective_params(c, g);
+    if (variant == GGA_VARIANT_AUTO && p.expansion == 2) { /* the autotuner picked the CDP variant */
+        variant = GGA_VARIANT_CDP_ATOMIC;
+        p.cdp_level = p.split_level ? p.split_level : 1;
+        p.cdp_buckets = p.split_buckets ? p.split_buckets : 10;
+    } else if (variant == GGA_VARIANT_AUTO && p.expansion == 1) { /* edge units over the split CSR */
+        p.use_split = 1;
+    }
     const bool sssp = algo == GGA_SSSP;
     const bool split = d->level != 0;
     gga_stats st;
@@ -498,7 +531,7 @@ gga_status gga_convergence(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t src
     ConvHook h;
     h.fin = fin;
     h.cnt = acc;
-    h.norm = (double *)(acc + 1);
+    h.norm = acc + 1;
     h.rec = records;
     h.cap = cap;
     h.n = 0;
@@ -563,7 +596,8 @@ gga_status gga_solve_many(gga_ctx *c, gga_graph *g, gga_algo algo, uint32_t n, c
     if ((s = ctx_activate(c))) return s;
     if ((s = dev_graph_ensure(g, c->device, c->st))) return s;
     const DevGraph *d = dev_graph_of(g);
-    const gga_params p = effective_params(c, g);
+    gga_params p = effective_params(c, g);
+    if (p.expansion == 1) p.use_split = 1; /* the autotuner's split view */
     const bool sssp = algo == GGA_SSSP;
     FrontierPlan fp;
     if ((s = frontier_plan(c, g, p, sssp, &fp))) return s;
@@ -674,64 +708,246 @@ gga_status gga_trace_get(gga_ctx *c, gga_round_trace *rounds, uint32_t cap, uint
 
 /* ------------------------------------------------------------ autotune */
 
+namespace {
+
+/* Timed trials of one candidate parameter set: kernel time (CUDA events) of
+ * solving `algo` from each source, `trials` times, on `variant`. */
+struct Tuner {
+    gga_ctx *c;
+    gga_graph *g;
+    uint32_t trials;
+    uint32_t srcs[2];
+    uint32_t nsrc;
+    uint32_t *tmp;
+    std::string log;
+
+    double time(const gga_params &p, gga_algo algo, gga_variant variant) {
+        c->params = p;
+        c->params_set = true;
+        double t = 0;
+        for (uint32_t k = 0; k < trials; ++k)
+            for (uint32_t i = 0; i < nsrc; ++i) {
+                gga_stats st;
+                if (gga_solve(c, g, algo, srcs[i], variant, tmp, &st)) return 1e30;
+                t += st.kernel_ms + st.aux_ms;
+            }
+        return t / trials;
+    }
+    void note(const char *key, double ms) {
+        char b[96];
+        snprintf(b, sizeof b, "%s\"%s\": %.4f", log.size() > 1 ? ", " : "", key, ms < 1e29 ? ms : -1.0);
+        log += b;
+    }
+};
+
+} // namespace
+
 gga_status gga_autotune(gga_ctx *c, gga_graph *g, uint32_t trials, gga_params *chosen) {
     if (!c || !g) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
     gga_params best = ctx_default_params(g);
     if (c->params_set) {
-        best.use_split = c->params.use_split;
         best.cdp_mode = c->params.cdp_mode;
         best.cdp_level = c->params.cdp_level ? c->params.cdp_level : best.cdp_level;
         best.cdp_buckets = c->params.cdp_buckets ? c->params.cdp_buckets : best.cdp_buckets;
     }
+    std::string report = "{";
     if (trials) {
-        /* time SSSP from the highest-degree vertex for a few bucket widths
-         * and CTA sizes; keep the fastest (all give identical distances) */
-        uint32_t src = 0, md = 0;
+        /* two sources: the highest-degree vertex and the vertex of median
+         * degree among those with edges */
+        Tuner T;
+        T.c = c;
+        T.g = g;
+        T.trials = trials;
+        T.nsrc = 0;
+        T.tmp = nullptr;
+        T.log = "{";
+        uint32_t md = 0, top = 0;
+        std::vector<uint32_t> degs;
+        degs.reserve(g->n);
         for (uint32_t u = 0; u < g->n; ++u) {
             const uint32_t dgr = g->off[u + 1] - g->off[u];
-            if (dgr > md) { md = dgr; src = u; }
+            if (dgr > md) { md = dgr; top = u; }
+            if (dgr) degs.push_back(dgr);
         }
-        uint32_t *tmp = nullptr;
+        T.srcs[T.nsrc++] = top;
+        if (!degs.empty()) {
+            std::nth_element(degs.begin(), degs.begin() + degs.size() / 2, degs.end());
+            const uint32_t med = degs[degs.size() / 2];
+            for (uint32_t u = 0; u < g->n; ++u)
+                if (u != top && g->off[u + 1] - g->off[u] == med) {
+                    T.srcs[T.nsrc++] = u;
+                    break;
+                }
+        }
+        const bool sssp_ok = g->maxw <= GGA_MAX_WEIGHT;
+        const int32_t level0 = g->split_level, buckets0 = g->split_buckets;
         {
             std::lock_guard<std::mutex> lk(c->mu);
             gga_status s = ctx_activate(c);
             if (!s) s = dev_graph_ensure(g, c->device, c->st);
             if (s) return s;
-            GGA_CK(cudaMalloc((void **)&tmp, (size_t)g->n * sizeof(uint32_t)));
+            GGA_CK(cudaMalloc((void **)&T.tmp, (size_t)g->n * sizeof(uint32_t)));
         }
+        const gga_params saved = c->params;
+        const bool saved_set = c->params_set;
+        char key[64];
+        /* 1. CTA size and SSSP bucket width (edge units, unsplit CSR) */
         const uint32_t base = ctx_profile_delta(g);
         const uint32_t deltas[] = {base / 4 ? base / 4 : 1, base / 2 ? base / 2 : 1, base * 3 / 4 ? base * 3 / 4 : 1,
                                    base, base * 3 / 2, base * 2, base * 4, 0};
-        const uint32_t sizes[] = {256, 512};
-        double best_ms = 1e30;
-        gga_params saved = c->params;
-        const bool saved_set = c->params_set;
-        for (uint32_t bs : sizes) {
+        double best_s = 1e30;
+        for (uint32_t bs : {256u, 512u})
             for (uint32_t dl : deltas) {
                 gga_params p = best;
                 p.block_threads = bs;
                 p.sssp_delta = dl;
-                c->params = p;
-                c->params_set = true;
-                double tsum = 0;
-                gga_status s = GGA_OK;
-                for (uint32_t t = 0; t < trials && !s; ++t) {
-                    gga_stats st;
-                    s = gga_solve(c, g, g->maxw <= GGA_MAX_WEIGHT ? GGA_SSSP : GGA_BFS, src, GGA_VARIANT_FRONTIER, tmp, &st);
-                    tsum += st.kernel_ms;
+                const double t = T.time(p, sssp_ok ? GGA_SSSP : GGA_BFS, GGA_VARIANT_FRONTIER);
+                snprintf(key, sizeof key, "sssp_bs%u_delta%u", bs, dl);
+                T.note(key, t);
+                if (t < best_s) {
+                    best_s = t;
+                    best = p;
                 }
-                if (!s && tsum < best_ms) {
-                    best_ms = tsum;
+            }
+        /* 2. BFS direction thresholds (bottom-up rounds need a symmetric graph) */
+        double best_b = T.time(best, GGA_BFS, GGA_VARIANT_FRONTIER);
+        T.note("bfs_alpha8_beta18", best_b);
+        const DevGraph *dg = dev_graph_of(g);
+        if (dg && dg->symmetric > 0) {
+            const uint32_t ab[][2] = {{4, 18}, {15, 18}, {30, 18}, {8, 12}, {8, 24}, {8, 48}};
+            for (const auto &x : ab) {
+                gga_params p = best;
+                p.bfs_alpha = x[0];
+                p.bfs_beta = x[1];
+                const double t = T.time(p, GGA_BFS, GGA_VARIANT_FRONTIER);
+                snprintf(key, sizeof key, "bfs_alpha%u_beta%u", x[0], x[1]);
+                T.note(key, t);
+                if (t < best_b) {
+                    best_b = t;
                     best = p;
                 }
             }
         }
+        /* 3. expansion strategy: BFS + SSSP time of edge units over the
+         * unsplit CSR, of the same units over the node-split CSR (histogram
+         * rule, ceil(maxdeg / level) for a few levels), and of the
+         * reference's CDP variant on small graphs */
+        double best_x = best_b + (sssp_ok ? best_s : 0.0);
+        T.note("expansion_edges_unsplit", best_x);
+        struct Split { int32_t level, buckets; };
+        std::vector<Split> splits;
+        uint32_t mda = 0;
+        if (md + 1 >= 10 && gga_max_allowed_out_degree(g, 10, &mda) == GGA_OK && mda) splits.push_back({-1, 10});
+        for (int32_t lv : {4, 16, 64})
+            if (md >= (uint32_t)lv * 2) splits.push_back({lv, 10});
+        int32_t split_pick = 0, split_pick_b = 10;
+        uint32_t x_pick = 0;
+        for (const Split &sp : splits) {
+            if (gga_node_split(c, g, sp.level, sp.buckets)) continue;
+            gga_params p = best;
+            p.use_split = 1;
+            const double t = T.time(p, GGA_BFS, GGA_VARIANT_FRONTIER) +
+                             (sssp_ok ? T.time(p, GGA_SSSP, GGA_VARIANT_FRONTIER) : 0.0);
+            snprintf(key, sizeof key, "expansion_edges_split_level%d", sp.level);
+            T.note(key, t);
+            if (t < best_x) {
+                best_x = t;
+                x_pick = 1;
+                split_pick = sp.level;
+                split_pick_b = sp.buckets;
+            }
+        }
+        if (g->m <= (1u << 21)) {
+            gga_node_split(c, g, 0, 10); /* CDP walks the unsplit graph */
+            for (int32_t lv : {-1, 1, 8}) {
+                if (lv < 0 && !(md + 1 >= 10)) continue;
+                gga_params p = best;
+                p.cdp_level = lv;
+                p.cdp_buckets = 10;
+                p.cdp_mode = 0;
+                const double t = T.time(p, GGA_BFS, GGA_VARIANT_CDP_ATOMIC) +
+                                 (sssp_ok ? T.time(p, GGA_SSSP, GGA_VARIANT_CDP_ATOMIC) : 0.0);
+                snprintf(key, sizeof key, "expansion_cdp_level%d", lv);
+                T.note(key, t);
+                if (t < best_x) {
+                    best_x = t;
+                    x_pick = 2;
+                    split_pick = lv;
+                    split_pick_b = 10;
+                }
+            }
+        }
+        best.expansion = x_pick;
+        best.split_level = x_pick ? split_pick : 0;
+        best.split_buckets = split_pick_b;
+        best.use_split = x_pick == 1 ? 1u : 0u;
+        /* leave the graph split as the pick needs it, else as it was */
+        if (x_pick == 1) gga_node_split(c, g, split_pick, split_pick_b);
+        else gga_node_split(c, g, level0, buckets0 ? buckets0 : 10);
         c->params = saved;
         c->params_set = saved_set;
-        cudaFree(tmp);
+        /* 4. the batch engine's bucket width: eight SSSP queries of this graph
+         * in one gga_multi_solve launch per candidate */
+        if (sssp_ok) {
+            const uint32_t nq = 8;
+            std::vector<uint32_t *> outs(nq, nullptr);
+            bool ok = true;
+            for (uint32_t i = 0; i < nq && ok; ++i)
+                ok = cudaMalloc((void **)&outs[i], (size_t)g->n * sizeof(uint32_t)) == cudaSuccess;
+            if (ok) {
+                std::vector<gga_query> qs(nq);
+                for (uint32_t i = 0; i < nq; ++i) {
+                    qs[i].graph = g;
+                    qs[i].algo = GGA_SSSP;
+                    qs[i].src = (uint32_t)(((uint64_t)i * 2654435761u) % g->n);
+                    qs[i].dist_out = outs[i];
+                }
+                double bt = 1e30;
+                uint32_t bpick = 0xFFFFFFFFu;
+                const int had = g->has_tuned;
+                const gga_params had_p = g->tuned;
+                for (uint32_t dl : {0u, base / 2 ? base / 2 : 1u, base, base * 2}) {
+                    g->tuned = best;
+                    g->tuned.batch_delta = dl;
+                    g->has_tuned = 1;
+                    double t = 0;
+                    for (uint32_t k = 0; k < trials; ++k) {
+                        gga_stats st;
+                        if (gga_multi_solve(c, nq, qs.data(), &st)) {
+                            t = 1e30;
+                            break;
+                        }
+                        t += st.kernel_ms;
+                    }
+                    snprintf(key, sizeof key, "batch_sssp8_delta%u", dl);
+                    T.note(key, t / trials);
+                    if (t < bt) {
+                        bt = t;
+                        bpick = dl;
+                    }
+                }
+                g->tuned = had_p;
+                g->has_tuned = had;
+                best.batch_delta = bpick;
+            }
+            cudaGetLastError();
+            for (uint32_t *o : outs) cudaFree(o);
+        }
+        cudaFree(T.tmp);
+        report = T.log;
     }
+    report += "}";
+    g->tuned = best;
+    g->has_tuned = 1;
     c->params = best;
     c->params_set = true;
+    c->tune_report = report;
     if (chosen) *chosen = best;
+    return GGA_OK;
+}
+
+gga_status gga_autotune_report(gga_ctx *c, char *buf, size_t len) {
+    if (!c || !buf || !len) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    snprintf(buf, len, "%s", c->tune_report.empty() ? "{}" : c->tune_report.c_str());
     return GGA_OK;
 }

@@ -12,7 +12,7 @@
  * improved-vertex frontier (Bellman-Ford order, per-query round stamps), and
  * both converge to the unique distances.
  *
- * The same engine runs in supersteps for the server (serve.cpp): a launch
+ * The same engine runs in supersteps for the server (serve.cu): a launch
  * processes at most `max_rounds` rounds and stops; between launches new
  * queries are initialised and injected into the next round's queue and
  * finished ones retired (continuous batching).
@@ -49,6 +49,12 @@ struct MqArgs {
     uint32_t nblocks;
     uint32_t max_rounds; /* rounds this launch may run */
     unsigned long long timeout_ns;
+    /* near-far mode: stop at the start of the first round in which fewer
+     * queries have work left than when the launch started (one finished) */
+    uint32_t stop_on_finish;
+    /* NULL, or (zeroed by the caller) per table slot: queue entries and far
+     * items the slot has when the launch stops (0: its answer is final) */
+    uint32_t *active;
 };
 
 __device__ __forceinline__ uint32_t *sel(uint32_t p, uint32_t *a, uint32_t *b) { return p ? b : a; }
@@ -64,6 +70,7 @@ struct MqCtrl {
     uint32_t unit, i0, cnt;
     uint32_t nitems, total;
     uint32_t ftot, fany;
+    uint32_t nact; /* near-far mode: queries with queue entries or far items this round */
     uint32_t fchunk; /* far-split ticket: its own field, because threads may still
                       * be reading `unit` for the expansion loop's exit test */
     uint32_t ws[32];
@@ -262,7 +269,7 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
     }
     __syncthreads();
     uint32_t round = ld_relaxed_u32(&ctl->round); /* fixed before launch */
-    uint32_t done = 0;
+    uint32_t done = 0, nact0 = 0;
     for (;; ++round, ++done) {
         const uint32_t r3 = round % 3, r3n = (round + 1) % 3, cur = round & 1, nxt = cur ^ 1;
         if (tid == 0) {
@@ -271,6 +278,7 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
             C.nitems = ni;
             C.total = ni ? (uint32_t)qc : 0u;
             C.fany = 0;
+            C.nact = 0;
         }
         __syncthreads();
         /* ---- this round's view of every query (near-far mode): one thread
@@ -280,11 +288,12 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
             const MqQuery &Q = a.qt[tid];
             MqQstate *st = a.qs + tid;
             uint32_t thr = NONE, old = NONE, tgt = 0;
+            const uint32_t nr = ld_relaxed_u32(&st->nr[r3]);
+            bool act = nr != 0;
             if (Q.algo == GGA_SSSP) {
                 const uint32_t par = round & 1;
                 thr = ld_relaxed_u32(&st->thr[par]);
                 const uint32_t fp = ld_relaxed_u32(&st->fp[par]) & 1u, cool = ld_relaxed_u32(&st->cool[par]);
-                const uint32_t nr = ld_relaxed_u32(&st->nr[r3]);
                 const uint32_t fc = min(ld_relaxed_u32(&st->fc[fp]), Q.n);
                 const uint32_t fm = ld_relaxed_u32(&st->fmin[fp]);
                 const uint32_t fpk = ld_relaxed_u32(&st->fpeak[par]);
@@ -299,18 +308,21 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
                 }
                 tgt = split ? fp ^ 1u : fp;
                 if (fc) atomicAdd(&C.fany, 1u);
+                act = act || fc != 0;
                 if (blockIdx.x == 0) {
                     st->thr[par ^ 1] = thr;
                     st->fp[par ^ 1] = tgt;
                     st->cool[par ^ 1] = split ? 1u : 0u;
                     st->fpeak[par ^ 1] = max(fpk, fc);
-                    st->nr[(round + 2) % 3] = 0; /* read two rounds ago, counted from next round */
-                    if (cool) {                  /* the pile split last round is free again */
+                    if (cool) { /* the pile split last round is free again */
                         st->fc[fp ^ 1] = 0;
                         st->fmin[fp ^ 1] = NONE;
                     }
                 }
             }
+            /* every query's round counter: read two rounds ago, counted from next round */
+            if (blockIdx.x == 0) st->nr[(round + 2) % 3] = 0;
+            if (act) atomicAdd(&C.nact, 1u);
             C.thr[tid] = thr;
             C.old[tid] = old;
             C.tgt[tid] = tgt;
@@ -328,9 +340,13 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
             ftot = C.ftot;
         }
         const uint32_t nitems = C.nitems, total = C.total, fany = a.nearfar ? C.fany : 0u;
+        const uint32_t nact = a.nearfar ? C.nact : 0u;
         const uint32_t units = min((uint32_t)(((uint64_t)total + MQ_UNIT - 1) / MQ_UNIT), a.ucap);
         __syncthreads();
-        if (done >= a.max_rounds || (units == 0 && fany == 0)) break; /* same decision in every block */
+        if (done == 0) nact0 = nact;
+        /* same decision in every block: the counters are the same everywhere */
+        if (done >= a.max_rounds || (units == 0 && fany == 0) || (a.stop_on_finish && a.nearfar && nact < nact0))
+            break;
         if (blockIdx.x == 0 && tid == 0) {
             ctl->qctr[(round + 2) % 3] = 0;
             ctl->work[(round + 2) % 3] = 0;
@@ -453,6 +469,22 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
         if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
     }
     if (tid == 0 && relaxed) atomicAdd(&ctl->edges_relaxed, relaxed);
+    /* what each slot still has when round `round` starts (k_mq_count's
+     * figures, without a second launch): that round's queue is complete, and
+     * the piles' counters are those round `round` reads */
+    if (a.active) {
+        const unsigned long long qc = ld_relaxed_u64(&ctl->qctr[round % 3]);
+        const uint32_t ni = min((uint32_t)(qc >> 32), a.cap);
+        const uint32_t *qq = sel(round & 1, a.qq0, a.qq1);
+        for (uint64_t i = (uint64_t)blockIdx.x * MQ_BS + tid; i < ni; i += (uint64_t)gridDim.x * MQ_BS)
+            atomicAdd(a.active + __ldcg(qq + i), 1u);
+        if (a.nearfar && blockIdx.x == 0)
+            for (uint32_t q = tid; q < a.nq; q += MQ_BS) {
+                const MqQstate &st = a.qs[q];
+                const uint32_t fc = ld_relaxed_u32(&st.fc[ld_relaxed_u32(&st.fp[round & 1]) & 1u]);
+                if (fc) atomicAdd(a.active + q, fc);
+            }
+    }
     if (blockIdx.x == 0 && tid == 0) {
         ctl->round = round;
         ctl->rounds_done += done;
@@ -692,15 +724,24 @@ gga_status mq_engine_admit(MqEngine *e, const MqQuery *host_q, const uint32_t *s
 }
 
 gga_status mq_engine_run(MqEngine *e, uint32_t max_rounds, cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1,
-                         uint32_t *rounds_run, float *ms) {
+                         uint32_t *rounds_run, float *ms, bool superstep) {
     MqArgs a = mq_args(e);
     a.max_rounds = max_rounds;
+    if (superstep) {
+        a.stop_on_finish = 1;
+        a.active = e->active;
+        const uint32_t ns = std::min(e->nslots, e->qcap);
+        GGA_CK(cudaMemsetAsync(e->active, 0, (size_t)(ns ? ns : 1) * sizeof(uint32_t), st));
+    }
     GGA_CK(cudaMemsetAsync(&e->ctl->bar, 0, sizeof(GridBarrier), st));
     if (ev0) GGA_CK(cudaEventRecord(ev0, st));
     void *args[] = {&a};
     GGA_CK(cudaLaunchCooperativeKernel((const void *)k_mq, dim3(a.nblocks), dim3(MQ_BS), args, mq_smem(), st));
     if (ev1) GGA_CK(cudaEventRecord(ev1, st));
     GGA_CK(cudaMemcpyAsync(e->hctl, e->ctl, sizeof(MqCtl), cudaMemcpyDeviceToHost, st));
+    if (superstep && e->nslots)
+        GGA_CK(cudaMemcpyAsync(e->hactive, e->active, (size_t)std::min(e->nslots, e->qcap) * sizeof(uint32_t),
+                               cudaMemcpyDeviceToHost, st));
     gga_status s = dev_wait(st, 60.0);
     if (s) return s;
     const MqCtl &h = *e->hctl;
@@ -833,7 +874,7 @@ gga_status gga_multi_solve(gga_ctx *c, uint32_t nq, const gga_query *queries, gg
         r.m = d->m;
         r.algo = q.algo;
         r.src = q.src;
-        r.delta = q.algo == GGA_SSSP ? ctx_profile_delta(q.graph) : 0;
+        r.delta = q.algo == GGA_SSSP ? ctx_batch_delta(q.graph) : 0;
         r.tail_at = r.delta && (uint64_t)d->m >= 8ull * d->n ? d->n / 4 : 0; /* as in the single-source engine */
         mq_state_layout(&r, b->pool + at);
         at += mq_state_words(d->n, q.algo);

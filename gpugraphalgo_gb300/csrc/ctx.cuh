@@ -3,6 +3,7 @@
  */
 #pragma once
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "frontier.cuh"
@@ -45,6 +46,7 @@ struct gga_ctx {
     bool trace_on = false;
     std::vector<uint32_t> trace_rounds; /* 5 words per round of the last traced solve */
     std::vector<uint32_t> trace_cta;    /* busy kilocycles per CTA */
+    std::string tune_report;            /* JSON of the last gga_autotune's trials */
     std::mutex mu;
 };
 
@@ -53,6 +55,9 @@ gga_params ctx_default_params(const gga_graph *g);
 /* SSSP bucket width from g's degree profile (never 0): the batch engines'
  * width, whose rounds are shared by many queries. */
 uint32_t ctx_profile_delta(const gga_graph *g);
+/* SSSP bucket width of g's queries in the batch engine (autotuned, else the
+ * profile width). */
+uint32_t ctx_batch_delta(const gga_graph *g);
 gga_status ctx_validate_solve(const gga_graph *g, gga_algo algo, uint32_t src);
 gga_status ctx_finish_output(gga_ctx *c, const DevGraph *d, const uint32_t *dev_out, uint32_t *dist_out,
                              gga_stats *stats);

@@ -18,6 +18,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+
 #include "gga_device.cuh"
 
 #include <time.h>
@@ -141,34 +143,120 @@ GraphView dev_graph_view(const DevGraph *d, bool split) {
 
 static unsigned grid_for(uint64_t items, unsigned bs);
 
-__global__ void k_light_flags(const uint32_t *wt, uint32_t m, uint32_t delta, uint32_t *flags) {
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x)
-        flags[e] = wt[e] < delta ? 1u : 0u;
-}
+/* Light-first row order for bucket width delta (delta-stepping's edge
+ * classes, Meyer & Sanders): within each row the edges with w < delta come
+ * first, then the rest, each class in its original order; light[u] counts
+ * the row's light edges.  A stable two-way partition per row:
+ *   k_lh_rows: one warp per row of at most LH_WARP_MAX edges: a first pass
+ *     counts the light edges (one ballot per 32 edges), a second writes each
+ *     edge at its rank among its class (ballot + popc); longer rows are
+ *     listed in `big` for
+ *   k_lh_big: one CTA per long row, the same two passes with a CTA-wide rank
+ *     (per-warp ballot counts scanned in shared memory) per 32 x warps edges.
+ * Loop bounds are warp- (CTA-) uniform; every collective is reached by the
+ * whole warp (CTA).  nlight accumulates the light edges of the graph. */
+constexpr uint32_t LH_WARP_MAX = 4096;
+constexpr unsigned LH_BIG_BS = 1024;
 
-/* Edge e of row u moves to off[u] + (its rank among the row's light edges)
- * when light, else to off[u] + light(u) + (its rank among the heavy ones);
- * ranks come from the exclusive scan `pos` of the light flags. */
-__global__ void k_lh_scatter(const uint32_t *off, const uint32_t *col, const uint32_t *wt, uint32_t n, uint32_t m,
-                             uint32_t delta, const uint32_t *pos, uint32_t *lcol, uint32_t *lwt) {
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t lo = 0, hi = n; /* row of e: largest u with off[u] <= e */
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (off[mid] <= e) lo = mid; else hi = mid;
+__global__ void k_lh_rows(const uint32_t *off, const uint32_t *col, const uint32_t *wt, uint32_t n, uint32_t delta,
+                          uint32_t *lcol, uint32_t *lwt, uint32_t *light, uint32_t *big, uint32_t *nbig,
+                          unsigned long long *nlight) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t w0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long mine = 0;
+    for (uint64_t u = w0; u < n; u += nw) {
+        const uint32_t b = off[u], e = off[u + 1];
+        if (e - b > LH_WARP_MAX) {
+            if (lane == 0) big[atomicAdd(nbig, 1u)] = (uint32_t)u;
+            continue;
         }
-        const uint32_t b = off[lo], lrank = pos[e] - pos[b];
-        uint32_t dst;
-        if (wt[e] < delta) dst = b + lrank;
-        else dst = b + (pos[off[lo + 1]] - pos[b]) + ((uint32_t)e - b - lrank);
-        lcol[dst] = col[e];
-        lwt[dst] = wt[e];
+        uint32_t nl = 0;
+        for (uint64_t k0 = b; k0 < e; k0 += 32) { /* 64-bit: no wrap near 2^32 edges */
+            const uint64_t k = k0 + lane;
+            nl += __popc(__ballot_sync(FULL, k < e && wt[k] < delta));
+        }
+        uint32_t lp = b, hp = b + nl;
+        for (uint64_t k0 = b; k0 < e; k0 += 32) {
+            const uint64_t k = k0 + lane;
+            const bool in = k < e;
+            const uint32_t w = in ? wt[k] : 0u, c = in ? col[k] : 0u;
+            const bool l = in && w < delta;
+            const uint32_t lm = __ballot_sync(FULL, l), hm = __ballot_sync(FULL, in && !l);
+            const uint32_t lt = (1u << lane) - 1u;
+            if (in) {
+                const uint32_t p = l ? lp + __popc(lm & lt) : hp + __popc(hm & lt);
+                lcol[p] = c;
+                lwt[p] = w;
+            }
+            lp += __popc(lm);
+            hp += __popc(hm);
+        }
+        if (lane == 0) {
+            light[u] = nl;
+            mine += nl;
+        }
     }
+    if (lane == 0 && mine) atomicAdd(nlight, mine);
 }
 
-__global__ void k_light_counts(const uint32_t *off, uint32_t n, const uint32_t *pos, uint32_t *light) {
-    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (uint64_t)gridDim.x * blockDim.x)
-        light[u] = pos[off[u + 1]] - pos[off[u]];
+__global__ void __launch_bounds__(LH_BIG_BS) k_lh_big(const uint32_t *off, const uint32_t *col, const uint32_t *wt,
+                                                      uint32_t delta, const uint32_t *big, const uint32_t *nbig,
+                                                      uint32_t *lcol, uint32_t *lwt, uint32_t *light,
+                                                      unsigned long long *nlight) {
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr uint32_t NWARP = LH_BIG_BS / 32;
+    __shared__ uint32_t s_l[NWARP], s_h[NWARP], s_tot;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t rows = *nbig;
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const uint32_t u = big[r], b = off[u], e = off[u + 1];
+        uint32_t cnt = 0;
+        for (uint64_t k = b + threadIdx.x; k < e; k += LH_BIG_BS) cnt += wt[k] < delta;
+        for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(FULL, cnt, d);
+        if (threadIdx.x == 0) s_tot = 0;
+        __syncthreads();
+        if (lane == 0) atomicAdd(&s_tot, cnt);
+        __syncthreads();
+        const uint32_t nl = s_tot;
+        uint32_t lp = b, hp = b + nl;
+        for (uint64_t k0 = b; k0 < e; k0 += LH_BIG_BS) {
+            const uint64_t k = k0 + threadIdx.x;
+            const bool in = k < e;
+            const uint32_t w = in ? wt[k] : 0u, c = in ? col[k] : 0u;
+            const bool l = in && w < delta;
+            const uint32_t lm = __ballot_sync(FULL, l), hm = __ballot_sync(FULL, in && !l);
+            if (lane == 0) {
+                s_l[warp] = __popc(lm);
+                s_h[warp] = __popc(hm);
+            }
+            __syncthreads();
+            uint32_t bl = 0, bh = 0, tl = 0, th = 0; /* ranks before this warp, totals of the chunk */
+            for (uint32_t q = 0; q < NWARP; ++q) {
+                if (q < warp) {
+                    bl += s_l[q];
+                    bh += s_h[q];
+                }
+                tl += s_l[q];
+                th += s_h[q];
+            }
+            const uint32_t lt = (1u << lane) - 1u;
+            if (in) {
+                const uint32_t p = l ? lp + bl + __popc(lm & lt) : hp + bh + __popc(hm & lt);
+                lcol[p] = c;
+                lwt[p] = w;
+            }
+            lp += tl;
+            hp += th;
+            __syncthreads(); /* s_l / s_h are rewritten by the next chunk */
+        }
+        if (threadIdx.x == 0) {
+            light[u] = nl;
+            atomicAdd(nlight, (unsigned long long)nl);
+        }
+        __syncthreads(); /* s_tot is reset by the next row */
+    }
 }
 
 gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st) {
@@ -191,25 +279,31 @@ gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st) 
         GGA_CK(cudaMemsetAsync(d->lwt + d->m, 0, (mpad - d->m) * sizeof(uint32_t), st));
     }
     d->lh_delta = 0;
-    uint32_t *flags = nullptr;
-    GGA_CK(cudaMallocAsync((void **)&flags, ((size_t)d->m + 1) * 2 * sizeof(uint32_t), st));
-    uint32_t *pos = flags + d->m + 1;
-    const unsigned grid = grid_for(d->m ? d->m : 1, 256);
-    k_light_flags<<<grid, 256, 0, st>>>(d->wt, d->m, delta, flags);
-    gga_status s = dev_exclusive_scan(flags, pos, d->m, st);
-    uint32_t nlight = 0;
-    if (s == GGA_OK) {
-        e = cudaMemcpyAsync(&nlight, pos + d->m, sizeof nlight, cudaMemcpyDeviceToHost, st);
-        if (d->m) k_lh_scatter<<<grid, 256, 0, st>>>(d->off, d->col, d->wt, d->n, d->m, delta, pos, d->lcol, d->lwt);
-        k_light_counts<<<grid_for(d->n ? d->n : 1, 256), 256, 0, st>>>(d->off, d->n, pos, d->light);
-        if (e == cudaSuccess) e = cudaGetLastError();
-        if (e != cudaSuccess) s = gga_fail(GGA_ERR_CUDA, "light/heavy order: %s", cudaGetErrorString(e));
+    /* scratch: the long-row list (at most m / LH_WARP_MAX rows), its count and the light total */
+    const size_t nbig_cap = (size_t)d->m / LH_WARP_MAX + 1;
+    uint32_t *scr = nullptr;
+    GGA_CK(cudaMallocAsync((void **)&scr, (nbig_cap + 4) * sizeof(uint32_t), st));
+    uint32_t *nbig = scr, *big = scr + 4;
+    unsigned long long *nlight = (unsigned long long *)(scr + 2);
+    gga_status s = gga_cuda_check(cudaMemsetAsync(scr, 0, 4 * sizeof(uint32_t), st));
+    if (s == GGA_OK && d->n) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d->device);
+        const uint64_t want_warps = d->n;
+        const unsigned grid = (unsigned)std::min<uint64_t>((want_warps + 7) / 8, (uint64_t)(sms > 0 ? sms : 1) * 16);
+        k_lh_rows<<<grid ? grid : 1, 256, 0, st>>>(d->off, d->col, d->wt, d->n, delta, d->lcol, d->lwt, d->light, big,
+                                                    nbig, nlight);
+        k_lh_big<<<(sms > 0 ? sms : 1) * 2, LH_BIG_BS, 0, st>>>(d->off, d->col, d->wt, delta, big, nbig, d->lcol,
+                                                                 d->lwt, d->light, nlight);
+        s = gga_cuda_check(cudaGetLastError());
     }
-    cudaFreeAsync(flags, st);
+    unsigned long long hl = 0;
+    if (s == GGA_OK) s = gga_cuda_check(cudaMemcpyAsync(&hl, nlight, sizeof hl, cudaMemcpyDeviceToHost, st));
+    cudaFreeAsync(scr, st);
     if (s) return s;
     if ((s = dev_wait(st, 60.0))) return s;
     d->lh_delta = delta;
-    d->lh_heavy = d->m - nlight;
+    d->lh_heavy = d->m - (uint32_t)hl;
     return GGA_OK;
 }
 

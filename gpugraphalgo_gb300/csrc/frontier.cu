@@ -80,6 +80,7 @@ struct Args {
     /* bucket closes by pull (every edge's reverse has its weight): 0 never,
      * 1 when the cost rule picks it, 2 always */
     uint32_t pull;
+    uint32_t *pbest; /* cap: per pull-list entry, the smallest offer its edges found (NONE: none) */
     uint32_t heavy_edges; /* edges with w >= delta */
     /* SSSP: when a bucket opens with at most this many far-pile entries, the
      * threshold goes to infinity and the rest runs as one label-correcting
@@ -451,6 +452,7 @@ __device__ __forceinline__ void pull_scan(const Args &a, uint32_t thr, uint32_t 
         for (uint32_t q = 0; q < PV; ++q)
             if (hd[q]) {
                 put_entry(a, i, o, (uint32_t)(v0 + 32 * q), b[q], hd[q], qv, qo, qb, uf);
+                if (i < a.cap) a.pbest[i] = NONE; /* the pull round's offers meet here */
                 ++i;
                 o += hd[q];
             }
@@ -475,8 +477,10 @@ __device__ __forceinline__ void pull_scan(const Args &a, uint32_t thr, uint32_t 
  * an edge whose other end u is settled (d(u) < settled) offers d(u) + w to
  * the entry's vertex.  The offers meet in shared memory first (one shared
  * atomicMin per edge into the entry's slot of t_best, which follows t_du),
- * and each entry then makes one global atomicMin, instead of one per edge
- * with a vertex's edges contending for its word. */
+ * and each entry's best then goes to its pbest word with one fire-and-forget
+ * atomicMin (an entry cut by a unit boundary gets one per unit).  Nothing is
+ * returned or staged here, so a unit's chain ends at its probes; pull_apply
+ * turns the pbest words into distance updates after a grid barrier. */
 template <int BS, bool SSSP, bool PULL = false>
 __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage &S, uint32_t *t_o, uint32_t *t_b,
                                              uint32_t *t_du, const uint32_t *qv, const uint32_t *qo,
@@ -566,17 +570,21 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                         if (t_o[mid] <= e) lo = mid; else hi = mid;
                     }
                     const uint32_t ei = t_b[lo] + (e - t_o[lo]);
-                    if (ei < a.m) {
+                    if (ei >= a.m) { /* unreachable by construction; keeps reads in bounds */
+                        set_err(ctl, GGA_DEV_BAD_EDGE);
+                        act[q] = false;
+                    } else {
                         v[q] = __ldg(a.col + ei);
-                        if (PULL) {
+                        if (v[q] >= a.n) { /* a target outside the graph (malformed CSR): no access */
+                            set_err(ctl, GGA_DEV_BAD_TARGET);
+                            act[q] = false;
+                            v[q] = 0;
+                        } else if (PULL) {
                             alt[q] = __ldg(a.wt + ei);
                             tgt[q] = lo;
                         } else {
                             alt[q] = SSSP ? t_du[lo] + __ldg(a.wt + ei) : round + 1;
                         }
-                    } else { /* unreachable by construction; keeps reads in bounds */
-                        set_err(ctl, GGA_DEV_BAD_EDGE);
-                        act[q] = false;
                     }
                 }
             }
@@ -654,18 +662,11 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
                     }
             }
         }
-        if (PULL) { /* each entry's best offer, once */
+        if (PULL) { /* each entry's best offer, to its pbest word (result unused: a reduction) */
             __syncthreads();
             for (uint32_t j = tid; j < cnt; j += BS) {
-                const uint32_t best = t_best[j], vq = t_du[j];
-                if (best == NONE || best >= atomicMin(a.dist + vq, best)) continue;
-                if (best < thr) {
-                    if (atomicExch(a.stamp + vq, round + 1) != round + 1) stage_near(a, C, S.sv, vq);
-                } else {
-                    atomicMin(&C.fmin, best);
-                    const uint32_t bit = 1u << (vq & 31);
-                    if (!(atomicOr(a.farbits + (vq >> 5), bit) & bit)) stage_far(a, C, S.sf, vq);
-                }
+                const uint32_t best = t_best[j];
+                if (best != NONE) atomicMin(a.pbest + i0 + j, best);
             }
         }
         if (tid == 0) relaxed += eend - ebase;
@@ -713,6 +714,46 @@ __device__ __forceinline__ void split_pile(const Args &a, Ctrl &C, const Stage &
                 atomicAnd(a.farbits + (v[q] >> 5), ~(1u << (v[q] & 31)));
                 if (d[q] >= thr_old && atomicExch(a.stamp + v[q], round + 1) != round + 1)
                     stage_near(a, C, S.sv, v[q]);
+            }
+        }
+        checkpoint<BS, true>(a, C, S, nxt, r3n, fq, bucket, BS);
+    }
+}
+
+/* Second half of a pull round (SSSP): every pull-list entry whose edges
+ * found an offer (pbest, complete after the grid barrier that follows the
+ * expansion) makes one atomicMin on its vertex's distance; an improvement
+ * below thr joins the next round's near queue (once, by round stamp), one
+ * at or above it the far pile fq.  A streaming pass over the list, PE
+ * entries per thread in flight; block-uniform, with the same checkpoints as
+ * split_pile (the caller publishes the last stage). */
+template <int BS>
+__device__ __forceinline__ void pull_apply(const Args &a, Ctrl &C, const Stage &S, const uint32_t *qv, uint32_t nitems,
+                                           uint32_t thr, uint32_t round, uint32_t nxt, uint32_t r3n, uint32_t fq,
+                                           uint32_t bucket) {
+    const uint32_t tid = threadIdx.x;
+    constexpr uint32_t PE = STAGE_BATCH;
+    const uint64_t gstep = (uint64_t)gridDim.x * BS * PE;
+    for (uint64_t base = (uint64_t)blockIdx.x * BS * PE; base < nitems; base += gstep) {
+        uint32_t v[PE], b[PE], old[PE];
+#pragma unroll
+        for (uint32_t q = 0; q < PE; ++q) {
+            const uint64_t i = base + q * BS + tid;
+            v[q] = i < nitems ? __ldcg(qv + i) : 0u;
+            b[q] = i < nitems ? __ldcg(a.pbest + i) : NONE;
+        }
+#pragma unroll
+        for (uint32_t q = 0; q < PE; ++q) old[q] = b[q] != NONE ? atomicMin(a.dist + v[q], b[q]) : 0u;
+#pragma unroll
+        for (uint32_t q = 0; q < PE; ++q) {
+            if (b[q] == NONE || b[q] >= old[q]) continue;
+            const uint32_t vq = v[q];
+            if (b[q] < thr) {
+                if (atomicExch(a.stamp + vq, round + 1) != round + 1) stage_near(a, C, S.sv, vq);
+            } else {
+                atomicMin(&C.fmin, b[q]);
+                const uint32_t bit = 1u << (vq & 31);
+                if (!(atomicOr(a.farbits + (vq >> 5), bit) & bit)) stage_far(a, C, S.sf, vq);
             }
         }
         checkpoint<BS, true>(a, C, S, nxt, r3n, fq, bucket, BS);
@@ -965,6 +1006,9 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : (BS >= 512 ? 2 : 4)) k_fr
             expand_units<BS, SSSP, true>(a, C, S, t_o, t_b, t_du, sel(cur, a.qv0, a.qv1), sel(cur, a.qo0, a.qo1),
                                          sel(cur, a.qb0, a.qb1), sel(cur, a.uf0, a.uf1), nitems, total, units, round,
                                          thr, thr_old, nxt, r3n, fq, bucket, relaxed);
+            /* every unit's offers are in the pbest words before any is applied */
+            if (!grid_barrier(&ctl->bar, &ctl->err, a.nblocks, gen, a.timeout_ns)) break;
+            pull_apply<BS>(a, C, S, sel(cur, a.qv0, a.qv1), nitems, thr, round, nxt, r3n, fq, bucket);
             split_pile<BS>(a, C, S, fp, fq, fc, thr, thr_old, round, nxt, r3n, bucket);
             publish_far(fq);
             if (a.trace && tid == 0) busy += clock64() - t_round;
@@ -1053,7 +1097,7 @@ void frontier_scratch_free(FrontierScratch *s) {
     cudaFree(s->qv0); cudaFree(s->qv1); cudaFree(s->qo0); cudaFree(s->qo1); cudaFree(s->qb0); cudaFree(s->qb1);
     cudaFree(s->uf0); cudaFree(s->uf1);
     cudaFree(s->far0); cudaFree(s->far1); cudaFree(s->far2);
-    cudaFree(s->out); cudaFree(s->ctl); cudaFree(s->trace); cudaFree(s->hstamp);
+    cudaFree(s->out); cudaFree(s->ctl); cudaFree(s->trace); cudaFree(s->hstamp); cudaFree(s->pbest);
     for (int i = 0; i < 3; ++i) {
         cudaFree(s->hv[i]); cudaFree(s->ho[i]); cudaFree(s->hb[i]); cudaFree(s->huf[i]);
     }
@@ -1074,7 +1118,7 @@ gga_status frontier_scratch_ensure(FrontierScratch *s, uint32_t n, uint32_t m) {
         (st = alloc_u32(&s->qo1, cap)) || (st = alloc_u32(&s->qb0, cap)) || (st = alloc_u32(&s->qb1, cap)) ||
         (st = alloc_u32(&s->uf0, ucap)) || (st = alloc_u32(&s->uf1, ucap)) ||
         (st = alloc_u32(&s->far0, cap)) || (st = alloc_u32(&s->far1, cap)) || (st = alloc_u32(&s->far2, cap)) ||
-        (st = alloc_u32(&s->out, cap)) || (st = alloc_u32(&s->hstamp, cap)) ||
+        (st = alloc_u32(&s->out, cap)) || (st = alloc_u32(&s->hstamp, cap)) || (st = alloc_u32(&s->pbest, cap)) ||
         (st = alloc_u32(&s->hv[0], cap)) || (st = alloc_u32(&s->hv[1], cap)) || (st = alloc_u32(&s->hv[2], cap)) ||
         (st = alloc_u32(&s->ho[0], cap)) || (st = alloc_u32(&s->ho[1], cap)) || (st = alloc_u32(&s->ho[2], cap)) ||
         (st = alloc_u32(&s->hb[0], cap)) || (st = alloc_u32(&s->hb[1], cap)) || (st = alloc_u32(&s->hb[2], cap)) ||
@@ -1141,6 +1185,7 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     if (sssp && lh.light && a.delta) {
         a.light = lh.light;
         a.pull = lh.pull;
+        a.pbest = s->pbest;
         a.heavy_edges = lh.heavy_edges;
         a.hstamp = s->hstamp;
         a.hv0 = s->hv[0]; a.hv1 = s->hv[1]; a.hv2 = s->hv[2];
@@ -1193,6 +1238,7 @@ gga_status frontier_verdict(const FrontierCtl &h) {
         return gga_fail(GGA_ERR_TIMEOUT, "frontier grid barrier timed out after %u rounds", h.rounds);
     if (h.err == GGA_DEV_OVERFLOW) return gga_fail(GGA_ERR_CUDA, "frontier queue overflow (internal error)");
     if (h.err == GGA_DEV_ROUND_LIMIT) return gga_fail(GGA_ERR_CUDA, "frontier round limit reached (internal error)");
+    if (h.err == GGA_DEV_BAD_TARGET) return gga_fail(GGA_ERR_FORMAT, "malformed CSR: an edge target is >= n");
     if (h.err == GGA_DEV_OVERFLOW_UNITS) return gga_fail(GGA_ERR_CUDA, "frontier unit table overflow (internal error)");
     if (h.err == GGA_DEV_OVERFLOW_FAR) return gga_fail(GGA_ERR_CUDA, "frontier far pile overflow (internal error)");
     if (h.err == GGA_DEV_BAD_EDGE)
@@ -1225,7 +1271,11 @@ gga_status frontier_verdict(const FrontierCtl &h) {
  * threads, or different streams without ordering between them) race and
  * corrupt each other's results; serialise them.  The first call on each
  * device looks up the array's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture begins.
+ * make that first call before any stream capture begins.  Each call is
+ * synchronous: it returns once the traversal on `stream` has finished.  The
+ * caller's CSR is not validated on the host (it is device memory): a column
+ * id >= n is caught in the kernel, which skips that edge and makes the call
+ * return GGA_ERR_FORMAT.
  * ------------------------------------------------------------------------ */
 
 
@@ -1318,6 +1368,8 @@ extern "C" gga_status gga_bfs_noalloc(const uint32_t *d_offsets, const uint32_t 
     GGA_CK(cudaMemcpyAsync(&err, &ctl->err, sizeof err, cudaMemcpyDeviceToHost, st));
     GGA_CK(cudaStreamSynchronize(st));
     if (err == GGA_DEV_TIMEOUT) return gga_fail(GGA_ERR_TIMEOUT, "gga_bfs_noalloc: grid barrier timed out");
+    if (err == GGA_DEV_BAD_TARGET)
+        return gga_fail(GGA_ERR_FORMAT, "gga_bfs_noalloc: malformed CSR: an edge target is >= n (%u)", n);
     if (err != GGA_DEV_OK) return gga_fail(GGA_ERR_CUDA, "gga_bfs_noalloc: kernel error %u", err);
     return GGA_OK;
 }

@@ -35,6 +35,7 @@ struct FrontierScratch {
     uint32_t *out;       /* cap: gathered original-order output */
     uint32_t *trace;     /* (TRACE_ROUNDS + 1) round records + per-CTA busy kilocycles */
     uint32_t *hstamp;    /* cap: SSSP light/heavy mode, bucket a vertex last joined a heavy list */
+    uint32_t *pbest;     /* cap: SSSP pull rounds, the best offer per pull-list entry */
     uint32_t *hv[3], *ho[3], *hb[3], *huf[3]; /* heavy lists (cap, cap, cap, ucap) */
     FrontierCtl *ctl;
     FrontierCtl *hctl;   /* pinned host mirror (keeps the read-back asynchronous) */

@@ -61,7 +61,7 @@ struct DevGraph {
 struct ConvHook {
     const uint32_t *fin;     /* device: final distances of the original vertices */
     unsigned long long *cnt; /* device: vertices that differ (one launch) */
-    double *norm;            /* device: sum of the squared differences */
+    unsigned long long *norm; /* device: sum of the squared differences (each < 2^32, so exact in 64 bits) */
     gga_conv_record *rec;    /* host: records, room for cap */
     uint32_t cap, n;         /* n: iterations logged */
 };
@@ -85,7 +85,8 @@ enum : uint32_t {
     GGA_DEV_OVERFLOW_UNITS = 4,
     GGA_DEV_OVERFLOW_FAR = 5,
     GGA_DEV_BAD_EDGE = 6,
-    GGA_DEV_ROUND_LIMIT = 7
+    GGA_DEV_ROUND_LIMIT = 7,
+    GGA_DEV_BAD_TARGET = 8 /* an edge's target id is >= n (malformed caller CSR) */
 };
 
 /* ---- small device helpers ---------------------------------------------- */

@@ -40,6 +40,10 @@ struct gga_graph {
     uint32_t ns;                    /* split vertex count n' */
     uint32_t parents_with_children; /* myParentCount */
 
+    /* parameters gga_autotune picked for this graph (has_tuned != 0) */
+    gga_params tuned;
+    int has_tuned;
+
     /* device residency, owned; see device_graph.cu */
     void *dev;
     int dev_device;

@@ -3,12 +3,16 @@
  *
  * The reference serves nothing: one process answers one source
  * (bfs_sssp.cu:103-539).  A server keeps its graphs resident and runs the
- * batch engine (batch.cu) in supersteps of a few rounds on its own stream.
- * Between supersteps the loop
- *   - counts every in-flight query's queue entries (one small kernel) and
- *     retires the queries that have none left: their distances are final
+ * batch engine (batch.cu) in supersteps on its own stream.  A superstep
+ * ends at the first round in which one of the in-flight queries has
+ * finished (or after SUPERSTEP_MAX_ROUNDS rounds, so queries that arrive
+ * meanwhile wait a bounded time); the launch itself leaves every slot's
+ * remaining queue entries and far items in a pinned array.  Between
+ * supersteps the loop
+ *   - retires the queries that have none left: their distances are final
  *     (improved-vertex frontier / BFS levels), so they are copied to the
- *     caller's buffer and the ticket completes;
+ *     callers' buffers (all copies queued, one wait) and the tickets
+ *     complete;
  *   - admits waiting queries while a slot is free and their device state fits:
  *     distances + visited bits or round stamps from a pool, queue room for one
  *     entry per vertex, and unit-table room for their edges.  The pool, the
@@ -32,7 +36,7 @@
 
 namespace {
 
-constexpr uint32_t SUPERSTEP_ROUNDS = 8;
+constexpr uint32_t SUPERSTEP_MAX_ROUNDS = 128;
 constexpr uint32_t QUEUE_BYTES_PER_VERTEX = 32; /* 4 arrays x 2 buffers x 4 bytes */
 
 struct Request {
@@ -221,8 +225,8 @@ void server_loop(gga_server *s) {
         gga_status st = mq_engine_admit(&s->eng, hq.data(), hslots.data(), (uint32_t)hq.size(), s->st);
         /* ---- one superstep */
         uint32_t rounds = 0;
-        if (st == GGA_OK) st = mq_engine_run(&s->eng, SUPERSTEP_ROUNDS, s->st, nullptr, nullptr, &rounds, nullptr);
-        if (st == GGA_OK) st = mq_engine_count(&s->eng, s->max_slots, s->st);
+        if (st == GGA_OK)
+            st = mq_engine_run(&s->eng, SUPERSTEP_MAX_ROUNDS, s->st, nullptr, nullptr, &rounds, nullptr, true);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             s->stats.supersteps++;
@@ -231,16 +235,23 @@ void server_loop(gga_server *s) {
             fail_all(s, st);
             continue;
         }
-        /* ---- retire finished queries */
+        /* ---- retire finished queries: every copy queued, then one wait */
+        std::vector<uint32_t> fin;
+        cudaError_t e = cudaSuccess;
         for (uint32_t i = 0; i < s->max_slots; ++i) {
             Slot &sl = s->slots[i];
             if (!sl.busy || s->eng.hactive[i] != 0) continue;
-            const Request rq = sl.rq;
-            gga_status cs = GGA_OK;
-            cudaError_t e = cudaMemcpyAsync(rq.out, s->pool + sl.pool_off, (size_t)sl.n * sizeof(uint32_t),
-                                            cudaMemcpyDefault, s->st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-            if (e != cudaSuccess) cs = gga_fail(GGA_ERR_CUDA, "server result copy: %s", cudaGetErrorString(e));
+            fin.push_back(i);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(sl.rq.out, s->pool + sl.pool_off, (size_t)sl.n * sizeof(uint32_t),
+                                    cudaMemcpyDefault, s->st);
+        }
+        if (!fin.empty() && e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        for (uint32_t i : fin) {
+            const Request rq = s->slots[i].rq;
+            const gga_status cs = e == cudaSuccess
+                                      ? GGA_OK
+                                      : gga_fail(GGA_ERR_CUDA, "server result copy: %s", cudaGetErrorString(e));
             release_slot(s, i);
             finish(s, rq, cs);
         }
@@ -290,7 +301,7 @@ gga_status gga_server_create(gga_ctx *c, uint32_t ngraphs, gga_graph *const *gra
     for (uint32_t i = 0; i < ngraphs; ++i) {
         sv->graphs.push_back(graphs[i]);
         sv->dgraphs.push_back(dev_graph_of(graphs[i]));
-        sv->delta.push_back(ctx_profile_delta(graphs[i]));
+        sv->delta.push_back(ctx_batch_delta(graphs[i]));
         max_n = std::max<uint64_t>(max_n, graphs[i]->n);
         max_m = std::max<uint64_t>(max_m, graphs[i]->m);
     }

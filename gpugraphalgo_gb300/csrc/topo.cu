@@ -194,15 +194,18 @@ struct TopoResult {
 /* printConv_rtime (convergence.h:100-159) on the device: over the original
  * vertices u, the current distance of u's parent against fin[u]; the count
  * of differences and the sum of (fs - fi)^2 taken in 32-bit unsigned
- * arithmetic, as the reference's foru expression computes it. */
+ * arithmetic, as the reference's foru expression computes it.  Every term is
+ * below 2^32 and there are fewer than 2^32 of them, so the sum is exact in a
+ * 64-bit integer whatever order the atomics land in; the host converts it to
+ * double once, which equals the reference's sequential double sum wherever
+ * that sum is exact (below 2^53). */
 __global__ void k_conv_compare(const uint32_t *dist, const uint32_t *first, const uint32_t *fin, uint32_t n,
-                               unsigned long long *cnt, double *norm) {
-    unsigned long long c = 0;
-    double sum = 0.0;
+                               unsigned long long *cnt, unsigned long long *norm) {
+    unsigned long long c = 0, sum = 0;
     for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n; u += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t fi = dist[first ? first[u] : u], fs = fin[u];
         const uint32_t d = fs - fi;
-        sum += (double)(uint32_t)(d * d);
+        sum += (uint32_t)(d * d);
         c += fs != fi;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -265,7 +268,7 @@ gga_status topo_run(const DevGraph *d, bool split, gga_variant variant, bool sss
         GGA_CK(cudaGetLastError());
         if (conv) {
             GGA_CK(cudaMemsetAsync(conv->cnt, 0, sizeof(unsigned long long), st));
-            GGA_CK(cudaMemsetAsync(conv->norm, 0, sizeof(double), st));
+            GGA_CK(cudaMemsetAsync(conv->norm, 0, sizeof(unsigned long long), st));
             const uint32_t cb = std::min<uint32_t>((d->n + 255) / 256, (uint32_t)sms * 8);
             k_conv_compare<<<cb ? cb : 1, 256, 0, st>>>(dist, split && !cdp ? d->first : nullptr, conv->fin, d->n,
                                                         conv->cnt, conv->norm);
@@ -276,8 +279,7 @@ gga_status topo_run(const DevGraph *d, bool split, gga_variant variant, bool sss
         gga_status w = dev_wait(st, 60.0);
         if (w) return w;
         if (conv) {
-            unsigned long long hc = 0;
-            double hn = 0.0;
+            unsigned long long hc = 0, hn = 0;
             GGA_CK(cudaMemcpy(&hc, conv->cnt, sizeof hc, cudaMemcpyDeviceToHost));
             GGA_CK(cudaMemcpy(&hn, conv->norm, sizeof hn, cudaMemcpyDeviceToHost));
             if (conv->n < conv->cap) {
@@ -285,7 +287,7 @@ gga_status topo_run(const DevGraph *d, bool split, gga_variant variant, bool sss
                 r.iteration = res->iterations;
                 r.pad = 0;
                 r.diff_count = hc;
-                r.norm2 = sqrt(hn);
+                r.norm2 = sqrt((double)hn);
             }
             conv->n++;
         }

@@ -63,6 +63,8 @@ def run_point(ctx: Context, g: Graph, flavour: str, algo: str, level: int, bucke
             mda = g.info()["mda"]
         if autotune:
             row["params"] = ctx.autotune(g, 1)
+            if not cdp:  # the tuner's trials re-split the graph: back to this point's split
+                g.NodeSplit(ctx, level, buckets)
         _, st = ctx.solve(g, algo, src, variant, stats=True)
     except GGAError as e:
         row["error"] = "split rule divides by zero" if e.status == ERR_SPLIT_RULE else str(e)

@@ -187,6 +187,13 @@ gga_status gga_ctx_synchronize(gga_ctx *ctx);
 gga_status gga_graph_pin(gga_graph *g, int pin);
 /* Drops the device copy (and split); the next solve uploads again. */
 gga_status gga_graph_release_device(gga_graph *g);
+/* Uploads g when needed (Graph::cudaCopy, graph.h:683-699) and builds what
+ * the frontier engine derives from it once per graph for `algo` under ctx's
+ * current parameters: the device symmetry check that bottom-up BFS rounds
+ * and pulled SSSP bucket closes rely on, and SSSP's light-first row order
+ * for the bucket width in use.  The first solve does the same when this was
+ * not called; calling it first takes that one-time work out of the solve. */
+gga_status gga_graph_prepare(gga_ctx *ctx, gga_graph *g, gga_algo algo);
 
 /* ---- single-source solve (bfs_sssp.cu:372-468 loop, L3/L4) -------------- */
 
@@ -263,13 +270,39 @@ typedef struct gga_params {
      * 4 on graphs averaging 8 or more edges per vertex, never on sparser
      * ones (grids); 1 = never; k > 1 = that k.  Distances are the same. */
     uint32_t sssp_tail;
+    /* Expansion strategy of GGA_VARIANT_AUTO (gga_autotune picks it per graph
+     * from timed trials; every choice gives the same distances):
+     * 0 = edge-balanced CTA-cooperative units over the unsplit CSR;
+     * 1 = the same units over the node-split CSR (the split at split_level /
+     *     split_buckets, as gga_node_split, graph.h:415-522);
+     * 2 = the reference's CDP variant (my_drelax_dynamicP,
+     *     cudaKernels.h:438-520) with the heavy-vertex threshold of
+     *     split_level / split_buckets. */
+    uint32_t expansion;
+    int32_t split_level;   /* 0 none, > 0 ceil(maxdeg/level), < 0 histogram rule */
+    int32_t split_buckets; /* histogram buckets when split_level < 0 */
+    /* SSSP bucket width the batch engine (gga_multi_solve, the server) uses
+     * for this graph's queries (0 = Bellman-Ford order); 0xFFFFFFFF = the
+     * degree-profile width. */
+    uint32_t batch_delta;
 } gga_params;
-/* p = NULL returns to the per-graph defaults. */
+/* p = NULL returns to the per-graph defaults (the graph's autotuned
+ * parameters when gga_autotune has run on it, else its degree profile). */
 gga_status gga_set_params(gga_ctx *ctx, const gga_params *p);
 gga_status gga_get_params(gga_ctx *ctx, gga_params *p);
-/* Picks parameters for g from its degree profile (and short timed trials when
- * trials > 0) and stores them in ctx. */
+/* Picks parameters for g from its degree profile and, when trials > 0,
+ * short timed trials from two sources: CTA size and SSSP bucket width, BFS
+ * direction thresholds (alpha, beta), the expansion strategy (edge units
+ * over the unsplit CSR, the node-split CSR at several split levels, or CDP
+ * on graphs under 2^21 edges) and the batch engine's bucket width.  The
+ * choice is stored on g (used by every solve of g on a context without
+ * explicit parameters, and by gga_multi_solve and the server for g's
+ * queries) and in ctx.  No counterpart in the reference, whose split level
+ * is a command-line argument swept by a shell script (mysc:20-51). */
 gga_status gga_autotune(gga_ctx *ctx, gga_graph *g, uint32_t trials, gga_params *chosen);
+/* The last gga_autotune's trials on ctx as a JSON object (candidates and
+ * their times in ms); at most len bytes with the terminating NUL. */
+gga_status gga_autotune_report(gga_ctx *ctx, char *buf, size_t len);
 
 /* ---- instrumentation ------------------------------------------------------
  * Device-counter counterparts of the reference's per-CTA clock64 histogram
@@ -354,7 +387,9 @@ gga_status gga_write_result_row(const char *path, const gga_result_row *row);
  * (NULL = default stream) on the current device.  All calls share the one
  * array: calls that overlap on the GPU race, so serialise them.  The first
  * call on a device looks up the array's address; make it before any stream
- * capture begins. */
+ * capture begins.  The call is synchronous: it returns after the traversal on
+ * `stream` has finished.  A column id >= n in the caller's CSR returns
+ * GGA_ERR_FORMAT (the kernel checks every edge target before using it). */
 gga_status gga_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_cols, uint32_t n, uint32_t m,
                            uint32_t src, uint32_t *d_dist, void *stream);
 

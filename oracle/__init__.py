@@ -62,6 +62,13 @@ def load():
     lib.oracle_verify.argtypes = [P, C.c_int, P]
     lib.oracle_ary2file.restype = C.c_int
     lib.oracle_ary2file.argtypes = [C.c_char_p, P, P, U]
+    lib.oracle_shortest.restype = C.c_int
+    lib.oracle_shortest.argtypes = [P, C.c_int, U, P]
+    D = C.c_double
+    lib.oracle_gen_rmat.restype = P
+    lib.oracle_gen_rmat.argtypes = [U, U, D, D, D, C.c_uint64, U, U]
+    lib.oracle_gen_grid.restype = P
+    lib.oracle_gen_grid.argtypes = [U, U, D, D, C.c_uint64, U, U]
     _lib = lib
     return lib
 
@@ -94,6 +101,17 @@ class OracleGraph:
     @classmethod
     def load_gr(cls, path: str):
         return cls(load().oracle_load_gr(path.encode()))
+
+    @classmethod
+    def gen_rmat(cls, scale, edge_factor, a=0.57, b=0.19, c=0.19, seed=1, wmin=1, wmax=255):
+        """The library's seeded R-MAT generator, run inside liboracle.so (the
+        GPU library is not loaded): the same graph gga.Graph.rmat returns."""
+        return cls(load().oracle_gen_rmat(scale, edge_factor, a, b, c, seed, wmin, wmax))
+
+    @classmethod
+    def gen_grid(cls, width, height, del_prob=0.05, longrange_frac=0.001, seed=1, wmin=1, wmax=1000):
+        """The library's seeded grid generator, run inside liboracle.so."""
+        return cls(load().oracle_gen_grid(width, height, del_prob, longrange_frac, seed, wmin, wmax))
 
     def __del__(self):
         try:
@@ -153,6 +171,22 @@ class OracleGraph:
         d = np.zeros(n, np.uint32)
         passes = load().oracle_serial(self._h, 1 if algo == "sssp" else 0, src, _p(d))
         return d, passes
+
+    def shortest(self, algo: str, src: int) -> np.ndarray:
+        """Exact distances by a second method (FIFO BFS / Dijkstra), for
+        graphs too large or too deep for the reference's sweeps."""
+        n = self.dims()["nnodes"]
+        d = np.zeros(max(n, 1), np.uint32)
+        if load().oracle_shortest(self._h, 1 if algo == "sssp" else 0, src, _p(d)):
+            raise MemoryError("oracle_shortest")
+        return d[:n]
+
+    def degrees(self) -> np.ndarray:
+        """Out-degree per vertex (noutgoing)."""
+        n = self.dims()["nnodes"]
+        d = np.zeros(max(n, 1), np.uint32)
+        load().oracle_arrays(self._h, None, _p(d), None, None, None, None, None)
+        return d[:n]
 
     def init_dist(self, parent_src: int):
         n = self.dims()["nnodes"]

@@ -4,7 +4,7 @@
  * A plain-C restatement of the reference's host algorithms for the BFS/SSSP
  * path, used only by tests/, __graft_entry__.smoke() and the CPU-baseline leg
  * of bench.py as the checker.  The shipped library never links or calls it.
- * It is pinned against the reference itself: oracle/build_ref.sh compiles the
+ * It is pinned against the reference itself: oracle/Makefile's `ref` target compiles the
  * reference's own graph.h/myutils.h into oracle/_ref/ and
  * tests/golden/make_golden.py records that build's outputs, which
  * tests/test_oracle_golden.py compares with this file bit for bit.
@@ -341,4 +341,107 @@ int oracle_ary2file(const char *fname, const uint32_t *ary, const uint32_t *ispa
     for (uint32_t i = 0; i < len; i++)
         if (isparent[i]) fprintf(f, "%u\n", ary[i]);
     return fclose(f) != 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Exact shortest distances by a second method, for graphs where the
+ * reference's O(passes x E) sweeps take minutes (a 4096^2 grid is thousands
+ * of BFS levels deep).  Not a restatement of reference code: BFS by a FIFO
+ * queue (sssp = 0, every weight 1) and Dijkstra with an indexed binary heap
+ * (sssp = 1).  Shortest distances are unique, so on any graph where
+ * oracle_serial finishes both give the same array (tests/test_oracle_golden.py
+ * checks that on the golden graphs).  Same layout and conventions as
+ * oracle_serial: unsplit graph, nnodes distances, ORACLE_INF if unreached.
+ * Returns 0, or 1 when memory runs out.
+ * ------------------------------------------------------------------------ */
+static void heap_sift_up(uint32_t *heap, uint32_t *pos, const uint32_t *key, uint32_t i) {
+    const uint32_t v = heap[i];
+    while (i > 0) {
+        const uint32_t p = (i - 1) / 2;
+        if (key[heap[p]] <= key[v]) break;
+        heap[i] = heap[p];
+        pos[heap[i]] = i;
+        i = p;
+    }
+    heap[i] = v;
+    pos[v] = i;
+}
+
+static void heap_sift_down(uint32_t *heap, uint32_t *pos, const uint32_t *key, uint32_t size, uint32_t i) {
+    const uint32_t v = heap[i];
+    for (;;) {
+        uint32_t c = 2 * i + 1;
+        if (c >= size) break;
+        if (c + 1 < size && key[heap[c + 1]] < key[heap[c]]) c++;
+        if (key[heap[c]] >= key[v]) break;
+        heap[i] = heap[c];
+        pos[heap[i]] = i;
+        i = c;
+    }
+    heap[i] = v;
+    pos[v] = i;
+}
+
+int oracle_shortest(const oracle_graph *g, int sssp, uint32_t src, uint32_t *dist) {
+    const uint32_t n = g->nnodes;
+    for (uint32_t i = 0; i < n; i++) dist[i] = ORACLE_INF;
+    if (src >= n) return 0;
+    uint32_t *heap = (uint32_t *)malloc((size_t)(n ? n : 1) * 4);
+    uint32_t *pos = (uint32_t *)malloc((size_t)(n ? n : 1) * 4);
+    if (!heap || !pos) {
+        free(heap);
+        free(pos);
+        return 1;
+    }
+    dist[src] = 0;
+    if (!sssp) { /* FIFO queue in `heap`; levels grow by one */
+        uint32_t head = 0, tail = 0;
+        heap[tail++] = src;
+        while (head < tail) {
+            const uint32_t u = heap[head++];
+            const uint32_t end = g->psrc[u] + g->noutgoing[u];
+            for (uint32_t ed = g->psrc[u]; ed < end; ed++) {
+                const uint32_t v = g->edgessrcdst[ed];
+                if (dist[v] == ORACLE_INF) {
+                    dist[v] = dist[u] + 1;
+                    heap[tail++] = v;
+                }
+            }
+        }
+    } else {
+        const uint32_t NOPOS = 0xffffffffu;
+        for (uint32_t i = 0; i < n; i++) pos[i] = NOPOS;
+        uint32_t size = 0;
+        heap[size++] = src;
+        pos[src] = 0;
+        while (size) {
+            const uint32_t u = heap[0];
+            pos[u] = NOPOS;
+            if (--size) {
+                heap[0] = heap[size];
+                pos[heap[0]] = 0;
+                heap_sift_down(heap, pos, dist, size, 0);
+            }
+            const uint32_t du = dist[u];
+            const uint32_t end = g->psrc[u] + g->noutgoing[u];
+            for (uint32_t ed = g->psrc[u]; ed < end; ed++) {
+                const uint32_t v = g->edgessrcdst[ed];
+                const uint32_t nd = du + g->edgessrcwt[ed];
+                if (nd < dist[v]) { /* the same test oracle_serial makes */
+                    dist[v] = nd;
+                    if (pos[v] == NOPOS) {
+                        heap[size] = v;
+                        pos[v] = size;
+                        heap_sift_up(heap, pos, dist, size);
+                        size++;
+                    } else {
+                        heap_sift_up(heap, pos, dist, pos[v]);
+                    }
+                }
+            }
+        }
+    }
+    free(heap);
+    free(pos);
+    return 0;
 }

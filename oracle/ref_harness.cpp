@@ -2,7 +2,7 @@
  * ORACLE — test infrastructure, not product code.
  *
  * A command-line driver around the reference's OWN host code, compiled from
- * the reference sources where they lie (oracle/build_ref.sh passes the
+ * the reference sources where they lie (oracle/Makefile's `ref` target passes the
  * reference directory with -I; nothing of the reference is copied here).  It
  * runs, in the reference's order (bfs_sssp.cu:188-241, 495):
  *   Graph::readFromGR -> getMaxdeg -> findSerialBFS/findSerialSSSP (unsplit,

@@ -28,7 +28,7 @@ int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint
     a.delta = delta; a.nblocks = NB; a.max_rounds = 4 * n + 4096; a.timeout_ns = 60000000000ull;
     a.bu = bu; a.alpha = alpha; a.beta = beta;
     if (SSSP && delta) a.tail_at = tail;
-    std::vector<uint32_t> lcol(m + 4), lwt(m + 4), light(n + 1), hstamp(cap), hq[9], huf[3];
+    std::vector<uint32_t> lcol(m + 4), lwt(m + 4), light(n + 1), hstamp(cap), pbest(cap), hq[9], huf[3];
     for (auto &x : hq) x.assign(cap, 0);
     for (auto &x : huf) x.assign(ucap, 0);
     if (SSSP && delta && lhm) { /* light-first rows, as dev_graph_light_heavy builds them */
@@ -44,6 +44,7 @@ int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint
         a.hb0 = hq[6].data(); a.hb1 = hq[7].data(); a.hb2 = hq[8].data();
         a.huf0 = huf[0].data(); a.huf1 = huf[1].data(); a.huf2 = huf[2].data();
         a.pull = pull;
+        a.pbest = pbest.data();
         for (uint32_t e = 0; e < m; ++e) a.heavy_edges += wt[e] >= delta;
     }
     run_grid(NB, BS, [&](int b) {

@@ -2,9 +2,11 @@
  * new queries injected before each (0 = all at once), finished queries
  * detected by their queue entries and far-pile items (k_mq_count).
  * Queries: the first 16 sources of srcs.bin, algorithm from algos.bin, SSSP
- * bucket width `delta` (0 = Bellman-Ford order).  args: dir NB per stagger delta [tail]
+ * bucket width `delta` (0 = Bellman-Ford order).  args: dir NB per stagger delta [tail [sof]]
  * (tail: a query's buckets end once its pile is at most this size and
- * shrinking; 0 never) */
+ * shrinking; 0 never; sof: 1 = the server's supersteps, which also stop at the
+ * first round in which a query finished and count each slot's remaining
+ * work in the launch, checked against the k_mq_count figures) */
 #include "kernel_mq.inc"
 int NB;
 void launch(MqArgs a) {
@@ -18,7 +20,7 @@ int main(int argc, char **argv) {
     std::string d = argv[1];
     NB = atoi(argv[2]);
     const uint32_t per = atoi(argv[3]), stagger = atoi(argv[4]), delta = atoi(argv[5]);
-    const uint32_t tail = argc > 6 ? atoi(argv[6]) : 0;
+    const uint32_t tail = argc > 6 ? atoi(argv[6]) : 0, sof = argc > 7 ? atoi(argv[7]) : 0;
     auto off = rd(d + "/off.bin"), col = rd(d + "/col.bin"), wt = rd(d + "/wt.bin"), srcs = rd(d + "/srcs.bin"),
          algos = rd(d + "/algos.bin"), want = rd(d + "/want_mix.bin");
     const uint32_t n = off.size() - 1, m = col.size(), nq = algos.size();
@@ -42,6 +44,11 @@ int main(int argc, char **argv) {
     a.uf0 = uf[0].data(); a.uf1 = uf[1].data();
     a.ctl = &ctl; a.cap = cap; a.ucap = ucap; a.nblocks = NB; a.timeout_ns = 60000000000ull;
     std::vector<int> admitted(nq, 0), finished(nq, 0);
+    std::vector<uint32_t> kact(nq, 0);
+    if (sof) {
+        a.stop_on_finish = 1;
+        a.active = kact.data();
+    }
     uint32_t next = 0, launches = 0;
     for (;;) {
         std::vector<uint32_t> list;
@@ -63,6 +70,7 @@ int main(int argc, char **argv) {
         blockIdx.x = 0;
         if (!list.empty()) k_mq_inject(a, qt.data(), list.data(), list.size());
         a.max_rounds = per;
+        std::fill(kact.begin(), kact.end(), 0u);
         launch(a);
         launches++;
         if (ctl.err) { printf("mq err=%u\n", ctl.err); return 1; }
@@ -75,6 +83,12 @@ int main(int argc, char **argv) {
             for (uint32_t i = 0; i < ni; ++i) active[qq[i]]++;
             for (uint32_t t = 0; t < nq; ++t) active[t] += qs[t].fc[qs[t].fp[r & 1] & 1];
         }
+        if (sof)
+            for (uint32_t t = 0; t < nq; ++t)
+                if (kact[t] != active[t]) {
+                    printf("mq active mismatch slot %u kernel %u count %u\n", t, kact[t], active[t]);
+                    return 1;
+                }
         uint32_t live = 0;
         for (uint32_t t = 0; t < nq; ++t)
             if (admitted[t] && !finished[t]) {

@@ -61,3 +61,18 @@ def test_context_without_gpu_fails_cleanly():
     with pytest.raises(gga.GGAError) as e:
         gga.Context(0)
     assert e.value.status in (gga.ERR_NO_DEVICE, gga.ERR_CUDA)
+
+
+def test_noalloc_host_checks_run_before_any_device_call():
+    """gga_bfs_noalloc's argument checks are host-side: NULL pointers and
+    graphs beyond its fixed working memory are rejected before any CUDA call,
+    with the status a caller maps (no GPU needed)."""
+    lib = _native.load()
+    buf = (ctypes.c_uint32 * 8)()
+    p = ctypes.cast(buf, ctypes.c_void_p)
+    assert lib.gga_bfs_noalloc(None, p, 4, 4, 0, p, None) == gga.ERR_INVALID_ARG
+    assert lib.gga_bfs_noalloc(p, p, 4, 4, 0, None, None) == gga.ERR_INVALID_ARG
+    assert lib.gga_bfs_noalloc(p, p, 4, 4, 4, p, None) == gga.ERR_INVALID_ARG  # source >= n
+    assert lib.gga_bfs_noalloc(p, p, (1 << 18) + 1, 4, 0, p, None) == gga.ERR_TOO_LARGE
+    assert "fixed working memory" in lib.gga_last_error().decode()
+    assert lib.gga_bfs_noalloc(p, p, 4, (1 << 23) + 1, 0, p, None) == gga.ERR_TOO_LARGE

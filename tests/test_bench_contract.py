@@ -31,7 +31,11 @@ def _check_line(d, gpus):
     assert d["config"]["workload"] == "rmat10_ef16_seed2_4src_bfs+sssp"
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert cb["cores"] == (os.cpu_count() or 1)  # every host thread, each taking the next traversal
+    assert set(cb["latency_1core_s"]) == {"bfs", "sssp"} and min(cb["latency_1core_s"].values()) > 0
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    # the same workload description the GPU arm prints
+    assert sorted(d["config"]) == ["edges", "graph", "l2", "maxdeg", "parallelism", "sources", "vertices", "workload"]
 
 
 def test_reference_arm_prints_one_json_line():
@@ -40,6 +44,17 @@ def test_reference_arm_prints_one_json_line():
     lines = _json_lines(r.stdout)
     assert len(lines) == 1, r.stdout
     _check_line(lines[0], 1)
+
+
+def test_reference_arm_does_not_load_the_gpu_library():
+    """The CPU arm builds its graph with the generator compiled into
+    liboracle.so; libgga.so is never mapped into the process."""
+    code = ("import sys; sys.argv = ['bench.py', *%r]; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LIBGGA', 'libgga.so' in maps, 'LIBORACLE', 'liboracle.so' in maps)") % (ARGS,)
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "LIBGGA False LIBORACLE True" in r.stdout, r.stdout[-500:]
 
 
 def test_reference_arm_two_ranks_rank0_prints():

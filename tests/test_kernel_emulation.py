@@ -114,7 +114,7 @@ def test_msbfs_kernel_text(emu, case):
 
 
 # graph, blocks, rounds per launch, queries admitted per launch, SSSP delta, pile size that ends a
-# query's buckets
+# query's buckets[, server supersteps]
 MQ = [
     ("r10", 4, 1000000, 0, 0, 0),
     ("r10", 4, 1000000, 0, 33, 0),
@@ -124,6 +124,10 @@ MQ = [
     ("grid", 3, 3, 2, 1, 0),
     ("r10", 4, 1000000, 0, 16, 256),
     ("grid", 3, 3, 2, 50, 120),
+    # the server's supersteps: stop at the first finished query, remaining work counted in the launch
+    ("r10", 4, 128, 3, 16, 0, 1),
+    ("grid", 3, 64, 2, 50, 120, 1),
+    ("r10", 2, 1000000, 0, 0, 0, 1),
 ]
 
 

@@ -143,3 +143,36 @@ def test_reference_build_agrees_with_oracle_on_fresh_graph():
             r = oracle.run_reference(p, algo, -1, 10, 3)
             assert r["returncode"] == 0
             np.testing.assert_array_equal(r["dist"], og.serial(algo, 3)[0])
+
+
+def test_oracle_shortest_matches_reference(golden):
+    """The second exact method (FIFO BFS / Dijkstra) that checks the graphs too
+    deep for the reference's sweeps gives the reference's own distances on
+    every golden graph and source."""
+    for name, e, arrays in _graphs(golden):
+        g = build_golden_graph(name, e, arrays)
+        og = oracle.OracleGraph.from_csr(*g.csr())
+        for key in e["dist"]:
+            algo, src = key.split("/")
+            np.testing.assert_array_equal(og.shortest(algo, int(src)), arrays[f"{name}/dist/{key}"],
+                                          err_msg=f"{name} {key}")
+
+
+def test_oracle_generators_build_the_library_graphs(golden):
+    """oracle.OracleGraph.gen_rmat / gen_grid (the benchmark's CPU legs, which
+    do not load the GPU library) build the same graphs as gga.Graph."""
+    meta, arrays = golden
+    for name, e in sorted(meta["graphs"].items()):
+        p = e.get("params")
+        if e["kind"] == "rmat":
+            og = oracle.OracleGraph.gen_rmat(p["scale"], p["edge_factor"], seed=p["seed"], wmin=p["wmin"],
+                                             wmax=p["wmax"])
+        elif e["kind"] == "grid":
+            og = oracle.OracleGraph.gen_grid(p["width"], p["height"], p["del_prob"], p["longrange_frac"],
+                                             seed=p["seed"], wmin=p["wmin"], wmax=p["wmax"])
+        else:
+            continue
+        a = og.arrays()
+        off = np.concatenate([a["psrc"][:-1] - 1, [len(a["edgessrcdst"]) - 1]]).astype(np.uint32)
+        assert csr_digest(off, a["edgessrcdst"][1:], a["edgessrcwt"][1:]) == e["csr_sha256"], name
+        np.testing.assert_array_equal(og.degrees(), np.diff(off.astype(np.int64)))
