@@ -603,12 +603,15 @@ template <typename T> gga_status grow(T **p, uint32_t *have, uint32_t want, cons
     return GGA_OK;
 }
 
+/* Table slots a launch scans: the caller's nslots, else every slot. */
+uint32_t mq_slots(const MqEngine *e) { return e->nslots ? std::min(e->nslots, e->qcap) : e->qcap; }
+
 MqArgs mq_args(const MqEngine *e) {
     MqArgs a;
     memset(&a, 0, sizeof a);
     a.qt = e->qt;
     a.qs = e->qs;
-    a.nq = e->nslots ? std::min(e->nslots, e->qcap) : e->qcap;
+    a.nq = mq_slots(e);
     a.nearfar = a.nq <= MQ_MAXQ ? 1u : 0u;
     a.qq0 = e->qq[0]; a.qq1 = e->qq[1];
     a.qv0 = e->qv[0]; a.qv1 = e->qv[1];
@@ -727,10 +730,10 @@ gga_status mq_engine_run(MqEngine *e, uint32_t max_rounds, cudaStream_t st, cuda
                          uint32_t *rounds_run, float *ms, bool superstep) {
     MqArgs a = mq_args(e);
     a.max_rounds = max_rounds;
+    const uint32_t ns = mq_slots(e); /* a.nq: every slot the launch scans gets a count */
     if (superstep) {
         a.stop_on_finish = 1;
         a.active = e->active;
-        const uint32_t ns = std::min(e->nslots, e->qcap);
         GGA_CK(cudaMemsetAsync(e->active, 0, (size_t)(ns ? ns : 1) * sizeof(uint32_t), st));
     }
     GGA_CK(cudaMemsetAsync(&e->ctl->bar, 0, sizeof(GridBarrier), st));
@@ -739,9 +742,8 @@ gga_status mq_engine_run(MqEngine *e, uint32_t max_rounds, cudaStream_t st, cuda
     GGA_CK(cudaLaunchCooperativeKernel((const void *)k_mq, dim3(a.nblocks), dim3(MQ_BS), args, mq_smem(), st));
     if (ev1) GGA_CK(cudaEventRecord(ev1, st));
     GGA_CK(cudaMemcpyAsync(e->hctl, e->ctl, sizeof(MqCtl), cudaMemcpyDeviceToHost, st));
-    if (superstep && e->nslots)
-        GGA_CK(cudaMemcpyAsync(e->hactive, e->active, (size_t)std::min(e->nslots, e->qcap) * sizeof(uint32_t),
-                               cudaMemcpyDeviceToHost, st));
+    if (superstep && ns)
+        GGA_CK(cudaMemcpyAsync(e->hactive, e->active, (size_t)ns * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     gga_status s = dev_wait(st, 60.0);
     if (s) return s;
     const MqCtl &h = *e->hctl;

@@ -28,6 +28,7 @@
 #include <deque>
 #include <map>
 #include <string.h>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -49,6 +50,7 @@ struct Request {
 struct Done {
     gga_status status;
     double latency_us;
+    std::string msg; /* the server thread's error message when status != GGA_OK */
 };
 
 struct Slot {
@@ -136,6 +138,7 @@ void finish(gga_server *s, const Request &rq, gga_status st) {
     Done d;
     d.status = st;
     d.latency_us = now_us() - rq.t_submit;
+    if (st != GGA_OK) d.msg = gga_last_error(); /* this thread's message, for the waiting thread */
     std::lock_guard<std::mutex> lk(s->mu);
     s->done[rq.ticket] = d;
     if (st == GGA_OK) s->stats.completed++;
@@ -328,12 +331,13 @@ gga_status gga_server_create(gga_ctx *c, uint32_t ngraphs, gga_graph *const *gra
         return gga_fail(GGA_ERR_CUDA, "server setup: %s", cudaGetErrorString(e));
     }
     sv->pa.init(pool_words);
-    sv->eng.nslots = max_slots;
     if ((s = mq_engine_reserve(&sv->eng, sv->device, (uint32_t)cap, sv->edges_cap, max_slots)) ||
         (s = mq_engine_reset(&sv->eng, sv->st))) {
         server_free(sv);
         return s;
     }
+    /* after reserve, which starts a fresh engine on its first call */
+    sv->eng.nslots = max_slots;
     e = cudaStreamSynchronize(sv->st);
     if (e != cudaSuccess) {
         server_free(sv);
@@ -390,7 +394,8 @@ gga_status gga_server_wait(gga_server *s, uint64_t ticket, uint32_t timeout_ms, 
     const Done d = s->done[ticket];
     s->done.erase(ticket);
     if (latency_us) *latency_us = d.latency_us;
-    if (d.status != GGA_OK) return gga_fail(d.status, "ticket %llu failed", (unsigned long long)ticket);
+    if (d.status != GGA_OK)
+        return gga_fail(d.status, "ticket %llu failed: %s", (unsigned long long)ticket, d.msg.c_str());
     return GGA_OK;
 }
 

@@ -6,7 +6,8 @@
  * (tail: a query's buckets end once its pile is at most this size and
  * shrinking; 0 never; sof: 1 = the server's supersteps, which also stop at the
  * first round in which a query finished and count each slot's remaining
- * work in the launch, checked against the k_mq_count figures) */
+ * work in the launch, checked against the k_mq_count figures; sof >= 2: the
+ * server's flow with that many slots, reused as queries retire) */
 #include "kernel_mq.inc"
 int NB;
 void launch(MqArgs a) {
@@ -15,12 +16,85 @@ void launch(MqArgs a) {
         switch (b) { case 0: k_mq<0>(a); break; case 1: k_mq<1>(a); break; case 2: k_mq<2>(a); break; default: k_mq<3>(a); }
     });
 }
+/* The server's flow: `nslot` table slots, queries admitted into free slots
+ * (a retired query's slot is reused), supersteps that stop at the first
+ * finished query and count each slot's remaining work in the launch; a
+ * query's distances are taken when its slot retires. */
+int run_server(const std::string &d, uint32_t nslot, uint32_t per, uint32_t delta, uint32_t tail) {
+    auto off = rd(d + "/off.bin"), col = rd(d + "/col.bin"), wt = rd(d + "/wt.bin"), srcs = rd(d + "/srcs.bin"),
+         algos = rd(d + "/algos.bin"), want = rd(d + "/want_mix.bin");
+    const uint32_t n = off.size() - 1, m = col.size(), nq = algos.size();
+    const uint32_t cap = n * nslot, ucap = (uint32_t)((uint64_t)m * nslot / MQ_UNIT + 4);
+    std::vector<uint32_t> q[8], uf[2];
+    for (auto &x : q) x.assign(cap, 0);
+    for (auto &x : uf) x.assign(ucap, 0);
+    std::vector<std::vector<uint32_t>> dist(nslot, std::vector<uint32_t>(n)), aux(nslot, std::vector<uint32_t>(n)),
+        fb(nslot, std::vector<uint32_t>(n / 32 + 1)), p0(nslot, std::vector<uint32_t>(n)), p1(nslot, std::vector<uint32_t>(n));
+    std::vector<MqQuery> qt(nslot);
+    std::vector<MqQstate> qs(nslot);
+    memset(qt.data(), 0, nslot * sizeof(MqQuery));
+    memset(qs.data(), 0, nslot * sizeof(MqQstate));
+    MqCtl ctl;
+    memset(&ctl, 0, sizeof ctl);
+    MqArgs a;
+    memset(&a, 0, sizeof a);
+    a.qt = qt.data(); a.qs = qs.data(); a.nq = nslot; a.nearfar = nslot <= MQ_MAXQ;
+    a.qq0 = q[0].data(); a.qq1 = q[1].data(); a.qv0 = q[2].data(); a.qv1 = q[3].data();
+    a.qo0 = q[4].data(); a.qo1 = q[5].data(); a.qb0 = q[6].data(); a.qb1 = q[7].data();
+    a.uf0 = uf[0].data(); a.uf1 = uf[1].data();
+    a.ctl = &ctl; a.cap = cap; a.ucap = ucap; a.nblocks = NB; a.timeout_ns = 60000000000ull;
+    std::vector<uint32_t> kact(nslot, 0);
+    a.stop_on_finish = 1;
+    a.active = kact.data();
+    std::vector<int> slot_q(nslot, -1);
+    uint32_t next = 0, done_q = 0, launches = 0;
+    size_t bad = 0;
+    while (done_q < nq) {
+        std::vector<uint32_t> list;
+        for (uint32_t sl = 0; sl < nslot && next < nq; ++sl) {
+            if (slot_q[sl] >= 0) continue;
+            const uint32_t t = next++;
+            slot_q[sl] = (int)t;
+            MqQuery &Q = qt[sl]; /* k_mq_init */
+            memset(&Q, 0, sizeof Q);
+            Q.off = off.data(); Q.col = col.data(); Q.wt = wt.data(); Q.n = n; Q.m = m;
+            Q.algo = algos[t]; Q.src = srcs[t]; Q.delta = Q.algo == GGA_SSSP ? delta : 0;
+            Q.tail_at = Q.delta ? tail : 0;
+            Q.dist = dist[sl].data(); Q.aux = aux[sl].data();
+            Q.fbits = fb[sl].data(); Q.pile0 = p0[sl].data(); Q.pile1 = p1[sl].data();
+            std::fill(dist[sl].begin(), dist[sl].end(), 1000000000u);
+            std::fill(aux[sl].begin(), aux[sl].end(), 0u);
+            std::fill(fb[sl].begin(), fb[sl].end(), 0u);
+            list.push_back(sl);
+        }
+        threadIdx.x = 0;
+        blockIdx.x = 0;
+        if (!list.empty()) k_mq_inject(a, qt.data(), list.data(), list.size());
+        a.max_rounds = per;
+        std::fill(kact.begin(), kact.end(), 0u);
+        launch(a);
+        launches++;
+        if (ctl.err) { printf("mq err=%u\n", ctl.err); return 1; }
+        for (uint32_t sl = 0; sl < nslot; ++sl) { /* retire */
+            if (slot_q[sl] < 0 || kact[sl] != 0) continue;
+            const uint32_t t = (uint32_t)slot_q[sl];
+            for (uint32_t v = 0; v < n; ++v) bad += dist[sl][v] != want[(size_t)t * n + v];
+            slot_q[sl] = -1;
+            done_q++;
+        }
+        if (launches > 100000) { printf("mq no progress\n"); return 1; }
+    }
+    printf("mq server delta=%u NB=%d slots=%u per=%u launches=%u rounds=%u err=%u bad=%zu relaxed=%llu\n", delta, NB,
+           nslot, per, launches, ctl.rounds_done, ctl.err, bad, ctl.edges_relaxed);
+    return bad != 0;
+}
 int main(int argc, char **argv) {
     if (argc < 6) return 3;
     std::string d = argv[1];
     NB = atoi(argv[2]);
     const uint32_t per = atoi(argv[3]), stagger = atoi(argv[4]), delta = atoi(argv[5]);
     const uint32_t tail = argc > 6 ? atoi(argv[6]) : 0, sof = argc > 7 ? atoi(argv[7]) : 0;
+    if (sof >= 2) return run_server(d, sof, per, delta, tail); /* sof = slots of the server flow */
     auto off = rd(d + "/off.bin"), col = rd(d + "/col.bin"), wt = rd(d + "/wt.bin"), srcs = rd(d + "/srcs.bin"),
          algos = rd(d + "/algos.bin"), want = rd(d + "/want_mix.bin");
     const uint32_t n = off.size() - 1, m = col.size(), nq = algos.size();
