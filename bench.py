@@ -479,7 +479,7 @@ def serving_section(gga, ctx, seconds: float, device: int):
     sys.setswitchinterval(0.0002)  # the submitting and the waiting thread share the GIL
     out = {"graphs": "R-MAT 16/18/20/21 ef16 seeds 30-33, grids 512/1024/1536/2048 seeds 34-37 (5% deleted, w 1..1000)",
            "mix": "70% BFS / 30% SSSP, uniform graph and source", "mem_cap_bytes": 60 << 30, "max_slots": 256,
-           "superstep": "until the first round in which an in-flight query has finished, at most 128 rounds",
+           "superstep": "until max(1, in-flight / 8) of its queries have finished, at most 128 rounds",
            "sequential_qps": seq_qps,
            "topo_reexpression_sequential": {"qps": ref_qps, "sample_queries": nref}, "rates": []}
     try:

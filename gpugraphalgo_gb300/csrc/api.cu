@@ -371,6 +371,7 @@ static gga_status frontier_plan(gga_ctx *c, gga_graph *g, const gga_params &p, b
         out->v.wt = d->lwt;
         out->lh.light = d->light;
         out->lh.heavy_edges = d->lh_heavy;
+        out->lh.cw = d->lh_cw;
         out->lh.pull = p.sssp_pull == 1 || d->wsymmetric <= 0 ? 0u : (p.sssp_pull == 2 ? 2u : 1u);
     }
     return frontier_scratch_ensure(&c->fs, out->v.n > d->n ? out->v.n : d->n, d->m);

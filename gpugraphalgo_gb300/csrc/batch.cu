@@ -49,8 +49,9 @@ struct MqArgs {
     uint32_t nblocks;
     uint32_t max_rounds; /* rounds this launch may run */
     unsigned long long timeout_ns;
-    /* near-far mode: stop at the start of the first round in which fewer
-     * queries have work left than when the launch started (one finished) */
+    /* near-far mode: stop at the start of the first round in which at least
+     * this many of the queries that had work when the launch started have
+     * finished (0: never) */
     uint32_t stop_on_finish;
     /* NULL, or (zeroed by the caller) per table slot: queue entries and far
      * items the slot has when the launch stops (0: its answer is final) */
@@ -345,7 +346,8 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
         __syncthreads();
         if (done == 0) nact0 = nact;
         /* same decision in every block: the counters are the same everywhere */
-        if (done >= a.max_rounds || (units == 0 && fany == 0) || (a.stop_on_finish && a.nearfar && nact < nact0))
+        if (done >= a.max_rounds || (units == 0 && fany == 0) ||
+            (a.stop_on_finish && a.nearfar && nact + a.stop_on_finish <= nact0))
             break;
         if (blockIdx.x == 0 && tid == 0) {
             ctl->qctr[(round + 2) % 3] = 0;
@@ -727,12 +729,12 @@ gga_status mq_engine_admit(MqEngine *e, const MqQuery *host_q, const uint32_t *s
 }
 
 gga_status mq_engine_run(MqEngine *e, uint32_t max_rounds, cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1,
-                         uint32_t *rounds_run, float *ms, bool superstep) {
+                         uint32_t *rounds_run, float *ms, uint32_t superstep) {
     MqArgs a = mq_args(e);
     a.max_rounds = max_rounds;
     const uint32_t ns = mq_slots(e); /* a.nq: every slot the launch scans gets a count */
     if (superstep) {
-        a.stop_on_finish = 1;
+        a.stop_on_finish = superstep;
         a.active = e->active;
         GGA_CK(cudaMemsetAsync(e->active, 0, (size_t)(ns ? ns : 1) * sizeof(uint32_t), st));
     }

@@ -87,11 +87,12 @@ gga_status mq_engine_reset(MqEngine *e, cudaStream_t st);
 gga_status mq_engine_admit(MqEngine *e, const MqQuery *host_q, const uint32_t *slots, uint32_t n, cudaStream_t st);
 /* Runs at most max_rounds rounds (UINT32_MAX: until the queue drains) and
  * waits for them; *rounds_run receives the rounds this launch ran.  With
- * superstep (near-far mode, at most MQ_MAXQ slots) the launch also stops at
- * the first round in which a query has finished, and fills e->hactive with
- * what each slot still has then (as mq_engine_count does). */
+ * superstep = k > 0 (near-far mode, at most MQ_MAXQ slots) the launch also
+ * stops at the first round in which k of its queries have finished, and
+ * fills e->hactive with what each slot still has then (as mq_engine_count
+ * does). */
 gga_status mq_engine_run(MqEngine *e, uint32_t max_rounds, cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1,
-                         uint32_t *rounds_run, float *ms, bool superstep = false);
+                         uint32_t *rounds_run, float *ms, uint32_t superstep = 0);
 /* Fills e->hactive[slot] with the queue entries each slot still has. */
 gga_status mq_engine_count(MqEngine *e, uint32_t nslots, cudaStream_t st);
 

@@ -143,26 +143,37 @@ GraphView dev_graph_view(const DevGraph *d, bool split) {
 
 static unsigned grid_for(uint64_t items, unsigned bs);
 
-/* Light-first row order for bucket width delta (delta-stepping's edge
- * classes, Meyer & Sanders): within each row the edges with w < delta come
- * first, then the rest, each class in its original order; light[u] counts
- * the row's light edges.  A stable two-way partition per row:
+/* Light-first, class-ordered rows for bucket width delta (delta-stepping's
+ * edge classes, Meyer & Sanders, refined): within each row the edges with
+ * w < delta come first (class 0), then the heavy edges in LH_CLASSES weight
+ * classes of width cw = ceil((maxw - delta + 1) / LH_CLASSES), class
+ * c >= 1 holding delta + (c-1) cw <= w < delta + c cw, each class in its
+ * original order; light[u] counts class 0.  So the class of the heavy edges
+ * never falls along a row, and a pulling bucket close can cut a vertex's
+ * heavy range where the classes become too heavy to lower its distance.  A
+ * stable multi-way partition per row:
  *   k_lh_rows: one warp per row of at most LH_WARP_MAX edges: a first pass
- *     counts the light edges (one ballot per 32 edges), a second writes each
- *     edge at its rank among its class (ballot + popc); longer rows are
- *     listed in `big` for
- *   k_lh_big: one CTA per long row, the same two passes with a CTA-wide rank
- *     (per-warp ballot counts scanned in shared memory) per 32 x warps edges.
+ *     counts each class (one ballot per class per 32 edges), a second
+ *     writes each edge at its class start plus its rank in the class
+ *     (ballot + popc); longer rows are listed in `big` for
+ *   k_lh_big: one CTA per long row, the same passes with CTA-wide ranks
+ *     (per-warp ballot counts in shared memory) per 32 x warps edges.
  * Loop bounds are warp- (CTA-) uniform; every collective is reached by the
  * whole warp (CTA).  nlight accumulates the light edges of the graph. */
 constexpr uint32_t LH_WARP_MAX = 4096;
 constexpr unsigned LH_BIG_BS = 1024;
+constexpr uint32_t LH_NCLS = LH_CLASSES + 1; /* class 0 light, 1..LH_CLASSES heavy */
+
+__device__ __forceinline__ uint32_t lh_class(uint32_t w, uint32_t delta, uint32_t cw) {
+    return w < delta ? 0u : 1u + min((w - delta) / cw, LH_CLASSES - 1);
+}
 
 __global__ void k_lh_rows(const uint32_t *off, const uint32_t *col, const uint32_t *wt, uint32_t n, uint32_t delta,
-                          uint32_t *lcol, uint32_t *lwt, uint32_t *light, uint32_t *big, uint32_t *nbig,
+                          uint32_t cw, uint32_t *lcol, uint32_t *lwt, uint32_t *light, uint32_t *big, uint32_t *nbig,
                           unsigned long long *nlight) {
     constexpr unsigned FULL = 0xffffffffu;
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt = (1u << lane) - 1u;
     const uint64_t w0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long mine = 0;
@@ -172,26 +183,39 @@ __global__ void k_lh_rows(const uint32_t *off, const uint32_t *col, const uint32
             if (lane == 0) big[atomicAdd(nbig, 1u)] = (uint32_t)u;
             continue;
         }
-        uint32_t nl = 0;
+        uint32_t pos[LH_NCLS]; /* class counts, then class write cursors (the same in every lane) */
+#pragma unroll
+        for (uint32_t c = 0; c < LH_NCLS; ++c) pos[c] = 0;
         for (uint64_t k0 = b; k0 < e; k0 += 32) { /* 64-bit: no wrap near 2^32 edges */
             const uint64_t k = k0 + lane;
-            nl += __popc(__ballot_sync(FULL, k < e && wt[k] < delta));
+            const uint32_t cls = k < e ? lh_class(wt[k], delta, cw) : LH_NCLS;
+#pragma unroll
+            for (uint32_t c = 0; c < LH_NCLS; ++c) pos[c] += __popc(__ballot_sync(FULL, cls == c));
         }
-        uint32_t lp = b, hp = b + nl;
+        const uint32_t nl = pos[0];
+        uint32_t run = b;
+#pragma unroll
+        for (uint32_t c = 0; c < LH_NCLS; ++c) {
+            const uint32_t cnt = pos[c];
+            pos[c] = run;
+            run += cnt;
+        }
         for (uint64_t k0 = b; k0 < e; k0 += 32) {
             const uint64_t k = k0 + lane;
             const bool in = k < e;
-            const uint32_t w = in ? wt[k] : 0u, c = in ? col[k] : 0u;
-            const bool l = in && w < delta;
-            const uint32_t lm = __ballot_sync(FULL, l), hm = __ballot_sync(FULL, in && !l);
-            const uint32_t lt = (1u << lane) - 1u;
+            const uint32_t w = in ? wt[k] : 0u, cv = in ? col[k] : 0u;
+            const uint32_t cls = in ? lh_class(w, delta, cw) : LH_NCLS;
+            uint32_t p = 0;
+#pragma unroll
+            for (uint32_t c = 0; c < LH_NCLS; ++c) {
+                const uint32_t m = __ballot_sync(FULL, cls == c);
+                if (cls == c) p = pos[c] + __popc(m & lt);
+                pos[c] += __popc(m);
+            }
             if (in) {
-                const uint32_t p = l ? lp + __popc(lm & lt) : hp + __popc(hm & lt);
-                lcol[p] = c;
+                lcol[p] = cv;
                 lwt[p] = w;
             }
-            lp += __popc(lm);
-            hp += __popc(hm);
         }
         if (lane == 0) {
             light[u] = nl;
@@ -202,60 +226,72 @@ __global__ void k_lh_rows(const uint32_t *off, const uint32_t *col, const uint32
 }
 
 __global__ void __launch_bounds__(LH_BIG_BS) k_lh_big(const uint32_t *off, const uint32_t *col, const uint32_t *wt,
-                                                      uint32_t delta, const uint32_t *big, const uint32_t *nbig,
-                                                      uint32_t *lcol, uint32_t *lwt, uint32_t *light,
-                                                      unsigned long long *nlight) {
+                                                      uint32_t delta, uint32_t cw, const uint32_t *big,
+                                                      const uint32_t *nbig, uint32_t *lcol, uint32_t *lwt,
+                                                      uint32_t *light, unsigned long long *nlight) {
     constexpr unsigned FULL = 0xffffffffu;
     constexpr uint32_t NWARP = LH_BIG_BS / 32;
-    __shared__ uint32_t s_l[NWARP], s_h[NWARP], s_tot;
+    __shared__ uint32_t s_cnt[LH_NCLS][NWARP]; /* per class, per warp: edges of the chunk */
+    __shared__ uint32_t s_pos[LH_NCLS];        /* per class: row total, then write cursor */
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
     const uint32_t rows = *nbig;
     for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
         const uint32_t u = big[r], b = off[u], e = off[u + 1];
-        uint32_t cnt = 0;
-        for (uint64_t k = b + threadIdx.x; k < e; k += LH_BIG_BS) cnt += wt[k] < delta;
-        for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(FULL, cnt, d);
-        if (threadIdx.x == 0) s_tot = 0;
+        if (threadIdx.x < LH_NCLS) s_pos[threadIdx.x] = 0;
         __syncthreads();
-        if (lane == 0) atomicAdd(&s_tot, cnt);
+        for (uint64_t k0 = b; k0 < e; k0 += LH_BIG_BS) { /* pass 1: class totals */
+            const uint64_t k = k0 + threadIdx.x;
+            const uint32_t cls = k < e ? lh_class(wt[k], delta, cw) : LH_NCLS;
+            for (uint32_t c = 0; c < LH_NCLS; ++c) {
+                const uint32_t m = __ballot_sync(FULL, cls == c);
+                if (lane == 0 && m) atomicAdd(&s_pos[c], (uint32_t)__popc(m));
+            }
+        }
         __syncthreads();
-        const uint32_t nl = s_tot;
-        uint32_t lp = b, hp = b + nl;
-        for (uint64_t k0 = b; k0 < e; k0 += LH_BIG_BS) {
+        const uint32_t nl = s_pos[0];
+        __syncthreads();
+        if (threadIdx.x == 0) { /* totals -> class starts */
+            uint32_t run = b;
+            for (uint32_t c = 0; c < LH_NCLS; ++c) {
+                const uint32_t cnt = s_pos[c];
+                s_pos[c] = run;
+                run += cnt;
+            }
+        }
+        __syncthreads();
+        for (uint64_t k0 = b; k0 < e; k0 += LH_BIG_BS) { /* pass 2: ranks within class across warps */
             const uint64_t k = k0 + threadIdx.x;
             const bool in = k < e;
-            const uint32_t w = in ? wt[k] : 0u, c = in ? col[k] : 0u;
-            const bool l = in && w < delta;
-            const uint32_t lm = __ballot_sync(FULL, l), hm = __ballot_sync(FULL, in && !l);
-            if (lane == 0) {
-                s_l[warp] = __popc(lm);
-                s_h[warp] = __popc(hm);
+            const uint32_t w = in ? wt[k] : 0u, cv = in ? col[k] : 0u;
+            const uint32_t cls = in ? lh_class(w, delta, cw) : LH_NCLS;
+            uint32_t mine = 0;
+            for (uint32_t c = 0; c < LH_NCLS; ++c) {
+                const uint32_t m = __ballot_sync(FULL, cls == c);
+                if (lane == 0) s_cnt[c][warp] = __popc(m);
+                if (cls == c) mine = __popc(m & lt);
             }
             __syncthreads();
-            uint32_t bl = 0, bh = 0, tl = 0, th = 0; /* ranks before this warp, totals of the chunk */
-            for (uint32_t q = 0; q < NWARP; ++q) {
-                if (q < warp) {
-                    bl += s_l[q];
-                    bh += s_h[q];
-                }
-                tl += s_l[q];
-                th += s_h[q];
-            }
-            const uint32_t lt = (1u << lane) - 1u;
             if (in) {
-                const uint32_t p = l ? lp + bl + __popc(lm & lt) : hp + bh + __popc(hm & lt);
-                lcol[p] = c;
+                uint32_t before = 0; /* edges of my class in earlier warps of this chunk */
+                for (uint32_t q = 0; q < warp; ++q) before += s_cnt[cls][q];
+                const uint32_t p = s_pos[cls] + before + mine;
+                lcol[p] = cv;
                 lwt[p] = w;
             }
-            lp += tl;
-            hp += th;
-            __syncthreads(); /* s_l / s_h are rewritten by the next chunk */
+            __syncthreads();
+            if (threadIdx.x < LH_NCLS) { /* advance the cursors past this chunk */
+                uint32_t t = 0;
+                for (uint32_t q = 0; q < NWARP; ++q) t += s_cnt[threadIdx.x][q];
+                s_pos[threadIdx.x] += t;
+            }
+            __syncthreads();
         }
         if (threadIdx.x == 0) {
             light[u] = nl;
             atomicAdd(nlight, (unsigned long long)nl);
         }
-        __syncthreads(); /* s_tot is reset by the next row */
+        __syncthreads(); /* s_pos is reset by the next row */
     }
 }
 
@@ -279,6 +315,8 @@ gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st) 
         GGA_CK(cudaMemsetAsync(d->lwt + d->m, 0, (mpad - d->m) * sizeof(uint32_t), st));
     }
     d->lh_delta = 0;
+    /* heavy class width: maxw < delta + LH_CLASSES * cw */
+    const uint32_t cw = g->maxw >= delta ? (uint32_t)(((uint64_t)g->maxw - delta + LH_CLASSES) / LH_CLASSES) : 1u;
     /* scratch: the long-row list (at most m / LH_WARP_MAX rows), its count and the light total */
     const size_t nbig_cap = (size_t)d->m / LH_WARP_MAX + 1;
     uint32_t *scr = nullptr;
@@ -291,9 +329,9 @@ gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st) 
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d->device);
         const uint64_t want_warps = d->n;
         const unsigned grid = (unsigned)std::min<uint64_t>((want_warps + 7) / 8, (uint64_t)(sms > 0 ? sms : 1) * 16);
-        k_lh_rows<<<grid ? grid : 1, 256, 0, st>>>(d->off, d->col, d->wt, d->n, delta, d->lcol, d->lwt, d->light, big,
-                                                    nbig, nlight);
-        k_lh_big<<<(sms > 0 ? sms : 1) * 2, LH_BIG_BS, 0, st>>>(d->off, d->col, d->wt, delta, big, nbig, d->lcol,
+        k_lh_rows<<<grid ? grid : 1, 256, 0, st>>>(d->off, d->col, d->wt, d->n, delta, cw, d->lcol, d->lwt, d->light,
+                                                    big, nbig, nlight);
+        k_lh_big<<<(sms > 0 ? sms : 1) * 2, LH_BIG_BS, 0, st>>>(d->off, d->col, d->wt, delta, cw, big, nbig, d->lcol,
                                                                  d->lwt, d->light, nlight);
         s = gga_cuda_check(cudaGetLastError());
     }
@@ -303,6 +341,7 @@ gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st) 
     if (s) return s;
     if ((s = dev_wait(st, 60.0))) return s;
     d->lh_delta = delta;
+    d->lh_cw = cw;
     d->lh_heavy = d->m - (uint32_t)hl;
     return GGA_OK;
 }

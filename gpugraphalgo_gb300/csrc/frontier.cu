@@ -81,6 +81,7 @@ struct Args {
      * 1 when the cost rule picks it, 2 always */
     uint32_t pull;
     uint32_t *pbest; /* cap: per pull-list entry, the smallest offer its edges found (NONE: none) */
+    uint32_t cw;     /* light/heavy rows: width of the heavy-edge weight classes (0: rows not class-ordered) */
     uint32_t heavy_edges; /* edges with w >= delta */
     /* SSSP: when a bucket opens with at most this many far-pile entries, the
      * threshold goes to infinity and the rest runs as one label-correcting
@@ -399,8 +400,10 @@ __device__ __forceinline__ void bottom_up_round(const Args &a, uint32_t round, u
 /* First half of a pulling bucket close (SSSP, light/heavy mode): list every
  * unsettled vertex (d >= thr) that has heavy edges as a queue entry over
  * those edges, in the next round's queue, where expand_units<PULL> relaxes
- * them from the settled side.  A warp takes 32 x PV consecutive vertices per
- * step, lane i vertices 32q + i, so the distance, offset and light-count
+ * them from the settled side.  With class-ordered rows a reached vertex's
+ * range is cut to the classes that can still lower its distance.  A warp
+ * takes 32 x PV consecutive vertices per step, lane i vertices 32q + i, so
+ * the distance, offset and light-count
  * loads are coalesced and PV of each are in flight per lane; the warp's
  * entries are allocated with one packed 64-bit atomicAdd (entries << 32 |
  * edges), as bottom_up_round does.  Trip counts are warp-uniform; no CTA
@@ -429,6 +432,23 @@ __device__ __forceinline__ void pull_scan(const Args &a, uint32_t thr, uint32_t 
                 const uint32_t o0 = __ldg(a.off + v);
                 b[q] = o0 + __ldg(a.light + v);
                 hd[q] = __ldg(a.off + v + 1) - b[q];
+                /* a vertex already reached (d(v) finite) can only be lowered
+                 * through an edge with w < d(v): with class-ordered rows the
+                 * heavy range ends where the classes start at or above d(v)
+                 * (class c holds w >= delta + (c-1) cw), found by a binary
+                 * search on the class, which never falls along the range */
+                if (a.cw && hd[q] && dv[q] < GGA_INFINITY) {
+                    const uint32_t cut_cls = 1u + (uint32_t)(((uint64_t)dv[q] - a.delta + a.cw - 1) / a.cw);
+                    if (cut_cls <= LH_CLASSES) {
+                        uint32_t lo = b[q], hi = b[q] + hd[q];
+                        while (lo < hi) {
+                            const uint32_t mid = lo + ((hi - lo) >> 1);
+                            if (1u + min((__ldg(a.wt + mid) - a.delta) / a.cw, LH_CLASSES - 1) >= cut_cls) hi = mid;
+                            else lo = mid + 1;
+                        }
+                        hd[q] = lo - b[q];
+                    }
+                }
                 cnt += hd[q] ? 1u : 0u;
                 edges += hd[q];
             }
@@ -1186,6 +1206,7 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
         a.light = lh.light;
         a.pull = lh.pull;
         a.pbest = s->pbest;
+        a.cw = lh.cw;
         a.heavy_edges = lh.heavy_edges;
         a.hstamp = s->hstamp;
         a.hv0 = s->hv[0]; a.hv1 = s->hv[1]; a.hv2 = s->hv[2];

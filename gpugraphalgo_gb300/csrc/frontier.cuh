@@ -63,6 +63,7 @@ struct LightHeavy {
     uint32_t heavy_edges = 0;        /* edges with w >= delta */
     uint32_t pull = 0;               /* bucket closes by pull: 0 never, 1 by the cost rule, 2 always (every
                                       * edge's reverse must have its weight) */
+    uint32_t cw = 0;                 /* width of the heavy-edge weight classes of the rows (0: not ordered) */
 };
 
 /* Runs one single-source BFS (sssp=false) or SSSP over `view`.  `first`

@@ -36,8 +36,11 @@ struct DevGraph {
     int wsymmetric; /* symmetric with equal weights both ways: 1 yes, -1 no, 0 not checked */
 
     /* delta-stepping light/heavy order of every row for bucket width lh_delta:
-     * edges with w < lh_delta first, then the rest, each group in CSR order */
+     * edges with w < lh_delta first, then the heavy edges in LH_CLASSES weight
+     * classes of width lh_cw (lh_delta + (c-1) lh_cw <= w < lh_delta + c lh_cw),
+     * each class in CSR order */
     uint32_t lh_delta;
+    uint32_t lh_cw;
     uint32_t *lcol, *lwt; /* m each */
     uint32_t *light;      /* n: light edges of each row */
     uint32_t lh_heavy;    /* edges with w >= lh_delta */
@@ -75,6 +78,9 @@ struct GraphView {
     uint32_t m;
     int symmetric;      /* every edge has its reverse (unsplit view only) */
 };
+
+/* Heavy-edge weight classes of the light/heavy row order (device_graph.cu). */
+constexpr uint32_t LH_CLASSES = 15;
 
 /* Error codes written by kernels into their control blocks. */
 enum : uint32_t {

@@ -4,9 +4,11 @@
  * The reference serves nothing: one process answers one source
  * (bfs_sssp.cu:103-539).  A server keeps its graphs resident and runs the
  * batch engine (batch.cu) in supersteps on its own stream.  A superstep
- * ends at the first round in which one of the in-flight queries has
- * finished (or after SUPERSTEP_MAX_ROUNDS rounds, so queries that arrive
- * meanwhile wait a bounded time); the launch itself leaves every slot's
+ * ends at the first round in which max(1, in-flight / 8) of its queries
+ * have finished -- one under light load, for the shortest turnaround; more
+ * under heavy load, so the host round trip between supersteps is paid for
+ * several retirements -- or after SUPERSTEP_MAX_ROUNDS rounds, so queries
+ * that arrive meanwhile wait a bounded time; the launch itself leaves every slot's
  * remaining queue entries and far items in a pinned array.  Between
  * supersteps the loop
  *   - retires the queries that have none left: their distances are final
@@ -228,8 +230,9 @@ void server_loop(gga_server *s) {
         gga_status st = mq_engine_admit(&s->eng, hq.data(), hslots.data(), (uint32_t)hq.size(), s->st);
         /* ---- one superstep */
         uint32_t rounds = 0;
+        const uint32_t stop_after = std::max<uint32_t>(1u, busy / 8);
         if (st == GGA_OK)
-            st = mq_engine_run(&s->eng, SUPERSTEP_MAX_ROUNDS, s->st, nullptr, nullptr, &rounds, nullptr, true);
+            st = mq_engine_run(&s->eng, SUPERSTEP_MAX_ROUNDS, s->st, nullptr, nullptr, &rounds, nullptr, stop_after);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             s->stats.supersteps++;

@@ -31,13 +31,20 @@ int run(int NB, const std::string &d, int row, uint32_t iters, uint32_t bu, uint
     std::vector<uint32_t> lcol(m + 4), lwt(m + 4), light(n + 1), hstamp(cap), pbest(cap), hq[9], huf[3];
     for (auto &x : hq) x.assign(cap, 0);
     for (auto &x : huf) x.assign(ucap, 0);
-    if (SSSP && delta && lhm) { /* light-first rows, as dev_graph_light_heavy builds them */
+    if (SSSP && delta && lhm) { /* light-first, class-ordered rows, as dev_graph_light_heavy builds them */
+        uint32_t maxw = 0;
+        for (uint32_t e = 0; e < m; ++e) maxw = std::max(maxw, wt[e]);
+        const uint32_t cw = maxw >= delta ? (maxw - delta + LH_CLASSES) / LH_CLASSES : 1;
+        auto cls = [&](uint32_t w) { return w < delta ? 0u : 1u + std::min((w - delta) / cw, LH_CLASSES - 1); };
         for (uint32_t u = 0; u < n; ++u) {
             uint32_t p = off[u];
-            for (uint32_t e = off[u]; e < off[u + 1]; ++e) if (wt[e] < delta) { lcol[p] = col[e]; lwt[p] = wt[e]; ++p; }
-            light[u] = p - off[u];
-            for (uint32_t e = off[u]; e < off[u + 1]; ++e) if (wt[e] >= delta) { lcol[p] = col[e]; lwt[p] = wt[e]; ++p; }
+            for (uint32_t c = 0; c <= LH_CLASSES; ++c)
+                for (uint32_t e = off[u]; e < off[u + 1]; ++e)
+                    if (cls(wt[e]) == c) { lcol[p] = col[e]; lwt[p] = wt[e]; ++p; }
+            light[u] = 0;
+            for (uint32_t e = off[u]; e < off[u + 1]; ++e) light[u] += wt[e] < delta;
         }
+        a.cw = cw;
         a.col = lcol.data(); a.wt = lwt.data(); a.light = light.data(); a.hstamp = hstamp.data();
         a.hv0 = hq[0].data(); a.hv1 = hq[1].data(); a.hv2 = hq[2].data();
         a.ho0 = hq[3].data(); a.ho1 = hq[4].data(); a.ho2 = hq[5].data();

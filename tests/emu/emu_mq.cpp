@@ -6,8 +6,10 @@
  * (tail: a query's buckets end once its pile is at most this size and
  * shrinking; 0 never; sof: 1 = the server's supersteps, which also stop at the
  * first round in which a query finished and count each slot's remaining
- * work in the launch, checked against the k_mq_count figures; sof >= 2: the
- * server's flow with that many slots, reused as queries retire) */
+ * work in the launch, checked against the k_mq_count figures; 2..15: the
+ * same, stopping once that many finished; sof >= 16: the server's flow with
+ * sof - 16 slots, reused as queries retire, stopping once half of the
+ * queries in flight finished) */
 #include "kernel_mq.inc"
 int NB;
 void launch(MqArgs a) {
@@ -44,7 +46,6 @@ int run_server(const std::string &d, uint32_t nslot, uint32_t per, uint32_t delt
     a.uf0 = uf[0].data(); a.uf1 = uf[1].data();
     a.ctl = &ctl; a.cap = cap; a.ucap = ucap; a.nblocks = NB; a.timeout_ns = 60000000000ull;
     std::vector<uint32_t> kact(nslot, 0);
-    a.stop_on_finish = 1;
     a.active = kact.data();
     std::vector<int> slot_q(nslot, -1);
     uint32_t next = 0, done_q = 0, launches = 0;
@@ -71,6 +72,9 @@ int run_server(const std::string &d, uint32_t nslot, uint32_t per, uint32_t delt
         blockIdx.x = 0;
         if (!list.empty()) k_mq_inject(a, qt.data(), list.data(), list.size());
         a.max_rounds = per;
+        uint32_t busy = 0;
+        for (uint32_t sl = 0; sl < nslot; ++sl) busy += slot_q[sl] >= 0;
+        a.stop_on_finish = std::max<uint32_t>(1u, busy / 2); /* as the server: a share of the queries in flight */
         std::fill(kact.begin(), kact.end(), 0u);
         launch(a);
         launches++;
@@ -94,7 +98,7 @@ int main(int argc, char **argv) {
     NB = atoi(argv[2]);
     const uint32_t per = atoi(argv[3]), stagger = atoi(argv[4]), delta = atoi(argv[5]);
     const uint32_t tail = argc > 6 ? atoi(argv[6]) : 0, sof = argc > 7 ? atoi(argv[7]) : 0;
-    if (sof >= 2) return run_server(d, sof, per, delta, tail); /* sof = slots of the server flow */
+    if (sof >= 16) return run_server(d, sof - 16, per, delta, tail); /* sof - 16 = slots of the server flow */
     auto off = rd(d + "/off.bin"), col = rd(d + "/col.bin"), wt = rd(d + "/wt.bin"), srcs = rd(d + "/srcs.bin"),
          algos = rd(d + "/algos.bin"), want = rd(d + "/want_mix.bin");
     const uint32_t n = off.size() - 1, m = col.size(), nq = algos.size();
@@ -120,7 +124,7 @@ int main(int argc, char **argv) {
     std::vector<int> admitted(nq, 0), finished(nq, 0);
     std::vector<uint32_t> kact(nq, 0);
     if (sof) {
-        a.stop_on_finish = 1;
+        a.stop_on_finish = sof;
         a.active = kact.data();
     }
     uint32_t next = 0, launches = 0;

@@ -121,6 +121,7 @@ inline uint32_t lane_id() { return threadIdx.x & 31u; }
 inline uint32_t lanemask_lt() { return (1u << (threadIdx.x & 31u)) - 1u; }
 inline uint32_t atom_add_acq_rel_u32(uint32_t *p, uint32_t v) { return __atomic_fetch_add(p, v, __ATOMIC_ACQ_REL); }
 uint32_t g_dyn[8][1 << 16];
+constexpr uint32_t LH_CLASSES = 15; /* heavy-edge weight classes of the light/heavy row order */
 enum : uint32_t { GGA_DEV_OK = 0, GGA_DEV_TIMEOUT = 1, GGA_DEV_OVERFLOW = 2, GGA_DEV_SPLIT_RULE = 3,
                   GGA_DEV_OVERFLOW_UNITS = 4, GGA_DEV_OVERFLOW_FAR = 5, GGA_DEV_BAD_EDGE = 6, GGA_DEV_ROUND_LIMIT = 7,
                   GGA_DEV_BAD_TARGET = 8 };

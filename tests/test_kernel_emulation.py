@@ -128,9 +128,11 @@ MQ = [
     ("r10", 4, 128, 3, 16, 0, 1),
     ("grid", 3, 64, 2, 50, 120, 1),
     ("r10", 2, 1000000, 0, 0, 0, 1),
-    # the server's flow: 4 or 3 slots reused as queries retire
-    ("r10", 4, 128, 0, 16, 0, 4),
-    ("grid", 3, 64, 0, 50, 120, 3),
+    # stop once 3 queries finished
+    ("r10", 3, 1000000, 0, 16, 0, 3),
+    # the server's flow: 4 or 3 slots (20, 19) reused as queries retire
+    ("r10", 4, 128, 0, 16, 0, 20),
+    ("grid", 3, 64, 0, 50, 120, 19),
 ]
 
 
