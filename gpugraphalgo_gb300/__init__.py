@@ -36,7 +36,9 @@ VARIANTS = {
 
 OK, ERR_INVALID_ARG, ERR_IO, ERR_FORMAT, ERR_SPLIT_RULE = 0, 1, 2, 3, 4
 ERR_NO_MEMORY, ERR_CUDA, ERR_NO_DEVICE, ERR_TIMEOUT, ERR_ADMISSION = 5, 6, 7, 8, 9
-ERR_TOO_LARGE, ERR_NOT_READY, ERR_UNSUPPORTED = 10, 11, 12
+ERR_TOO_LARGE, ERR_NOT_READY, ERR_UNSUPPORTED, ERR_NO_PROGRESS = 10, 11, 12, 13
+MESH_NONE = 0xFFFFFFFF  # no neighbour: a domain boundary edge
+DMR_MIN_ANGLE = 25.0  # MINANGLE, Kepler_DMR/dmr.cu:34
 
 
 class GGAError(RuntimeError):
@@ -273,6 +275,83 @@ class Graph:
         return vr.value, er.value
 
 
+
+class Mesh:
+    """A 2-D triangulation on the host (the reference DMR's mesh: nodex/nodey,
+    tnodes and neighbours, Kepler_DMR/dmesh.h), refined on the GPU by
+    :meth:`Context.refine`."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def _make(cls, fn, *args, where="mesh"):
+        h = C.c_void_p()
+        _check(fn(*args, C.byref(h)), where)
+        return cls(h.value)
+
+    @classmethod
+    def load(cls, base: str) -> "Mesh":
+        """Reads <base>.node and <base>.ele (readNodes / readTriangles, helpers.h:5-63)."""
+        return cls._make(N.load().gga_mesh_load_triangle, base.encode(), where=f"load({base})")
+
+    @classmethod
+    def from_arrays(cls, x, y, tri) -> "Mesh":
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.ascontiguousarray(y, np.float64)
+        t = np.ascontiguousarray(tri, np.uint32).reshape(-1)
+        return cls._make(N.load().gga_mesh_from_arrays, len(x), _ptr(x), _ptr(y), len(t) // 3,
+                         _ptr(t) if len(t) else None, where="from_arrays")
+
+    @classmethod
+    def jittered(cls, w: int, h: int, jitter: float = 0.3, seed: int = 1) -> "Mesh":
+        return cls._make(N.load().gga_mesh_gen_jittered, w, h, jitter, seed, where="jittered")
+
+    @classmethod
+    def random(cls, npoints: int, seed: int = 1) -> "Mesh":
+        return cls._make(N.load().gga_mesh_gen_random, npoints, seed, where="random")
+
+    def save(self, base: str):
+        _check(N.load().gga_mesh_save_triangle(self._h, base.encode()), f"save({base})")
+
+    def free(self):
+        if self._h and self._h.value:
+            N.load().gga_mesh_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        i = N.MeshInfo()
+        _check(N.load().gga_mesh_get_info(self._h, C.byref(i)), "info")
+        return {"npoints": i.npoints, "ntriangles": i.ntriangles}
+
+    def arrays(self) -> dict:
+        """Copies of x, y (float64) and tri, nbr (uint32, 3 per triangle)."""
+        inf = self.info()
+        x, y, t, n = N.PD(), N.PD(), N.PU32(), N.PU32()
+        _check(N.load().gga_mesh_arrays(self._h, C.byref(x), C.byref(y), C.byref(t), C.byref(n)), "arrays")
+        P, T = inf["npoints"], inf["ntriangles"]
+
+        def grab(ptr, cnt, dt):
+            return np.ctypeslib.as_array(ptr, (cnt,)).astype(dt, copy=True) if cnt else np.zeros(0, dt)
+        return {"x": grab(x, P, np.float64), "y": grab(y, P, np.float64), "tri": grab(t, 3 * T, np.uint32),
+                "nbr": grab(n, 3 * T, np.uint32)}
+
+    def check(self, min_angle_deg: float = DMR_MIN_ANGLE) -> dict:
+        r = N.MeshCheck()
+        _check(N.load().gga_mesh_check(self._h, min_angle_deg, C.byref(r)), "check")
+        return {k: getattr(r, k) for k, _ in r._fields_}
+
+
 def writeResult(path: str, **fields):
     """Appends one 17-column result.vi row (myutils.h:86-113)."""
     r = N.ResultRow()
@@ -456,6 +535,16 @@ class Context:
                                         cap, C.byref(nrec), _ptr(out)), f"convergence({algo}, src={src}, {variant})")
         return ([{"iteration": r.iteration, "diff_count": r.diff_count, "norm2": r.norm2}
                  for r in recs[: min(nrec.value, cap)]], out)
+
+    def refine(self, mesh: "Mesh", min_angle_deg: float = DMR_MIN_ANGLE, max_triangles: int = 0,
+               batch_cap: int = 0) -> dict:
+        """Delaunay refinement of `mesh` in place on this context's GPU until no
+        angle is below min_angle_deg (the reference's dmr <basefile> run);
+        returns the refinement statistics (myresult's fields and timings)."""
+        st = N.RefineStats()
+        _check(N.load().gga_mesh_refine(self._h, mesh.handle, min_angle_deg, max_triangles, batch_cap,
+                                        C.byref(st)), "refine")
+        return {k: getattr(st, k) for k, _ in st._fields_}
 
     def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False, out=None):
         """Up to 64 BFS sources in one bit-packed launch; out: optional

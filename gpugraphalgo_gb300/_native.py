@@ -129,6 +129,39 @@ class ServerStats(C.Structure):
     ]
 
 
+class MeshInfo(C.Structure):
+    _fields_ = [("npoints", u32), ("ntriangles", u32)]
+
+
+class MeshCheck(C.Structure):
+    _fields_ = [
+        ("bad_triangles", u64),
+        ("bad_orientation", u64),
+        ("bad_neighbors", u64),
+        ("non_delaunay_edges", u64),
+        ("boundary_edges", u64),
+        ("area", C.c_double),
+    ]
+
+
+class RefineStats(C.Structure):
+    _fields_ = [
+        ("triangles_in", u32),
+        ("bad_in", u32),
+        ("triangles_out", u32),
+        ("bad_out", u32),
+        ("points_out", u32),
+        ("rounds", u32),
+        ("insertions", u64),
+        ("boundary_splits", u64),
+        ("failed_plans", u64),
+        ("total_ms", C.c_double),
+        ("device_ms", C.c_double),
+    ]
+
+
+PD = C.POINTER(C.c_double)
+
 # name -> (restype, argtypes); every symbol declared in include/gga.h
 SIGNATURES = {
     "gga_status_string": (C.c_char_p, [C.c_int]),
@@ -184,6 +217,16 @@ SIGNATURES = {
     "gga_trace_enable": (C.c_int, [P, C.c_int]),
     "gga_convergence": (C.c_int, [P, P, C.c_int, u32, C.c_int, P, C.POINTER(ConvRecord), u32, C.POINTER(u32), P]),
     "gga_trace_get": (C.c_int, [P, C.POINTER(RoundTrace), u32, C.POINTER(u32), C.POINTER(u32), u32, C.POINTER(u32)]),
+    "gga_mesh_load_triangle": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+    "gga_mesh_save_triangle": (C.c_int, [P, C.c_char_p]),
+    "gga_mesh_from_arrays": (C.c_int, [u32, P, P, u32, P, C.POINTER(P)]),
+    "gga_mesh_gen_jittered": (C.c_int, [u32, u32, C.c_double, u64, C.POINTER(P)]),
+    "gga_mesh_gen_random": (C.c_int, [u32, u64, C.POINTER(P)]),
+    "gga_mesh_free": (None, [P]),
+    "gga_mesh_get_info": (C.c_int, [P, C.POINTER(MeshInfo)]),
+    "gga_mesh_arrays": (C.c_int, [P, C.POINTER(PD), C.POINTER(PD), C.POINTER(PU32), C.POINTER(PU32)]),
+    "gga_mesh_check": (C.c_int, [P, C.c_double, C.POINTER(MeshCheck)]),
+    "gga_mesh_refine": (C.c_int, [P, P, C.c_double, u32, u32, C.POINTER(RefineStats)]),
 }
 
 _lib = None

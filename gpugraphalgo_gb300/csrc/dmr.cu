@@ -1,0 +1,625 @@
+/*
+ * Delaunay mesh refinement on the GPU (the reference's DMR program,
+ * Programs/CUDA_src/Kepler_DMR/dmr.cu:54-398 with its refine kernels in
+ * m_refine.h), redesigned as rounds of five short kernels over a mesh kept
+ * resident in HBM.
+ *
+ * Round (all state on the device; the host only launches):
+ *   k_bad_count / k_bad_gather  worklist = the bad triangles in ascending id
+ *                               (two-pass chunked compaction; at most
+ *                               batch_cap of them);
+ *   k_plan      one thread per bad triangle: circumcentre, straight walk to
+ *               the triangle that holds it (or to the boundary edge the walk
+ *               leaves through), cavity growth by the in-circle test, the
+ *               boundary-encroachment rule, and a claim of every triangle the
+ *               plan would rewrite (cavity + outer ring) with a 64-bit
+ *               atomicMax of (round << 32 | a bijection of the triangle id);
+ *   k_resolve   a plan wins if it holds every claim; per-chunk counts;
+ *   k_commit    winners take point and triangle slots in worklist order
+ *               (chunk prefix + block scan), rewrite the cavity as a fan from
+ *               the new point, relink the outer ring and re-mark the new
+ *               triangles;
+ *   k_finish    advances the point/triangle counts and the stop word.
+ * Claims make committed cavities disjoint, so commits never race; the round
+ * structure is the reference's mark / re-mark / retriangulate loop, with its
+ * spin barrier (helpers.h:415) replaced by kernel boundaries.
+ *
+ * The result is a function of the input mesh and the arguments alone: every
+ * step is deterministic and the arithmetic is IEEE double without fused
+ * multiply-adds (this file is compiled with --fmad=false), so it equals the
+ * oracle's serial restatement of the same schedule bit for bit.
+ *
+ * Rounds are issued in groups with no host synchronisation inside a group;
+ * once the stop word is set every kernel returns at once, so surplus rounds
+ * of the last group cost one launch each.  Every index read from the mesh is
+ * bounds-checked (an out-of-range id stops the refinement with an error
+ * instead of being used), and every loop is bounded (walk length, cavity
+ * size, round count).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "ctx.cuh"
+#include "gga_device.cuh"
+
+namespace {
+
+constexpr uint32_t NONE = GGA_MESH_NONE;
+constexpr uint32_t CAV_MAX = 64;            /* cavity triangles per plan */
+constexpr uint32_t FAN_MAX = CAV_MAX + 2;   /* boundary edges of a cavity */
+constexpr uint32_t WALK_MAX = 65536;        /* point-location steps */
+constexpr uint32_t MAX_ROUNDS = 65536;
+constexpr uint32_t PLAN_FAIL = 0, PLAN_INSERT = 1, PLAN_SPLIT = 2;
+constexpr uint32_t STOP_NONE = 0, STOP_DONE = 1, STOP_CAPACITY = 2, STOP_STALLED = 3, STOP_ROUNDS = 4,
+                   STOP_ERROR = 5;
+constexpr uint32_t SCAN_BS = 1024;          /* compaction / commit blocks */
+constexpr uint32_t PLAN_BS = 128;
+constexpr uint32_t ROUND_GROUP = 8;         /* rounds launched between host checks */
+
+struct DmrState {
+    uint32_t npts, ntri, round, nw;
+    uint32_t nbad, stop, winners, added;
+    uint32_t pcap, tcap, bcap, max_rounds;
+    uint32_t err, bad_in, pad0, pad1;
+    unsigned long long insertions, splits, failed;
+};
+
+struct DmrArgs {
+    double *x, *y;
+    uint32_t *tri, *nbr, *bad;
+    unsigned long long *owner;
+    uint32_t *work;
+    uint32_t *p_mode; /* mode | nc << 8 | nf << 16 */
+    double *p_px, *p_py;
+    uint32_t *p_cav;  /* [CAV_MAX][B] */
+    uint4 *p_fan;     /* [FAN_MAX][B]: (a, b, outer, outer's edge | member when outer is NONE) */
+    uint32_t *p_win;  /* [B] */
+    uint32_t *bsum;   /* [3][G] */
+    DmrState *st;
+    double cos_bound;
+    uint32_t B, G;
+};
+
+__device__ __forceinline__ void set_err(DmrState *st) { atomicCAS(&st->err, 0u, 1u); }
+
+__device__ __forceinline__ double orient(const DmrArgs &a, uint32_t p, uint32_t q, double px, double py) {
+    const double xp = a.x[p], yp = a.y[p], xq = a.x[q], yq = a.y[q];
+    return (xq - xp) * (py - yp) - (yq - yp) * (px - xp);
+}
+
+__device__ __forceinline__ double incircle(const DmrArgs &a, uint32_t t, double px, double py) {
+    const uint32_t i0 = a.tri[3 * t], i1 = a.tri[3 * t + 1], i2 = a.tri[3 * t + 2];
+    const double adx = a.x[i0] - px, ady = a.y[i0] - py;
+    const double bdx = a.x[i1] - px, bdy = a.y[i1] - py;
+    const double cdx = a.x[i2] - px, cdy = a.y[i2] - py;
+    const double ad = adx * adx + ady * ady, bd = bdx * bdx + bdy * bdy, cd = cdx * cdx + cdy * cdy;
+    return adx * (bdy * cd - bd * cdy) - ady * (bdx * cd - bd * cdx) + ad * (bdx * cdy - bdy * cdx);
+}
+
+/* an angle whose cosine exceeds cos(MINANGLE) (checkbad, helpers.h:147-180) */
+__device__ __forceinline__ uint32_t tri_bad(const DmrArgs &a, uint32_t t) {
+    const uint32_t v[3] = {a.tri[3 * t], a.tri[3 * t + 1], a.tri[3 * t + 2]};
+    uint32_t bad = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < 3; ++i) {
+        const uint32_t p = v[i], q = v[(i + 1) % 3], r = v[(i + 2) % 3];
+        const double ux = a.x[q] - a.x[p], uy = a.y[q] - a.y[p];
+        const double wx = a.x[r] - a.x[p], wy = a.y[r] - a.y[p];
+        const double dot = ux * wx + uy * wy;
+        if (!bad && dot > a.cos_bound * sqrt((ux * ux + uy * uy) * (wx * wx + wy * wy))) bad = 1;
+    }
+    return bad;
+}
+
+__device__ __forceinline__ uint32_t round_prio(uint32_t t, uint32_t round) {
+    return (t ^ (round * 0x9E3779B9u)) * 0x85EBCA6Bu; /* a bijection of t */
+}
+
+/* Contiguous chunk of [0, n) for block b of G. */
+__device__ __forceinline__ void chunk_of(uint32_t n, uint32_t b, uint32_t G, uint32_t &lo, uint32_t &hi) {
+    const uint32_t c = (uint32_t)(((uint64_t)n + G - 1) / G);
+    const uint64_t l = (uint64_t)b * c, h = l + c;
+    lo = (uint32_t)(l < n ? l : n);
+    hi = (uint32_t)(h < n ? h : n);
+}
+
+/* Block sum of `v` (one value per thread); result in every thread. */
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *ws) {
+    uint32_t tot;
+    block_exclusive_scan(v, ws, &tot);
+    __syncthreads();
+    return tot;
+}
+
+/* Sum of bsum[row * G + j] for j < upto, across the block. */
+__device__ __forceinline__ uint32_t prefix_of(const DmrArgs &a, uint32_t row, uint32_t upto, uint32_t *ws) {
+    uint32_t v = 0;
+    for (uint32_t j = threadIdx.x; j < upto; j += blockDim.x) v += a.bsum[row * a.G + j];
+    return block_sum(v, ws);
+}
+
+/* ---------------------------------------------------------------- marking */
+
+__global__ void __launch_bounds__(SCAN_BS) k_mark_all(DmrArgs a) {
+    const uint32_t n = a.st->ntri;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t *v = a.tri + 3 * (size_t)t;
+        if (v[0] >= a.st->npts || v[1] >= a.st->npts || v[2] >= a.st->npts) {
+            set_err(a.st);
+            a.bad[t] = 0;
+            continue;
+        }
+        a.bad[t] = tri_bad(a, t);
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_BS) k_bad_count(DmrArgs a) {
+    __shared__ uint32_t ws[32];
+    if (a.st->stop != STOP_NONE || a.st->err) return;
+    uint32_t lo, hi, c = 0;
+    chunk_of(a.st->ntri, blockIdx.x, a.G, lo, hi);
+    for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) c += a.bad[t];
+    c = block_sum(c, ws);
+    if (threadIdx.x == 0) a.bsum[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(SCAN_BS) k_bad_gather(DmrArgs a) {
+    __shared__ uint32_t ws[32];
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE) return;
+    if (st->err) { /* an id out of range: nothing reads the mesh after this */
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            st->nw = 0;
+            st->stop = STOP_ERROR;
+        }
+        return;
+    }
+    const uint32_t total = prefix_of(a, 0, a.G, ws);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->nbad = total;
+        if (st->round == 0) st->bad_in = total;
+        if (total == 0) {
+            st->nw = 0;
+            st->stop = STOP_DONE;
+        } else if (st->round >= st->max_rounds) {
+            st->nw = 0;
+            st->stop = STOP_ROUNDS;
+        } else {
+            st->round += 1;
+            st->nw = total < st->bcap ? total : st->bcap;
+        }
+    }
+    if (total == 0) return;
+    uint32_t base = prefix_of(a, 0, blockIdx.x, ws);
+    if (base >= st->bcap) return;
+    uint32_t lo, hi;
+    chunk_of(st->ntri, blockIdx.x, a.G, lo, hi);
+    for (uint32_t t0 = lo; t0 < hi; t0 += blockDim.x) {
+        const uint32_t t = t0 + threadIdx.x;
+        const uint32_t f = t < hi ? a.bad[t] : 0;
+        uint32_t tot;
+        const uint32_t pos = base + block_exclusive_scan(f, ws, &tot);
+        if (f && pos < st->bcap) a.work[pos] = t;
+        base += tot;
+        __syncthreads();
+    }
+}
+
+/* ---------------------------------------------------------------- planning */
+
+/* The cavity of (px, py) grown from seed (the oracle's grow_cavity, same
+ * visiting order).  Fan entries go to the plan record; cav stays local. */
+__device__ bool grow_cavity(const DmrArgs &a, uint32_t k, uint32_t ntri, double px, double py, uint32_t seed,
+                            uint32_t skip_m, uint32_t skip_i, uint32_t *cav, uint32_t &nc, uint32_t &nf) {
+    nc = 1;
+    nf = 0;
+    cav[0] = seed;
+    for (uint32_t q = 0; q < nc; ++q) {
+        const uint32_t c = cav[q];
+        for (uint32_t i = 0; i < 3; ++i) {
+            const uint32_t o = a.nbr[3 * c + i];
+            if (o != NONE) {
+                if (o >= ntri) {
+                    set_err(a.st);
+                    return false;
+                }
+                bool in = false;
+                for (uint32_t j = 0; j < nc; ++j) in |= cav[j] == o;
+                if (in) continue;
+                if (incircle(a, o, px, py) > 0) {
+                    if (nc == CAV_MAX) return false;
+                    cav[nc++] = o;
+                    continue;
+                }
+            }
+            if (c == skip_m && i == skip_i) continue;
+            if (nf == FAN_MAX) return false;
+            uint32_t e = c; /* member id when the edge is on the domain boundary */
+            if (o != NONE) {
+                e = 0;
+                while (e < 3 && a.nbr[3 * o + e] != c) ++e;
+                if (e == 3) {
+                    set_err(a.st); /* neighbour links not mutual */
+                    return false;
+                }
+            }
+            a.p_fan[(size_t)nf * a.B + k] = make_uint4(a.tri[3 * c + (i + 1) % 3], a.tri[3 * c + (i + 2) % 3], o, e);
+            ++nf;
+        }
+    }
+    return true;
+}
+
+__device__ bool fan_ok(const DmrArgs &a, uint32_t k, uint32_t mode, uint32_t nc, uint32_t nf, double px,
+                       double py) {
+    if (nf != nc + (mode == PLAN_SPLIT ? 1u : 2u)) return false;
+    for (uint32_t j = 0; j < nf; ++j) {
+        const uint4 f = a.p_fan[(size_t)j * a.B + k];
+        if (!(orient(a, f.x, f.y, px, py) > 0)) return false;
+        for (uint32_t i = 0; i < j; ++i)
+            if (a.p_fan[(size_t)i * a.B + k].x == f.x) return false;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE) return;
+    const uint32_t nw = st->nw, ntri = st->ntri, round = st->round;
+    uint32_t cav[CAV_MAX];
+    uint32_t fails = 0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
+        const uint32_t t = a.work[k];
+        uint32_t mode = PLAN_FAIL, nc = 0, nf = 0;
+        const unsigned long long key = ((unsigned long long)round << 32) | round_prio(t, round);
+        /* circumcentre (same expression order as the oracle) */
+        const uint32_t v0 = a.tri[3 * t], v1 = a.tri[3 * t + 1], v2 = a.tri[3 * t + 2];
+        const double bx = a.x[v1] - a.x[v0], by = a.y[v1] - a.y[v0];
+        const double cx = a.x[v2] - a.x[v0], cy = a.y[v2] - a.y[v0];
+        const double d = 2.0 * (bx * cy - by * cx);
+        const double b2 = bx * bx + by * by, c2 = cx * cx + cy * cy;
+        double px = a.x[v0] + (cy * b2 - by * c2) / d;
+        double py = a.y[v0] + (bx * c2 - cx * b2) / d;
+        uint32_t cur = t, split_m = NONE, split_i = 0, step = 0;
+        bool ok = true;
+        for (; step < WALK_MAX; ++step) {
+            uint32_t cross = 3;
+            for (uint32_t i = 0; i < 3 && cross == 3; ++i)
+                if (orient(a, a.tri[3 * cur + (i + 1) % 3], a.tri[3 * cur + (i + 2) % 3], px, py) < 0) cross = i;
+            if (cross == 3) break;
+            const uint32_t n = a.nbr[3 * cur + cross];
+            if (n == NONE) {
+                split_m = cur;
+                split_i = cross;
+                break;
+            }
+            if (n >= ntri) {
+                set_err(st);
+                ok = false;
+                break;
+            }
+            cur = n;
+        }
+        if (step == WALK_MAX) ok = false;
+        if (ok && split_m == NONE) {
+            ok = grow_cavity(a, k, ntri, px, py, cur, NONE, 0, cav, nc, nf);
+            for (uint32_t j = 0; ok && j < nf && split_m == NONE; ++j) {
+                const uint4 f = a.p_fan[(size_t)j * a.B + k];
+                if (f.z != NONE) continue;
+                if ((px - a.x[f.x]) * (px - a.x[f.y]) + (py - a.y[f.x]) * (py - a.y[f.y]) < 0) {
+                    split_m = f.w;
+                    for (uint32_t i = 0; i < 3; ++i)
+                        if (a.tri[3 * split_m + (i + 1) % 3] == f.x) split_i = i;
+                }
+            }
+            if (ok && split_m == NONE) {
+                mode = fan_ok(a, k, PLAN_INSERT, nc, nf, px, py) ? PLAN_INSERT : PLAN_FAIL;
+                ok = false; /* done */
+            }
+        }
+        if (ok) { /* split_m's edge split_i, at its midpoint */
+            const uint32_t e0 = a.tri[3 * split_m + (split_i + 1) % 3], e1 = a.tri[3 * split_m + (split_i + 2) % 3];
+            px = (a.x[e0] + a.x[e1]) * 0.5;
+            py = (a.y[e0] + a.y[e1]) * 0.5;
+            if (grow_cavity(a, k, ntri, px, py, split_m, split_m, split_i, cav, nc, nf))
+                mode = fan_ok(a, k, PLAN_SPLIT, nc, nf, px, py) ? PLAN_SPLIT : PLAN_FAIL;
+        }
+        a.p_mode[k] = mode | nc << 8 | nf << 16;
+        if (mode == PLAN_FAIL) {
+            ++fails;
+            continue;
+        }
+        a.p_px[k] = px;
+        a.p_py[k] = py;
+        for (uint32_t j = 0; j < nc; ++j) {
+            a.p_cav[(size_t)j * a.B + k] = cav[j];
+            atomicMax(a.owner + cav[j], key);
+        }
+        for (uint32_t j = 0; j < nf; ++j) {
+            const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+            if (o != NONE) atomicMax(a.owner + o, key);
+        }
+    }
+    if (fails) atomicAdd(&st->failed, (unsigned long long)fails);
+}
+
+/* -------------------------------------------------------- resolve, commit */
+
+__global__ void __launch_bounds__(SCAN_BS) k_resolve(DmrArgs a) {
+    __shared__ uint32_t ws[32];
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE || st->nw == 0) return;
+    const unsigned long long rk = (unsigned long long)st->round << 32;
+    uint32_t lo, hi, wins = 0, need = 0;
+    chunk_of(st->nw, blockIdx.x, a.G, lo, hi);
+    for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+        const uint32_t pm = a.p_mode[k], mode = pm & 0xFF, nc = (pm >> 8) & 0xFF, nf = pm >> 16;
+        uint32_t win = 0;
+        if (mode != PLAN_FAIL) {
+            const unsigned long long key = rk | round_prio(a.work[k], st->round);
+            win = 1;
+            for (uint32_t j = 0; j < nc && win; ++j) win = a.owner[a.p_cav[(size_t)j * a.B + k]] == key;
+            for (uint32_t j = 0; j < nf && win; ++j) {
+                const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+                win = o == NONE || a.owner[o] == key;
+            }
+        }
+        a.p_win[k] = win;
+        wins += win;
+        need += win ? nf - nc : 0;
+    }
+    wins = block_sum(wins, ws);
+    need = block_sum(need, ws);
+    if (threadIdx.x == 0) {
+        a.bsum[a.G + blockIdx.x] = wins;
+        a.bsum[2 * a.G + blockIdx.x] = need;
+    }
+}
+
+/* Totals of a round's winners and added triangles, and whether they fit. */
+__device__ __forceinline__ bool round_fits(const DmrArgs &a, uint32_t *ws, uint32_t &W, uint32_t &A) {
+    W = prefix_of(a, 1, a.G, ws);
+    A = prefix_of(a, 2, a.G, ws);
+    const DmrState *st = a.st;
+    return W > 0 && (uint64_t)st->npts + W <= st->pcap && (uint64_t)st->ntri + A <= st->tcap;
+}
+
+__global__ void __launch_bounds__(SCAN_BS) k_commit(DmrArgs a) {
+    __shared__ uint32_t ws[32];
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE || st->nw == 0) return;
+    uint32_t W, A;
+    if (!round_fits(a, ws, W, A)) return;
+    uint32_t wbase = prefix_of(a, 1, blockIdx.x, ws), abase = prefix_of(a, 2, blockIdx.x, ws);
+    const uint32_t npts = st->npts, ntri = st->ntri;
+    uint32_t lo, hi, ins = 0, spl = 0;
+    chunk_of(st->nw, blockIdx.x, a.G, lo, hi);
+    uint32_t slot[FAN_MAX], fa[FAN_MAX], fb[FAN_MAX];
+    for (uint32_t k0 = lo; k0 < hi; k0 += blockDim.x) {
+        const uint32_t k = k0 + threadIdx.x;
+        uint32_t win = 0, pm = 0;
+        if (k < hi) {
+            win = a.p_win[k];
+            pm = a.p_mode[k];
+        }
+        const uint32_t nc = (pm >> 8) & 0xFF, nf = pm >> 16;
+        uint32_t wt, at;
+        const uint32_t wpre = block_exclusive_scan(win, ws, &wt);
+        __syncthreads();
+        const uint32_t apre = block_exclusive_scan(win ? nf - nc : 0, ws, &at);
+        __syncthreads();
+        if (win) {
+            const uint32_t pid = npts + wbase + wpre, tb = ntri + abase + apre;
+            a.x[pid] = a.p_px[k];
+            a.y[pid] = a.p_py[k];
+            for (uint32_t j = 0; j < nf; ++j) {
+                slot[j] = j < nc ? a.p_cav[(size_t)j * a.B + k] : tb + (j - nc);
+                const uint4 f = a.p_fan[(size_t)j * a.B + k];
+                fa[j] = f.x;
+                fb[j] = f.y;
+            }
+            for (uint32_t j = 0; j < nf; ++j) {
+                const uint4 f = a.p_fan[(size_t)j * a.B + k];
+                const uint32_t s = slot[j];
+                uint32_t n0 = NONE, n1 = NONE;
+                for (uint32_t i = 0; i < nf; ++i) {
+                    if (fa[i] == fb[j]) n0 = slot[i];
+                    if (fb[i] == fa[j]) n1 = slot[i];
+                }
+                a.tri[3 * (size_t)s] = f.x;
+                a.tri[3 * (size_t)s + 1] = f.y;
+                a.tri[3 * (size_t)s + 2] = pid;
+                a.nbr[3 * (size_t)s] = n0;
+                a.nbr[3 * (size_t)s + 1] = n1;
+                a.nbr[3 * (size_t)s + 2] = f.z;
+                if (f.z != NONE) a.nbr[3 * (size_t)f.z + f.w] = s;
+            }
+            for (uint32_t j = 0; j < nf; ++j) a.bad[slot[j]] = tri_bad(a, slot[j]);
+            if ((pm & 0xFF) == PLAN_SPLIT) ++spl;
+            else ++ins;
+        }
+        wbase += wt;
+        abase += at;
+    }
+    if (ins) atomicAdd(&st->insertions, (unsigned long long)ins);
+    if (spl) atomicAdd(&st->splits, (unsigned long long)spl);
+}
+
+__global__ void __launch_bounds__(SCAN_BS) k_finish(DmrArgs a) {
+    __shared__ uint32_t ws[32];
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE) return;
+    if (st->err) {
+        if (threadIdx.x == 0) st->stop = STOP_ERROR;
+        return;
+    }
+    if (st->nw == 0) return;
+    uint32_t W, A;
+    const bool fits = round_fits(a, ws, W, A);
+    if (threadIdx.x == 0) {
+        st->winners = W;
+        st->added = A;
+        if (W == 0) st->stop = STOP_STALLED;
+        else if (!fits) st->stop = STOP_CAPACITY;
+        else {
+            st->npts += W;
+            st->ntri += A;
+        }
+    }
+}
+
+struct DmrBufs {
+    double *x = nullptr, *y = nullptr, *p_px = nullptr, *p_py = nullptr;
+    uint32_t *tri = nullptr, *nbr = nullptr, *bad = nullptr, *work = nullptr, *p_mode = nullptr, *p_cav = nullptr,
+             *p_win = nullptr, *bsum = nullptr;
+    uint4 *p_fan = nullptr;
+    unsigned long long *owner = nullptr;
+    DmrState *st = nullptr;
+    DmrState *hst = nullptr; /* pinned */
+    void free_all(cudaStream_t s) {
+        void *p[] = {x, y, p_px, p_py, tri, nbr, bad, work, p_mode, p_cav, p_win, bsum, p_fan, owner, st};
+        for (void *q : p)
+            if (q) cudaFreeAsync(q, s);
+        if (hst) cudaFreeHost(hst);
+        cudaStreamSynchronize(s);
+    }
+};
+
+template <class T> gga_status dalloc(T **p, size_t n, cudaStream_t s) {
+    GGA_CK(cudaMallocAsync((void **)p, (n ? n : 1) * sizeof(T), s));
+    return GGA_OK;
+}
+
+gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, uint32_t bcap, DmrBufs &b,
+                      gga_refine_stats *out) {
+    cudaStream_t s = c->st;
+    const uint32_t pcap = (uint32_t)(m->npts + (uint64_t)(tcap - m->ntri));
+    const uint32_t B = bcap < tcap ? bcap : tcap;
+    const uint32_t G = (uint32_t)(c->sms > 0 ? 2 * c->sms : 304);
+    gga_status r;
+    if ((r = dalloc(&b.x, pcap, s)) || (r = dalloc(&b.y, pcap, s)) || (r = dalloc(&b.tri, 3 * (size_t)tcap, s)) ||
+        (r = dalloc(&b.nbr, 3 * (size_t)tcap, s)) || (r = dalloc(&b.bad, tcap, s)) ||
+        (r = dalloc(&b.owner, tcap, s)) || (r = dalloc(&b.work, B, s)) || (r = dalloc(&b.p_mode, B, s)) ||
+        (r = dalloc(&b.p_px, B, s)) || (r = dalloc(&b.p_py, B, s)) || (r = dalloc(&b.p_cav, (size_t)CAV_MAX * B, s)) ||
+        (r = dalloc(&b.p_fan, (size_t)FAN_MAX * B, s)) || (r = dalloc(&b.p_win, B, s)) ||
+        (r = dalloc(&b.bsum, 3 * (size_t)G, s)) || (r = dalloc(&b.st, 1, s)))
+        return r;
+    GGA_CK(cudaMallocHost((void **)&b.hst, sizeof(DmrState)));
+    memset(b.hst, 0, sizeof(DmrState));
+    b.hst->npts = m->npts;
+    b.hst->ntri = m->ntri;
+    b.hst->pcap = pcap;
+    b.hst->tcap = tcap;
+    b.hst->bcap = B;
+    b.hst->max_rounds = MAX_ROUNDS;
+    GGA_CK(cudaMemcpyAsync(b.st, b.hst, sizeof(DmrState), cudaMemcpyHostToDevice, s));
+    GGA_CK(cudaMemcpyAsync(b.x, m->x, (size_t)m->npts * sizeof(double), cudaMemcpyHostToDevice, s));
+    GGA_CK(cudaMemcpyAsync(b.y, m->y, (size_t)m->npts * sizeof(double), cudaMemcpyHostToDevice, s));
+    GGA_CK(cudaMemcpyAsync(b.tri, m->tri, (size_t)m->ntri * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    GGA_CK(cudaMemcpyAsync(b.nbr, m->nbr, (size_t)m->ntri * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    GGA_CK(cudaMemsetAsync(b.owner, 0, (size_t)tcap * sizeof(unsigned long long), s));
+
+    DmrArgs a;
+    a.x = b.x;
+    a.y = b.y;
+    a.tri = b.tri;
+    a.nbr = b.nbr;
+    a.bad = b.bad;
+    a.owner = b.owner;
+    a.work = b.work;
+    a.p_mode = b.p_mode;
+    a.p_px = b.p_px;
+    a.p_py = b.p_py;
+    a.p_cav = b.p_cav;
+    a.p_fan = b.p_fan;
+    a.p_win = b.p_win;
+    a.bsum = b.bsum;
+    a.st = b.st;
+    a.cos_bound = cos_bound;
+    a.B = B;
+    a.G = G;
+    const unsigned plan_grid = ctx_grid(c, B, PLAN_BS);
+    cudaEvent_t e0 = c->ev[0], e1 = c->ev[1];
+    GGA_CK(cudaEventRecord(e0, s));
+    k_mark_all<<<G, SCAN_BS, 0, s>>>(a);
+    for (uint32_t issued = 0;;) {
+        for (uint32_t g = 0; g < ROUND_GROUP; ++g) {
+            k_bad_count<<<G, SCAN_BS, 0, s>>>(a);
+            k_bad_gather<<<G, SCAN_BS, 0, s>>>(a);
+            k_plan<<<plan_grid, PLAN_BS, 0, s>>>(a);
+            k_resolve<<<G, SCAN_BS, 0, s>>>(a);
+            k_commit<<<G, SCAN_BS, 0, s>>>(a);
+            k_finish<<<1, SCAN_BS, 0, s>>>(a);
+        }
+        GGA_CK(cudaGetLastError());
+        issued += ROUND_GROUP;
+        GGA_CK(cudaMemcpyAsync(b.hst, b.st, sizeof(DmrState), cudaMemcpyDeviceToHost, s));
+        GGA_CK(cudaStreamSynchronize(s));
+        if (b.hst->stop != STOP_NONE || issued > MAX_ROUNDS + ROUND_GROUP) break;
+    }
+    GGA_CK(cudaEventRecord(e1, s));
+    const DmrState h = *b.hst;
+    if (h.err || h.stop == STOP_ERROR)
+        return gga_fail(GGA_ERR_FORMAT, "mesh refinement: a triangle or neighbour id out of range");
+    if ((r = gga_mesh_resize(m, h.npts, h.ntri))) return r;
+    GGA_CK(cudaMemcpyAsync(m->x, b.x, (size_t)h.npts * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GGA_CK(cudaMemcpyAsync(m->y, b.y, (size_t)h.npts * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GGA_CK(cudaMemcpyAsync(m->tri, b.tri, (size_t)h.ntri * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GGA_CK(cudaMemcpyAsync(m->nbr, b.nbr, (size_t)h.ntri * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GGA_CK(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    out->triangles_out = h.ntri;
+    out->points_out = h.npts;
+    out->bad_in = h.bad_in;
+    out->bad_out = h.nbad;
+    out->rounds = h.round;
+    out->insertions = h.insertions;
+    out->boundary_splits = h.splits;
+    out->failed_plans = h.failed;
+    out->device_ms = ms;
+    switch (h.stop) {
+    case STOP_DONE: return GGA_OK;
+    case STOP_CAPACITY:
+        return gga_fail(GGA_ERR_TOO_LARGE, "mesh refinement: round %u needs more than %u triangles", h.round, tcap);
+    case STOP_STALLED:
+        return gga_fail(GGA_ERR_NO_PROGRESS, "mesh refinement: every plan of round %u failed (%u bad left)", h.round,
+                        h.nbad);
+    case STOP_ROUNDS:
+        return gga_fail(GGA_ERR_NO_PROGRESS, "mesh refinement: %u rounds, %u bad left", h.round, h.nbad);
+    case STOP_ERROR:
+        return gga_fail(GGA_ERR_FORMAT, "mesh refinement: a triangle or neighbour id out of range");
+    default: return gga_fail(GGA_ERR_NO_PROGRESS, "mesh refinement: round limit");
+    }
+}
+
+} // namespace
+
+extern "C" gga_status gga_mesh_refine(gga_ctx *c, gga_mesh *m, double min_angle_deg, uint32_t max_triangles,
+                                      uint32_t batch_cap, gga_refine_stats *st) {
+    const double t0 = gga_now_ms();
+    if (!c || !m) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    if (!(min_angle_deg < 60.0)) return gga_fail(GGA_ERR_INVALID_ARG, "min angle %g (must be below 60)", min_angle_deg);
+    if (min_angle_deg <= 0) min_angle_deg = GGA_DMR_MIN_ANGLE;
+    const uint64_t dflt = 4ull * m->ntri + 65536;
+    const uint64_t tcap64 = max_triangles ? max_triangles : (dflt < 0x3FFFFFFFull ? dflt : 0x3FFFFFFFull);
+    if (tcap64 < m->ntri) return gga_fail(GGA_ERR_INVALID_ARG, "max_triangles %u < %u", max_triangles, m->ntri);
+    if ((uint64_t)m->npts + (tcap64 - m->ntri) >= NONE)
+        return gga_fail(GGA_ERR_TOO_LARGE, "mesh capacity of %llu triangles", (unsigned long long)tcap64);
+    gga_refine_stats local;
+    gga_refine_stats *out = st ? st : &local;
+    memset(out, 0, sizeof *out);
+    out->triangles_in = m->ntri;
+    std::lock_guard<std::mutex> lk(c->mu);
+    gga_status s;
+    if ((s = ctx_activate(c))) return s;
+    DmrBufs b;
+    s = refine_run(c, m, cos(min_angle_deg * (3.14159265358979323846 / 180.0)), (uint32_t)tcap64,
+                   batch_cap ? batch_cap : (1u << 20), b, out);
+    b.free_all(c->st);
+    out->total_ms = gga_now_ms() - t0;
+    return s;
+}

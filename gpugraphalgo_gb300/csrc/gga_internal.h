@@ -50,6 +50,22 @@ struct gga_graph {
     pthread_mutex_t lock;
 };
 
+/* Host-side mesh (gga_mesh_*): points, counter-clockwise triangles and the
+ * neighbour across each triangle edge (edge i opposite vertex i). */
+struct gga_mesh {
+    uint32_t npts;
+    uint32_t ntri;
+    double *x, *y;  /* npts */
+    uint32_t *tri;  /* 3 * ntri */
+    uint32_t *nbr;  /* 3 * ntri, GGA_MESH_NONE on the boundary */
+};
+
+/* Recomputes nbr from tri (GGA_ERR_FORMAT if an edge has > 2 triangles). */
+gga_status gga_mesh_build_neighbors(gga_mesh *m);
+/* Replaces the mesh's arrays with fresh ones of the given sizes (contents
+ * undefined). */
+gga_status gga_mesh_resize(gga_mesh *m, uint32_t npts, uint32_t ntri);
+
 /* Thread-local error message; returns `st` for tail calls. */
 gga_status gga_fail(gga_status st, const char *fmt, ...);
 void gga_clear_error(void);

@@ -49,7 +49,7 @@ const char *gga_status_string(gga_status s) {
     case GGA_OK: return "ok";
     case GGA_ERR_INVALID_ARG: return "invalid argument";
     case GGA_ERR_IO: return "I/O error";
-    case GGA_ERR_FORMAT: return "malformed graph file";
+    case GGA_ERR_FORMAT: return "malformed graph or mesh";
     case GGA_ERR_SPLIT_RULE: return "split rule gives a zero edge limit";
     case GGA_ERR_NO_MEMORY: return "host out of memory";
     case GGA_ERR_CUDA: return "CUDA error";
@@ -59,6 +59,7 @@ const char *gga_status_string(gga_status s) {
     case GGA_ERR_TOO_LARGE: return "graph too large";
     case GGA_ERR_NOT_READY: return "not ready";
     case GGA_ERR_UNSUPPORTED: return "unsupported";
+    case GGA_ERR_NO_PROGRESS: return "refinement made no progress";
     }
     return "unknown status";
 }

@@ -51,7 +51,8 @@ typedef enum gga_status {
     GGA_ERR_ADMISSION = 9,   /* request exceeds the configured device-memory cap */
     GGA_ERR_TOO_LARGE = 10,  /* graph exceeds the uint32 vertex/edge limits */
     GGA_ERR_NOT_READY = 11,  /* serving ticket not finished yet */
-    GGA_ERR_UNSUPPORTED = 12
+    GGA_ERR_UNSUPPORTED = 12,
+    GGA_ERR_NO_PROGRESS = 13 /* mesh refinement: every remaining insertion failed, or the round cap */
 } gga_status;
 
 typedef enum gga_algo { GGA_BFS = 0, GGA_SSSP = 1 } gga_algo;
@@ -456,6 +457,86 @@ gga_status gga_server_get_stats(gga_server *s, gga_server_stats *st);
 /* Stops the loop after the current superstep; queries still queued or in
  * flight are dropped (their buffers are not written after this returns). */
 void gga_server_destroy(gga_server *s);
+
+/* ------------------------------------------------------------------------
+ * Delaunay mesh refinement (the reference's DMR program, Kepler_DMR/dmr.cu).
+ *
+ * A mesh is a 2-D triangulation held on the host: points (double x, y),
+ * triangles as three point ids in counter-clockwise order, and per triangle
+ * the neighbour across each edge (edge i is opposite vertex i;
+ * GGA_MESH_NONE on the domain boundary).  gga_mesh_refine inserts points on
+ * the GPU until no triangle has an angle below the bound, keeping the mesh
+ * Delaunay, and writes the refined mesh back into the same handle.
+ * ---------------------------------------------------------------------- */
+#define GGA_MESH_NONE 0xFFFFFFFFu
+#define GGA_DMR_MIN_ANGLE 25.0 /* MINANGLE, dmr.cu:34 */
+
+typedef struct gga_mesh gga_mesh;
+
+typedef struct gga_mesh_info {
+    uint32_t npoints;
+    uint32_t ntriangles;
+} gga_mesh_info;
+
+typedef struct gga_mesh_check_result {
+    uint64_t bad_triangles;      /* smallest angle below the bound */
+    uint64_t bad_orientation;    /* zero or negative signed area */
+    uint64_t bad_neighbors;      /* links that are not mutual across one shared edge */
+    uint64_t non_delaunay_edges; /* the neighbour's far vertex inside the circumcircle */
+    uint64_t boundary_edges;     /* edges with no neighbour */
+    double area;                 /* sum of signed areas */
+} gga_mesh_check_result;
+
+typedef struct gga_refine_stats {
+    uint32_t triangles_in, bad_in;   /* myresult.i_ntriangles / i_bad */
+    uint32_t triangles_out, bad_out; /* myresult.o_ntriangles / o_bad */
+    uint32_t points_out;
+    uint32_t rounds;                 /* myresult.iteration */
+    uint64_t insertions;             /* circumcentres inserted */
+    uint64_t boundary_splits;        /* boundary edges split at their midpoint */
+    uint64_t failed_plans;           /* insertions given up (walk, cavity or shape limits) */
+    double total_ms;                 /* upload + refinement + download */
+    double device_ms;                /* refinement rounds on the device */
+} gga_refine_stats;
+
+/* Reads "<base>.node" and "<base>.ele" (Triangle format, as readNodes /
+ * readTriangles in helpers.h:5-63; a .poly file is not needed).  Triangles
+ * are reordered counter-clockwise and their neighbours derived.
+ * GGA_ERR_FORMAT on a bad count, a bad line, an id out of range, a
+ * degenerate triangle or an edge shared by more than two triangles. */
+gga_status gga_mesh_load_triangle(const char *base, gga_mesh **out);
+gga_status gga_mesh_save_triangle(const gga_mesh *m, const char *base);
+/* Builds a mesh from arrays (copied): points x/y[npoints], triangles
+ * tri[3 * ntriangles] of point ids; same checks as the loader. */
+gga_status gga_mesh_from_arrays(uint32_t npoints, const double *x, const double *y, uint32_t ntriangles,
+                                const uint32_t *tri, gga_mesh **out);
+/* Seeded Delaunay triangulation of a jittered w x h point grid over the unit
+ * square (jitter in cell units, [0, 0.5)). */
+gga_status gga_mesh_gen_jittered(uint32_t w, uint32_t h, double jitter, uint64_t seed, gga_mesh **out);
+/* Seeded Delaunay triangulation of npoints uniform random points in the unit
+ * square plus its four corners (incremental Bowyer-Watson insertion; a point
+ * that lands exactly on an edge is left out): about 2 * npoints triangles,
+ * the kind of random-point mesh the reference's DMR inputs are. */
+gga_status gga_mesh_gen_random(uint32_t npoints, uint64_t seed, gga_mesh **out);
+void gga_mesh_free(gga_mesh *m);
+gga_status gga_mesh_get_info(const gga_mesh *m, gga_mesh_info *info);
+/* Borrowed views of the mesh's arrays, valid until the mesh changes. */
+gga_status gga_mesh_arrays(const gga_mesh *m, const double **x, const double **y, const uint32_t **tri,
+                           const uint32_t **nbr);
+/* Orientation, neighbour symmetry, the local Delaunay property, the count
+ * of triangles with an angle below min_angle_deg and the total area. */
+gga_status gga_mesh_check(const gga_mesh *m, double min_angle_deg, gga_mesh_check_result *r);
+/* Refines m in place on ctx's GPU until no angle is below min_angle_deg
+ * (<= 0 means GGA_DMR_MIN_ANGLE).  Each round plans one insertion per bad
+ * triangle (at most batch_cap of them, 0 = 1,048,576, lowest ids first),
+ * commits the plans whose cavities no higher-priority plan touches, and
+ * re-marks the new triangles; the result depends only on the input mesh and
+ * the arguments.  max_triangles bounds the refined mesh (0 = 4 x the input +
+ * 65,536).  Returns GGA_ERR_TOO_LARGE when a round would pass that bound and
+ * GGA_ERR_NO_PROGRESS when every remaining plan fails or 65,536 rounds pass;
+ * in both cases m holds the mesh after the last completed round. */
+gga_status gga_mesh_refine(gga_ctx *ctx, gga_mesh *m, double min_angle_deg, uint32_t max_triangles,
+                           uint32_t batch_cap, gga_refine_stats *st);
 
 #ifdef __cplusplus
 }

@@ -10,6 +10,7 @@ never as part of the GPU path being measured.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 import tempfile
@@ -69,6 +70,21 @@ def load():
     lib.oracle_gen_rmat.argtypes = [U, U, D, D, D, C.c_uint64, U, U]
     lib.oracle_gen_grid.restype = P
     lib.oracle_gen_grid.argtypes = [U, U, D, D, C.c_uint64, U, U]
+    lib.oracle_mesh_refine.restype = C.c_int
+    lib.oracle_mesh_refine.argtypes = [P, P, P, P, P, P, U, U, D, U, U, P]
+    lib.oracle_mesh_count_bad.restype = C.c_uint64
+    lib.oracle_mesh_count_bad.argtypes = [U, P, P, P, D]
+    lib.gga_mesh_gen_jittered.restype = C.c_int
+    lib.gga_mesh_gen_jittered.argtypes = [U, U, D, C.c_uint64, P]
+    lib.gga_mesh_gen_random.restype = C.c_int
+    lib.gga_mesh_gen_random.argtypes = [U, C.c_uint64, P]
+    lib.gga_mesh_from_arrays.restype = C.c_int
+    lib.gga_mesh_from_arrays.argtypes = [U, P, P, U, P, P]
+    lib.gga_mesh_check.restype = C.c_int
+    lib.gga_mesh_check.argtypes = [P, D, P]
+    lib.gga_mesh_get_info.argtypes = [P, P]
+    lib.gga_mesh_arrays.argtypes = [P, P, P, P, P]
+    lib.gga_mesh_free.argtypes = [P]
     _lib = lib
     return lib
 
@@ -197,6 +213,107 @@ class OracleGraph:
     def verify(self, algo: str, dist_split) -> int:
         d = np.ascontiguousarray(dist_split, np.uint32)
         return int(load().oracle_verify(self._h, 1 if algo == "sssp" else 0, _p(d)))
+
+
+MESH_STATUS = {0: "ok", 1: "capacity", 2: "stalled", 3: "rounds", 4: "no_memory"}
+
+
+def cos_bound(min_angle_deg: float) -> float:
+    """cos(MINANGLE * (PI / 180)) as the refinement compares it (helpers.h:171)."""
+    return math.cos(min_angle_deg * (math.pi / 180.0))
+
+
+def _mesh_dict(lib, h_) -> dict:
+    info = (C.c_uint32 * 2)()
+    lib.gga_mesh_get_info(h_, info)
+    npts, ntri = int(info[0]), int(info[1])
+    px, py, pt, pn = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+    lib.gga_mesh_arrays(h_, C.byref(px), C.byref(py), C.byref(pt), C.byref(pn))
+
+    def grab(ptr, n, ct, dt):
+        if n == 0:
+            return np.zeros(0, dt)
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), (n,)).astype(dt, copy=True)
+    return {"x": grab(px, npts, C.c_double, np.float64), "y": grab(py, npts, C.c_double, np.float64),
+            "tri": grab(pt, 3 * ntri, C.c_uint32, np.uint32), "nbr": grab(pn, 3 * ntri, C.c_uint32, np.uint32)}
+
+
+def _mesh_call(fn, *args) -> dict:
+    lib = load()
+    h_ = C.c_void_p()
+    if fn(*args, C.byref(h_)) != 0:
+        raise RuntimeError("oracle: mesh construction failed")
+    try:
+        return _mesh_dict(lib, h_)
+    finally:
+        lib.gga_mesh_free(h_)
+
+
+def mesh_gen_jittered(w: int, h: int, jitter: float, seed: int) -> dict:
+    """The library's seeded jittered-grid Delaunay mesh, built inside
+    liboracle.so (the GPU library is not loaded): the same mesh that
+    gga.Mesh.jittered returns.  Arrays x, y (float64), tri, nbr (uint32)."""
+    return _mesh_call(load().gga_mesh_gen_jittered, w, h, jitter, seed)
+
+
+def mesh_gen_random(npoints: int, seed: int) -> dict:
+    """The library's seeded random-point Delaunay mesh (gga.Mesh.random)."""
+    return _mesh_call(load().gga_mesh_gen_random, npoints, seed)
+
+
+def mesh_check(mesh: dict, min_angle_deg: float = 25.0) -> dict:
+    """Checks a mesh's arrays: its neighbour array must equal the one derived
+    from its triangles, every triangle must be counter-clockwise (the
+    derivation would reorder it otherwise), and the derived mesh's check
+    counts (gga_mesh_check) are returned."""
+    lib = load()
+    x = np.ascontiguousarray(mesh["x"], np.float64)
+    y = np.ascontiguousarray(mesh["y"], np.float64)
+    tri = np.ascontiguousarray(mesh["tri"], np.uint32)
+    h_ = C.c_void_p()
+    if lib.gga_mesh_from_arrays(len(x), _p(x), _p(y), len(tri) // 3, _p(tri), C.byref(h_)) != 0:
+        return {"valid": False}
+    try:
+        d = _mesh_dict(lib, h_)
+        r = (C.c_char * 48)()  # gga_mesh_check_result: 5 x uint64, then double area
+        lib.gga_mesh_check(h_, min_angle_deg, r)
+        u = np.frombuffer(bytes(r), np.uint64, 5)
+        area = float(np.frombuffer(bytes(r), np.float64, 1, 40)[0])
+    finally:
+        lib.gga_mesh_free(h_)
+    return {"valid": True, "tri_ccw": bool(np.array_equal(d["tri"], tri)),
+            "nbr_consistent": bool(np.array_equal(d["nbr"], np.asarray(mesh["nbr"], np.uint32))),
+            "bad_triangles": int(u[0]), "bad_orientation": int(u[1]), "bad_neighbors": int(u[2]),
+            "non_delaunay_edges": int(u[3]), "boundary_edges": int(u[4]), "area": area}
+
+
+def mesh_refine(mesh: dict, min_angle_deg: float = 25.0, max_triangles: int = 0, batch_cap: int = 1 << 20,
+                max_rounds: int = 65536) -> dict:
+    """Serial refinement in the GPU's round schedule (mesh_oracle.c).  Takes
+    and returns dicts of x, y, tri, nbr; adds 'status' and the stats."""
+    x, y = mesh["x"], mesh["y"]
+    tri, nbr = mesh["tri"], mesh["nbr"]
+    npts, ntri = len(x), len(tri) // 3
+    tcap = max_triangles or min(4 * ntri + 65536, 0x3FFFFFFF)
+    pcap = npts + (tcap - ntri)  # each insertion adds one point and at least one triangle
+    X = np.zeros(pcap, np.float64); X[:npts] = x
+    Y = np.zeros(pcap, np.float64); Y[:npts] = y
+    T = np.zeros(3 * tcap, np.uint32); T[:3 * ntri] = tri
+    N = np.zeros(3 * tcap, np.uint32); N[:3 * ntri] = nbr
+    np_, nt_ = C.c_uint32(npts), C.c_uint32(ntri)
+    st = np.zeros(6, np.uint64)
+    rc = load().oracle_mesh_refine(C.byref(np_), C.byref(nt_), _p(X), _p(Y), _p(T), _p(N), pcap, tcap,
+                                   cos_bound(min_angle_deg), batch_cap, max_rounds, _p(st))
+    P, Tn = np_.value, nt_.value
+    return {"x": X[:P].copy(), "y": Y[:P].copy(), "tri": T[:3 * Tn].copy(), "nbr": N[:3 * Tn].copy(),
+            "status": MESH_STATUS.get(rc, str(rc)), "rounds": int(st[0]), "insertions": int(st[1]),
+            "boundary_splits": int(st[2]), "failed_plans": int(st[3]), "bad_in": int(st[4]), "bad_out": int(st[5])}
+
+
+def mesh_count_bad(mesh: dict, min_angle_deg: float = 25.0) -> int:
+    tri = np.ascontiguousarray(mesh["tri"], np.uint32)
+    return int(load().oracle_mesh_count_bad(len(tri) // 3, _p(mesh["x"]), _p(mesh["y"]), _p(tri),
+                                            cos_bound(min_angle_deg)))
 
 
 def serial_distances(off, col, wt, algo: str, src: int) -> np.ndarray:

@@ -1,0 +1,56 @@
+/* Runs the mesh refinement kernels' text (dmr.cu) round by round on a mesh
+ * in dir/{x,y}.bin (float64) and dir/{tri,nbr}.bin (uint32), the way
+ * gga_mesh_refine launches them, and writes the refined arrays and the stop
+ * word to dir/out_*.bin.  args: dir G BS PBS batch_cap tcap cos_bound(hex) */
+#include "kernel_dmr.inc"
+static std::vector<double> rdd(const std::string &p) {
+    std::ifstream f(p, std::ios::binary); f.seekg(0, std::ios::end); size_t n = f.tellg() / 8; f.seekg(0);
+    std::vector<double> v(n); f.read((char *)v.data(), n * 8); return v;
+}
+template <class T> static void wr(const std::string &p, const T *v, size_t n) {
+    std::ofstream f(p, std::ios::binary); f.write((const char *)v, n * sizeof(T));
+}
+#define LAUNCH(K, NB, BS) run_grid(NB, BS, [&](int b) { switch (b) { case 0: K<0>(a); break; case 1: K<1>(a); break; case 2: K<2>(a); break; default: K<3>(a); } })
+int main(int argc, char **argv) {
+    if (argc < 8) return 1;
+    const std::string d = argv[1];
+    const int G = atoi(argv[2]), BS = atoi(argv[3]), PBS = atoi(argv[4]);
+    const uint32_t bcap = (uint32_t)atol(argv[5]), tcap = (uint32_t)atol(argv[6]);
+    const double cb = strtod(argv[7], nullptr);
+    auto x0 = rdd(d + "/x.bin"), y0 = rdd(d + "/y.bin");
+    auto t0 = rd(d + "/tri.bin"), n0 = rd(d + "/nbr.bin");
+    const uint32_t npts = x0.size(), ntri = t0.size() / 3, pcap = npts + (tcap - ntri);
+    const uint32_t B = bcap < tcap ? bcap : tcap;
+    std::vector<double> x(pcap), y(pcap), px(B), py(B);
+    std::vector<uint32_t> tri(3 * (size_t)tcap), nbr(3 * (size_t)tcap), bad(tcap), work(B), pm(B), pc((size_t)CAV_MAX * B),
+        pw(B), bsum(3 * G);
+    std::vector<uint4> pf((size_t)FAN_MAX * B);
+    std::vector<unsigned long long> owner(tcap, 0);
+    std::copy(x0.begin(), x0.end(), x.begin());
+    std::copy(y0.begin(), y0.end(), y.begin());
+    std::copy(t0.begin(), t0.end(), tri.begin());
+    std::copy(n0.begin(), n0.end(), nbr.begin());
+    DmrState st;
+    memset(&st, 0, sizeof st);
+    st.npts = npts; st.ntri = ntri; st.pcap = pcap; st.tcap = tcap; st.bcap = B; st.max_rounds = MAX_ROUNDS;
+    DmrArgs a;
+    a.x = x.data(); a.y = y.data(); a.tri = tri.data(); a.nbr = nbr.data(); a.bad = bad.data(); a.owner = owner.data();
+    a.work = work.data(); a.p_mode = pm.data(); a.p_px = px.data(); a.p_py = py.data(); a.p_cav = pc.data();
+    a.p_fan = pf.data(); a.p_win = pw.data(); a.bsum = bsum.data(); a.st = &st; a.cos_bound = cb; a.B = B; a.G = G;
+    LAUNCH(k_mark_all, G, BS);
+    for (uint32_t r = 0; st.stop == STOP_NONE && r < 4096; ++r) {
+        LAUNCH(k_bad_count, G, BS);
+        LAUNCH(k_bad_gather, G, BS);
+        LAUNCH(k_plan, 2, PBS);
+        LAUNCH(k_resolve, G, BS);
+        LAUNCH(k_commit, G, BS);
+        LAUNCH(k_finish, 1, BS);
+    }
+    wr(d + "/out_x.bin", x.data(), st.npts);
+    wr(d + "/out_y.bin", y.data(), st.npts);
+    wr(d + "/out_tri.bin", tri.data(), 3 * (size_t)st.ntri);
+    wr(d + "/out_nbr.bin", nbr.data(), 3 * (size_t)st.ntri);
+    printf("stop %u rounds %u npts %u ntri %u nbad %u bad_in %u ins %llu splits %llu failed %llu err %u\n", st.stop,
+           st.round, st.npts, st.ntri, st.nbad, st.bad_in, st.insertions, st.splits, st.failed, st.err);
+    return 0;
+}

@@ -1,7 +1,7 @@
 """Turns a kernel source file into host-compilable text for the emulator
 (prelude.h): each kernel becomes a template on its block index, so its
 __shared__ statics are per-block, and dynamic shared memory comes from a
-per-block host array.  Usage: gen_kernels.py {frontier|sssp32|msbfs|mq} OUT"""
+per-block host array.  Usage: gen_kernels.py {frontier|sssp32|msbfs|mq|dmr} OUT"""
 import os
 import re
 import sys
@@ -53,6 +53,9 @@ def generate(which):
         first = "constexpr uint32_t NONE" if "constexpr uint32_t NONE" in src else "constexpr uint32_t MQ_BS"
         body = hdr + transform("batch.cu", first, "/* Reached vertices", ["k_mq"],
                                [("extern __shared__ uint32_t dyn[];", "uint32_t *dyn")])
+    elif which == "dmr":
+        body = transform("dmr.cu", "constexpr uint32_t NONE", "struct DmrBufs",
+                         ["k_mark_all", "k_bad_count", "k_bad_gather", "k_plan", "k_resolve", "k_commit", "k_finish"], [])
     else:
         raise SystemExit("unknown kernel " + which)
     return helpers() + "\n" + body

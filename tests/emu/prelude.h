@@ -17,6 +17,7 @@
 #pragma once
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <barrier>
 #include <chrono>
 #include <cstdint>
@@ -102,6 +103,7 @@ inline unsigned long long atomicOr(unsigned long long *p, unsigned long long v) 
 inline unsigned atomicAnd(unsigned *p, unsigned v) { return __atomic_fetch_and(p, v, __ATOMIC_SEQ_CST); }
 inline unsigned atomicExch(unsigned *p, unsigned v) { return __atomic_exchange_n(p, v, __ATOMIC_SEQ_CST); }
 inline unsigned atomicMin(unsigned *p, unsigned v) { unsigned o = __atomic_load_n(p, __ATOMIC_SEQ_CST); while (v < o && !__atomic_compare_exchange_n(p, &o, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {} return o; }
+inline unsigned long long atomicMax(unsigned long long *p, unsigned long long v) { unsigned long long o = __atomic_load_n(p, __ATOMIC_SEQ_CST); while (v > o && !__atomic_compare_exchange_n(p, &o, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {} return o; }
 inline unsigned atomicCAS(unsigned *p, unsigned c, unsigned v) { __atomic_compare_exchange_n(p, &c, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST); return c; }
 template <class T> T __ldg(const T *p) { return *p; }
 template <class T> T __ldcg(const T *p) { return __atomic_load_n(p, __ATOMIC_SEQ_CST); }
@@ -112,6 +114,9 @@ using std::min; using std::max;
 inline uint32_t min(uint32_t a, uint32_t b) { return a < b ? a : b; }
 inline uint32_t max(uint32_t a, uint32_t b) { return a > b ? a : b; }
 #define GGA_INFINITY 1000000000u
+#define GGA_MESH_NONE 0xFFFFFFFFu
+struct uint4 { uint32_t x, y, z, w; };
+inline uint4 make_uint4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) { return uint4{x, y, z, w}; }
 enum { GGA_BFS = 0, GGA_SSSP = 1 };
 inline uint32_t ld_acquire_u32(const uint32_t *p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
 inline uint32_t ld_relaxed_u32(const uint32_t *p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }

@@ -53,14 +53,15 @@ def emu(tmp_path_factory):
                  ).astype(np.uint32).tofile(d / "want_mix.bin")
     shutil.copy(os.path.join(EMU, "prelude.h"), root / "prelude.h")
     bins = {}
-    for k in ("frontier", "sssp32", "msbfs", "mq"):
+    for k in ("frontier", "sssp32", "msbfs", "mq", "dmr"):
         harness = os.path.join(EMU, f"emu_{k}.cpp")
         if not os.path.exists(harness):
             continue
         subprocess.run(["python3", os.path.join(EMU, "gen_kernels.py"), k, str(root / f"kernel_{k}.inc")], check=True)
         shutil.copy(harness, root / f"emu_{k}.cpp")
         exe = str(root / f"emu_{k}")
-        subprocess.run(["g++", "-std=c++20", "-O1", "-pthread", "-w", "-I", str(root), str(root / f"emu_{k}.cpp"),
+        subprocess.run(["g++", "-std=c++20", "-O1", "-pthread", "-w", "-ffp-contract=off", "-I", str(root),
+                        str(root / f"emu_{k}.cpp"),
                         "-o", exe], check=True)
         bins[k] = exe
     return root, bins
@@ -139,3 +140,33 @@ MQ = [
 @pytest.mark.parametrize("case", MQ, ids=lambda c: "-".join(map(str, c)))
 def test_batch_kernel_text(emu, case):
     _run(emu, "mq", *case)
+
+
+# Mesh refinement kernels (dmr.cu): every round's kernels run as emulated
+# threads (3 blocks of 64 for the compactions and commits, 2 x 32 planning
+# threads), and the refined mesh must equal the oracle's serial restatement
+# of the same schedule bit for bit: points, triangles and neighbours.
+DMR_CASES = [("jittered", 1 << 20), ("jittered", 7), ("random", 1 << 20)]
+
+
+@pytest.mark.parametrize("case", DMR_CASES, ids=[f"{m}-cap{c}" for m, c in DMR_CASES])
+def test_dmr_kernel_text(emu, case):
+    root, bins = emu
+    kind, bcap = case
+    mesh = oracle.mesh_gen_jittered(14, 12, 0.35, 2) if kind == "jittered" else oracle.mesh_gen_random(120, 5)
+    d = root / f"dmr_{kind}_{bcap}"
+    d.mkdir()
+    for k in ("x", "y", "tri", "nbr"):
+        mesh[k].tofile(d / f"{k}.bin")
+    tcap = 4 * (len(mesh["tri"]) // 3) + 65536
+    r = subprocess.run([bins["dmr"], str(d), "3", "64", "32", str(bcap), str(tcap), oracle.cos_bound(25.0).hex()],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    fields = dict(zip(r.stdout.split()[0::2], r.stdout.split()[1::2]))
+    want = oracle.mesh_refine(mesh, batch_cap=bcap)
+    assert want["status"] == "ok" and want["bad_out"] == 0
+    assert fields["stop"] == "1" and fields["err"] == "0"  # done, no index error
+    assert int(fields["rounds"]) == want["rounds"] and int(fields["ins"]) == want["insertions"]
+    assert int(fields["splits"]) == want["boundary_splits"] and int(fields["bad_in"]) == want["bad_in"]
+    for k, dt in (("x", np.float64), ("y", np.float64), ("tri", np.uint32), ("nbr", np.uint32)):
+        np.testing.assert_array_equal(np.fromfile(d / f"out_{k}.bin", dt), want[k], err_msg=k)
