@@ -1,7 +1,7 @@
 /*
  * Delaunay mesh refinement on the GPU (the reference's DMR program,
  * Programs/CUDA_src/Kepler_DMR/dmr.cu:54-398 with its refine kernels in
- * m_refine.h), redesigned as rounds of five short kernels over a mesh kept
+ * m_refine.h), redesigned as rounds of nine short kernels over a mesh kept
  * resident in HBM.
  *
  * Round (all state on the device; the host only launches):
@@ -11,23 +11,34 @@
  *   k_plan      one thread per bad triangle: circumcentre, straight walk to
  *               the triangle that holds it (or to the boundary edge the walk
  *               leaves through), cavity growth by the in-circle test, the
- *               boundary-encroachment rule, and a claim of every triangle the
- *               plan would rewrite (cavity + outer ring) with a 64-bit
- *               atomicMax of (round << 32 | a bijection of the triangle id);
- *   k_resolve   a plan wins if it holds every claim; per-chunk counts;
- *   k_commit    winners take point and triangle slots in worklist order
- *               (chunk prefix + block scan), rewrite the cavity as a fan from
- *               the new point, relink the outer ring and re-mark the new
+ *               boundary-encroachment rule, and 64-bit atomicMax claims of
+ *               its cavity and of its outer ring (the triangles across the
+ *               cavity boundary, whose links it rewrites) in two tables, keyed
+ *               by (round, pass, a bijection of the triangle id);
+ *   k_resolve0  a plan wins the first pass if no higher key claims its cavity
+ *               (in either table) or claims its ring as cavity; winners stamp
+ *               their cavity and ring in the lock table;
+ *   k_reclaim   plans that lost and touch no stamp claim again, higher keys;
+ *   k_resolve1  second-pass winners; per-chunk winner and triangle counts;
+ *   k_compact   winners listed in worklist order with their point and
+ *               triangle slots (chunk prefix + block scan);
+ *   k_commit    one thread per winner rewrites its cavity as a fan from the
+ *               new point, relinks the outer ring and re-marks the new
  *               triangles;
  *   k_finish    advances the point/triangle counts and the stop word.
- * Claims make committed cavities disjoint, so commits never race; the round
- * structure is the reference's mark / re-mark / retriangulate loop, with its
- * spin barrier (helpers.h:415) replaced by kernel boundaries.
+ * Two rings may share a triangle (their plans rewrite different edges of it),
+ * and then neither plan's new triangles can hold the other's point, so the
+ * commits of one round equal some sequential order of insertions.
+ * Committed cavities and rings never overlap a cavity, so commits never race;
+ * the round structure is the reference's mark / re-mark / retriangulate loop,
+ * with its spin barrier (helpers.h:415) replaced by kernel boundaries.
  *
  * The result is a function of the input mesh and the arguments alone: every
- * step is deterministic and the arithmetic is IEEE double without fused
- * multiply-adds (this file is compiled with --fmad=false), so it equals the
- * oracle's serial restatement of the same schedule bit for bit.
+ * step is deterministic, new coordinates are IEEE double without fused
+ * multiply-adds (this file is compiled with --fmad=false), and every
+ * geometric decision equals the all-double one (single-precision filters
+ * with proven error bounds, falling back to double), so the result equals
+ * the oracle's serial restatement of the same schedule bit for bit.
  *
  * Rounds are issued in groups with no host synchronisation inside a group;
  * once the stop word is set every kernel returns at once, so surplus rounds
@@ -63,15 +74,18 @@ struct DmrState {
     uint32_t npts, ntri, round, nw;
     uint32_t nbad, stop, winners, added;
     uint32_t pcap, tcap, bcap, max_rounds;
-    uint32_t err, bad_in, pad0, pad1;
+    uint32_t err, bad_in, fits, pad;
     unsigned long long insertions, splits, failed;
 };
 
 struct DmrArgs {
     double *x, *y;
     uint32_t *tri, *nbr, *bad;
-    unsigned long long *owner;
+    unsigned long long *owner; /* cavity claims */
+    unsigned long long *ring;  /* outer-ring claims */
+    uint32_t *lock;            /* round << 2 | 1 (cavity) or 2 (ring) of a first-pass winner */
     uint32_t *work;
+    uint32_t *wlist, *wtri;    /* winners in worklist order, their first new triangle */
     uint32_t *p_mode; /* mode | nc << 8 | nf << 16 */
     double *p_px, *p_py;
     uint32_t *p_cav;  /* [CAV_MAX][B] */
@@ -85,37 +99,90 @@ struct DmrArgs {
 
 __device__ __forceinline__ void set_err(DmrState *st) { atomicCAS(&st->err, 0u, 1u); }
 
-__device__ __forceinline__ double orient(const DmrArgs &a, uint32_t p, uint32_t q, double px, double py) {
-    const double xp = a.x[p], yp = a.y[p], xq = a.x[q], yq = a.y[q];
-    return (xq - xp) * (py - yp) - (yq - yp) * (px - xp);
+/* Predicates.  Each takes the differences the double expression is built
+ * from (computed in double, exactly as the oracle computes them), evaluates
+ * the expression in single precision first, and returns that sign only when
+ * it clears a forward error bound: if |F| exceeds c * eps * M (eps = 2^-24,
+ * M the float sum of the absolute products, c above the bound's constant),
+ * the exact value on the double inputs has F's sign with a margin far above
+ * the double expression's own error, so the double expression has that sign
+ * too.  Otherwise the double expression decides.  So every decision equals
+ * the all-double one, while GB300's few FP64 units see a subtraction and a
+ * conversion per input instead of the whole expression. */
+constexpr float EPSF = 5.9604644775390625e-08f; /* 2^-24 */
+constexpr float TINYF = 1e-30f;                  /* below this, float rounding is not relative */
+
+/* sign of (u1 * v1 - u2 * v2) as double would compute it: the orientation
+ * determinant (q - p) x (r - p) */
+__device__ __forceinline__ int det2_sign(double u1, double v1, double u2, double v2) {
+    const float a1 = (float)u1 * (float)v1, a2 = (float)u2 * (float)v2;
+    const float F = a1 - a2, M = fabsf(a1) + fabsf(a2);
+    if (M > TINYF && fabsf(F) > 8.0f * EPSF * M) return F > 0.0f ? 1 : -1;
+    const double D = u1 * v1 - u2 * v2;
+    return D > 0 ? 1 : (D < 0 ? -1 : 0);
 }
 
-__device__ __forceinline__ double incircle(const DmrArgs &a, uint32_t t, double px, double py) {
+/* sign of the orientation of (p, q, (px, py)) */
+__device__ __forceinline__ int orient_sign(const DmrArgs &a, uint32_t p, uint32_t q, double px, double py) {
+    const double xp = a.x[p], yp = a.y[p], xq = a.x[q], yq = a.y[q];
+    return det2_sign(xq - xp, py - yp, yq - yp, px - xp);
+}
+
+/* sign of the in-circle determinant of counter-clockwise t and (px, py):
+ * > 0 when the point is strictly inside t's circumcircle */
+__device__ __forceinline__ int incircle_sign(const DmrArgs &a, uint32_t t, double px, double py) {
     const uint32_t i0 = a.tri[3 * t], i1 = a.tri[3 * t + 1], i2 = a.tri[3 * t + 2];
     const double adx = a.x[i0] - px, ady = a.y[i0] - py;
     const double bdx = a.x[i1] - px, bdy = a.y[i1] - py;
     const double cdx = a.x[i2] - px, cdy = a.y[i2] - py;
+    {
+        const float ax = (float)adx, ay = (float)ady, bx = (float)bdx, by = (float)bdy, cx = (float)cdx,
+                    cy = (float)cdy;
+        const float ad = ax * ax + ay * ay, bd = bx * bx + by * by, cd = cx * cx + cy * cy;
+        const float F = ax * (by * cd - bd * cy) - ay * (bx * cd - bd * cx) + ad * (bx * cy - by * cx);
+        const float M = fabsf(ax) * (fabsf(by) * cd + bd * fabsf(cy)) + fabsf(ay) * (fabsf(bx) * cd + bd * fabsf(cx)) +
+                        ad * (fabsf(bx * cy) + fabsf(by * cx));
+        if (M > TINYF && fabsf(F) > 32.0f * EPSF * M) return F > 0.0f ? 1 : -1;
+    }
     const double ad = adx * adx + ady * ady, bd = bdx * bdx + bdy * bdy, cd = cdx * cdx + cdy * cdy;
-    return adx * (bdy * cd - bd * cdy) - ady * (bdx * cd - bd * cdx) + ad * (bdx * cdy - bdy * cdx);
+    const double D = adx * (bdy * cd - bd * cdy) - ady * (bdx * cd - bd * cdx) + ad * (bdx * cdy - bdy * cdx);
+    return D > 0 ? 1 : (D < 0 ? -1 : 0);
 }
 
-/* an angle whose cosine exceeds cos(MINANGLE) (checkbad, helpers.h:147-180) */
-__device__ __forceinline__ uint32_t tri_bad(const DmrArgs &a, uint32_t t) {
-    const uint32_t v[3] = {a.tri[3 * t], a.tri[3 * t + 1], a.tri[3 * t + 2]};
-    uint32_t bad = 0;
-#pragma unroll
-    for (uint32_t i = 0; i < 3; ++i) {
-        const uint32_t p = v[i], q = v[(i + 1) % 3], r = v[(i + 2) % 3];
-        const double ux = a.x[q] - a.x[p], uy = a.y[q] - a.y[p];
-        const double wx = a.x[r] - a.x[p], wy = a.y[r] - a.y[p];
-        const double dot = ux * wx + uy * wy;
-        if (!bad && dot > a.cos_bound * sqrt((ux * ux + uy * uy) * (wx * wx + wy * wy))) bad = 1;
+/* the angle between u and w has a cosine above cos(MINANGLE):
+ * dot > cos_bound * sqrt(|u|^2 |w|^2), decided as in double */
+__device__ __forceinline__ bool angle_small(double ux, double uy, double wx, double wy, double cb) {
+    {
+        const float fux = (float)ux, fuy = (float)uy, fwx = (float)wx, fwy = (float)wy;
+        const float p1 = fux * fwx, p2 = fuy * fwy;
+        const float dot = p1 + p2;
+        const float r = (float)cb * sqrtf((fux * fux + fuy * fuy) * (fwx * fwx + fwy * fwy));
+        const float M = fabsf(p1) + fabsf(p2) + r, diff = dot - r;
+        if (M > TINYF && fabsf(diff) > 16.0f * EPSF * M) return diff > 0.0f;
     }
-    return bad;
+    const double dot = ux * wx + uy * wy;
+    return dot > cb * sqrt((ux * ux + uy * uy) * (wx * wx + wy * wy));
+}
+
+/* an angle whose cosine exceeds cos(MINANGLE) (checkbad, helpers.h:147-180);
+ * an edge vector from q to p is the negated one from p to q, as IEEE
+ * subtraction is antisymmetric, so three differences serve all angles */
+__device__ __forceinline__ uint32_t tri_bad(const DmrArgs &a, uint32_t t) {
+    const uint32_t v0 = a.tri[3 * t], v1 = a.tri[3 * t + 1], v2 = a.tri[3 * t + 2];
+    const double x0 = a.x[v0], y0 = a.y[v0], x1 = a.x[v1], y1 = a.y[v1], x2 = a.x[v2], y2 = a.y[v2];
+    const double ex01 = x1 - x0, ey01 = y1 - y0, ex02 = x2 - x0, ey02 = y2 - y0, ex12 = x2 - x1, ey12 = y2 - y1;
+    /* angle at v0: (v1 - v0, v2 - v0); at v1: (v2 - v1, v0 - v1); at v2: (v0 - v2, v1 - v2) */
+    return angle_small(ex01, ey01, ex02, ey02, a.cos_bound) || angle_small(ex12, ey12, -ex01, -ey01, a.cos_bound) ||
+           angle_small(-ex02, -ey02, -ex12, -ey12, a.cos_bound);
 }
 
 __device__ __forceinline__ uint32_t round_prio(uint32_t t, uint32_t round) {
     return (t ^ (round * 0x9E3779B9u)) * 0x85EBCA6Bu; /* a bijection of t */
+}
+
+/* pass 0 and 1 keys of a round, above every key of earlier rounds */
+__device__ __forceinline__ unsigned long long claim_key(uint32_t t, uint32_t round, uint32_t pass) {
+    return ((unsigned long long)(2 * round + pass) << 32) | round_prio(t, round);
 }
 
 /* Contiguous chunk of [0, n) for block b of G. */
@@ -229,7 +296,7 @@ __device__ bool grow_cavity(const DmrArgs &a, uint32_t k, uint32_t ntri, double 
                 bool in = false;
                 for (uint32_t j = 0; j < nc; ++j) in |= cav[j] == o;
                 if (in) continue;
-                if (incircle(a, o, px, py) > 0) {
+                if (incircle_sign(a, o, px, py) > 0) {
                     if (nc == CAV_MAX) return false;
                     cav[nc++] = o;
                     continue;
@@ -258,7 +325,7 @@ __device__ bool fan_ok(const DmrArgs &a, uint32_t k, uint32_t mode, uint32_t nc,
     if (nf != nc + (mode == PLAN_SPLIT ? 1u : 2u)) return false;
     for (uint32_t j = 0; j < nf; ++j) {
         const uint4 f = a.p_fan[(size_t)j * a.B + k];
-        if (!(orient(a, f.x, f.y, px, py) > 0)) return false;
+        if (orient_sign(a, f.x, f.y, px, py) <= 0) return false;
         for (uint32_t i = 0; i < j; ++i)
             if (a.p_fan[(size_t)i * a.B + k].x == f.x) return false;
     }
@@ -274,7 +341,7 @@ __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
         const uint32_t t = a.work[k];
         uint32_t mode = PLAN_FAIL, nc = 0, nf = 0;
-        const unsigned long long key = ((unsigned long long)round << 32) | round_prio(t, round);
+        const unsigned long long key = claim_key(t, round, 0);
         /* circumcentre (same expression order as the oracle) */
         const uint32_t v0 = a.tri[3 * t], v1 = a.tri[3 * t + 1], v2 = a.tri[3 * t + 2];
         const double bx = a.x[v1] - a.x[v0], by = a.y[v1] - a.y[v0];
@@ -288,7 +355,7 @@ __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
         for (; step < WALK_MAX; ++step) {
             uint32_t cross = 3;
             for (uint32_t i = 0; i < 3 && cross == 3; ++i)
-                if (orient(a, a.tri[3 * cur + (i + 1) % 3], a.tri[3 * cur + (i + 2) % 3], px, py) < 0) cross = i;
+                if (orient_sign(a, a.tri[3 * cur + (i + 1) % 3], a.tri[3 * cur + (i + 2) % 3], px, py) < 0) cross = i;
             if (cross == 3) break;
             const uint32_t n = a.nbr[3 * cur + cross];
             if (n == NONE) {
@@ -340,7 +407,7 @@ __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
         }
         for (uint32_t j = 0; j < nf; ++j) {
             const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
-            if (o != NONE) atomicMax(a.owner + o, key);
+            if (o != NONE) atomicMax(a.ring + o, key);
         }
     }
     if (fails) atomicAdd(&st->failed, (unsigned long long)fails);
@@ -348,25 +415,75 @@ __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
 
 /* -------------------------------------------------------- resolve, commit */
 
-__global__ void __launch_bounds__(SCAN_BS) k_resolve(DmrArgs a) {
+/* No higher key on k's cavity (in either table) or on its ring's cavity
+ * claims. */
+__device__ __forceinline__ bool holds(const DmrArgs &a, uint32_t k, uint32_t nc, uint32_t nf,
+                                      unsigned long long key) {
+    for (uint32_t j = 0; j < nc; ++j) {
+        const uint32_t t = a.p_cav[(size_t)j * a.B + k];
+        if (a.owner[t] != key || a.ring[t] >= key) return false;
+    }
+    for (uint32_t j = 0; j < nf; ++j) {
+        const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+        if (o != NONE && a.owner[o] >= key) return false;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(PLAN_BS) k_resolve0(DmrArgs a) {
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE) return;
+    const uint32_t nw = st->nw, round = st->round, stamp = round << 2;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
+        const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16;
+        const uint32_t win = (pm & 0xFF) != PLAN_FAIL && holds(a, k, nc, nf, claim_key(a.work[k], round, 0));
+        a.p_win[k] = win;
+        if (!win) continue;
+        for (uint32_t j = 0; j < nc; ++j) a.lock[a.p_cav[(size_t)j * a.B + k]] = stamp | 1;
+        for (uint32_t j = 0; j < nf; ++j) {
+            const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+            if (o != NONE) a.lock[o] = stamp | 2;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(PLAN_BS) k_reclaim(DmrArgs a) {
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE) return;
+    const uint32_t nw = st->nw, round = st->round, stamp = round << 2;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
+        const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16;
+        if ((pm & 0xFF) == PLAN_FAIL || a.p_win[k]) continue;
+        bool blocked = false;
+        for (uint32_t j = 0; j < nc && !blocked; ++j) blocked = (a.lock[a.p_cav[(size_t)j * a.B + k]] >> 2) == round;
+        for (uint32_t j = 0; j < nf && !blocked; ++j) {
+            const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+            blocked = o != NONE && a.lock[o] == (stamp | 1);
+        }
+        if (blocked) {
+            a.p_win[k] = 2;
+            continue;
+        }
+        const unsigned long long key = claim_key(a.work[k], round, 1);
+        for (uint32_t j = 0; j < nc; ++j) atomicMax(a.owner + a.p_cav[(size_t)j * a.B + k], key);
+        for (uint32_t j = 0; j < nf; ++j) {
+            const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+            if (o != NONE) atomicMax(a.ring + o, key);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_BS) k_resolve1(DmrArgs a) {
     __shared__ uint32_t ws[32];
     DmrState *st = a.st;
     if (st->stop != STOP_NONE || st->nw == 0) return;
-    const unsigned long long rk = (unsigned long long)st->round << 32;
+    const uint32_t round = st->round;
     uint32_t lo, hi, wins = 0, need = 0;
     chunk_of(st->nw, blockIdx.x, a.G, lo, hi);
     for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
-        const uint32_t pm = a.p_mode[k], mode = pm & 0xFF, nc = (pm >> 8) & 0xFF, nf = pm >> 16;
-        uint32_t win = 0;
-        if (mode != PLAN_FAIL) {
-            const unsigned long long key = rk | round_prio(a.work[k], st->round);
-            win = 1;
-            for (uint32_t j = 0; j < nc && win; ++j) win = a.owner[a.p_cav[(size_t)j * a.B + k]] == key;
-            for (uint32_t j = 0; j < nf && win; ++j) {
-                const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
-                win = o == NONE || a.owner[o] == key;
-            }
-        }
+        const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16, w = a.p_win[k];
+        const uint32_t win = w == 1 || (w == 0 && (pm & 0xFF) != PLAN_FAIL &&
+                                        holds(a, k, nc, nf, claim_key(a.work[k], round, 1)));
         a.p_win[k] = win;
         wins += win;
         need += win ? nf - nc : 0;
@@ -387,17 +504,22 @@ __device__ __forceinline__ bool round_fits(const DmrArgs &a, uint32_t *ws, uint3
     return W > 0 && (uint64_t)st->npts + W <= st->pcap && (uint64_t)st->ntri + A <= st->tcap;
 }
 
-__global__ void __launch_bounds__(SCAN_BS) k_commit(DmrArgs a) {
+__global__ void __launch_bounds__(SCAN_BS) k_compact(DmrArgs a) {
     __shared__ uint32_t ws[32];
     DmrState *st = a.st;
     if (st->stop != STOP_NONE || st->nw == 0) return;
     uint32_t W, A;
-    if (!round_fits(a, ws, W, A)) return;
+    const bool fits = round_fits(a, ws, W, A);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->winners = W;
+        st->added = A;
+        st->fits = fits;
+    }
+    if (!fits) return;
     uint32_t wbase = prefix_of(a, 1, blockIdx.x, ws), abase = prefix_of(a, 2, blockIdx.x, ws);
-    const uint32_t npts = st->npts, ntri = st->ntri;
-    uint32_t lo, hi, ins = 0, spl = 0;
+    const uint32_t ntri = st->ntri;
+    uint32_t lo, hi;
     chunk_of(st->nw, blockIdx.x, a.G, lo, hi);
-    uint32_t slot[FAN_MAX], fa[FAN_MAX], fb[FAN_MAX];
     for (uint32_t k0 = lo; k0 < hi; k0 += blockDim.x) {
         const uint32_t k = k0 + threadIdx.x;
         uint32_t win = 0, pm = 0;
@@ -405,82 +527,86 @@ __global__ void __launch_bounds__(SCAN_BS) k_commit(DmrArgs a) {
             win = a.p_win[k];
             pm = a.p_mode[k];
         }
-        const uint32_t nc = (pm >> 8) & 0xFF, nf = pm >> 16;
         uint32_t wt, at;
         const uint32_t wpre = block_exclusive_scan(win, ws, &wt);
-        __syncthreads();
-        const uint32_t apre = block_exclusive_scan(win ? nf - nc : 0, ws, &at);
-        __syncthreads();
+        const uint32_t apre = block_exclusive_scan(win ? (pm >> 16) - ((pm >> 8) & 0xFF) : 0, ws, &at);
         if (win) {
-            const uint32_t pid = npts + wbase + wpre, tb = ntri + abase + apre;
-            a.x[pid] = a.p_px[k];
-            a.y[pid] = a.p_py[k];
-            for (uint32_t j = 0; j < nf; ++j) {
-                slot[j] = j < nc ? a.p_cav[(size_t)j * a.B + k] : tb + (j - nc);
-                const uint4 f = a.p_fan[(size_t)j * a.B + k];
-                fa[j] = f.x;
-                fb[j] = f.y;
-            }
-            for (uint32_t j = 0; j < nf; ++j) {
-                const uint4 f = a.p_fan[(size_t)j * a.B + k];
-                const uint32_t s = slot[j];
-                uint32_t n0 = NONE, n1 = NONE;
-                for (uint32_t i = 0; i < nf; ++i) {
-                    if (fa[i] == fb[j]) n0 = slot[i];
-                    if (fb[i] == fa[j]) n1 = slot[i];
-                }
-                a.tri[3 * (size_t)s] = f.x;
-                a.tri[3 * (size_t)s + 1] = f.y;
-                a.tri[3 * (size_t)s + 2] = pid;
-                a.nbr[3 * (size_t)s] = n0;
-                a.nbr[3 * (size_t)s + 1] = n1;
-                a.nbr[3 * (size_t)s + 2] = f.z;
-                if (f.z != NONE) a.nbr[3 * (size_t)f.z + f.w] = s;
-            }
-            for (uint32_t j = 0; j < nf; ++j) a.bad[slot[j]] = tri_bad(a, slot[j]);
-            if ((pm & 0xFF) == PLAN_SPLIT) ++spl;
-            else ++ins;
+            a.wlist[wbase + wpre] = k;
+            a.wtri[wbase + wpre] = ntri + abase + apre;
         }
         wbase += wt;
         abase += at;
+    }
+}
+
+__global__ void __launch_bounds__(PLAN_BS) k_commit(DmrArgs a) {
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE || st->nw == 0 || !st->fits) return;
+    const uint32_t W = st->winners, npts = st->npts;
+    uint32_t ins = 0, spl = 0;
+    uint32_t slot[FAN_MAX], fa[FAN_MAX], fb[FAN_MAX];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < W; i += gridDim.x * blockDim.x) {
+        const uint32_t k = a.wlist[i], pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16;
+        const uint32_t pid = npts + i, tb = a.wtri[i];
+        a.x[pid] = a.p_px[k];
+        a.y[pid] = a.p_py[k];
+        for (uint32_t j = 0; j < nf; ++j) {
+            slot[j] = j < nc ? a.p_cav[(size_t)j * a.B + k] : tb + (j - nc);
+            const uint4 f = a.p_fan[(size_t)j * a.B + k];
+            fa[j] = f.x;
+            fb[j] = f.y;
+        }
+        for (uint32_t j = 0; j < nf; ++j) {
+            const uint4 f = a.p_fan[(size_t)j * a.B + k];
+            const uint32_t s = slot[j];
+            uint32_t n0 = NONE, n1 = NONE;
+            for (uint32_t q = 0; q < nf; ++q) {
+                if (fa[q] == fb[j]) n0 = slot[q];
+                if (fb[q] == fa[j]) n1 = slot[q];
+            }
+            a.tri[3 * (size_t)s] = f.x;
+            a.tri[3 * (size_t)s + 1] = f.y;
+            a.tri[3 * (size_t)s + 2] = pid;
+            a.nbr[3 * (size_t)s] = n0;
+            a.nbr[3 * (size_t)s + 1] = n1;
+            a.nbr[3 * (size_t)s + 2] = f.z;
+            if (f.z != NONE) a.nbr[3 * (size_t)f.z + f.w] = s;
+        }
+        for (uint32_t j = 0; j < nf; ++j) a.bad[slot[j]] = tri_bad(a, slot[j]);
+        if ((pm & 0xFF) == PLAN_SPLIT) ++spl;
+        else ++ins;
     }
     if (ins) atomicAdd(&st->insertions, (unsigned long long)ins);
     if (spl) atomicAdd(&st->splits, (unsigned long long)spl);
 }
 
-__global__ void __launch_bounds__(SCAN_BS) k_finish(DmrArgs a) {
-    __shared__ uint32_t ws[32];
+__global__ void k_finish(DmrArgs a) {
     DmrState *st = a.st;
     if (st->stop != STOP_NONE) return;
     if (st->err) {
-        if (threadIdx.x == 0) st->stop = STOP_ERROR;
+        st->stop = STOP_ERROR;
         return;
     }
     if (st->nw == 0) return;
-    uint32_t W, A;
-    const bool fits = round_fits(a, ws, W, A);
-    if (threadIdx.x == 0) {
-        st->winners = W;
-        st->added = A;
-        if (W == 0) st->stop = STOP_STALLED;
-        else if (!fits) st->stop = STOP_CAPACITY;
-        else {
-            st->npts += W;
-            st->ntri += A;
-        }
+    if (st->winners == 0) st->stop = STOP_STALLED;
+    else if (!st->fits) st->stop = STOP_CAPACITY;
+    else {
+        st->npts += st->winners;
+        st->ntri += st->added;
     }
 }
 
 struct DmrBufs {
     double *x = nullptr, *y = nullptr, *p_px = nullptr, *p_py = nullptr;
     uint32_t *tri = nullptr, *nbr = nullptr, *bad = nullptr, *work = nullptr, *p_mode = nullptr, *p_cav = nullptr,
-             *p_win = nullptr, *bsum = nullptr;
+             *p_win = nullptr, *bsum = nullptr, *lock = nullptr, *wlist = nullptr, *wtri = nullptr;
     uint4 *p_fan = nullptr;
-    unsigned long long *owner = nullptr;
+    unsigned long long *owner = nullptr, *ring = nullptr;
     DmrState *st = nullptr;
     DmrState *hst = nullptr; /* pinned */
     void free_all(cudaStream_t s) {
-        void *p[] = {x, y, p_px, p_py, tri, nbr, bad, work, p_mode, p_cav, p_win, bsum, p_fan, owner, st};
+        void *p[] = {x, y, p_px, p_py, tri, nbr, bad, work, p_mode, p_cav, p_win, bsum, lock, wlist, wtri, p_fan, owner,
+                     ring, st};
         for (void *q : p)
             if (q) cudaFreeAsync(q, s);
         if (hst) cudaFreeHost(hst);
@@ -502,7 +628,8 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     gga_status r;
     if ((r = dalloc(&b.x, pcap, s)) || (r = dalloc(&b.y, pcap, s)) || (r = dalloc(&b.tri, 3 * (size_t)tcap, s)) ||
         (r = dalloc(&b.nbr, 3 * (size_t)tcap, s)) || (r = dalloc(&b.bad, tcap, s)) ||
-        (r = dalloc(&b.owner, tcap, s)) || (r = dalloc(&b.work, B, s)) || (r = dalloc(&b.p_mode, B, s)) ||
+        (r = dalloc(&b.owner, tcap, s)) || (r = dalloc(&b.ring, tcap, s)) || (r = dalloc(&b.lock, tcap, s)) ||
+        (r = dalloc(&b.wlist, B, s)) || (r = dalloc(&b.wtri, B, s)) || (r = dalloc(&b.work, B, s)) || (r = dalloc(&b.p_mode, B, s)) ||
         (r = dalloc(&b.p_px, B, s)) || (r = dalloc(&b.p_py, B, s)) || (r = dalloc(&b.p_cav, (size_t)CAV_MAX * B, s)) ||
         (r = dalloc(&b.p_fan, (size_t)FAN_MAX * B, s)) || (r = dalloc(&b.p_win, B, s)) ||
         (r = dalloc(&b.bsum, 3 * (size_t)G, s)) || (r = dalloc(&b.st, 1, s)))
@@ -521,6 +648,8 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     GGA_CK(cudaMemcpyAsync(b.tri, m->tri, (size_t)m->ntri * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     GGA_CK(cudaMemcpyAsync(b.nbr, m->nbr, (size_t)m->ntri * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     GGA_CK(cudaMemsetAsync(b.owner, 0, (size_t)tcap * sizeof(unsigned long long), s));
+    GGA_CK(cudaMemsetAsync(b.ring, 0, (size_t)tcap * sizeof(unsigned long long), s));
+    GGA_CK(cudaMemsetAsync(b.lock, 0, (size_t)tcap * sizeof(uint32_t), s));
 
     DmrArgs a;
     a.x = b.x;
@@ -529,6 +658,10 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     a.nbr = b.nbr;
     a.bad = b.bad;
     a.owner = b.owner;
+    a.ring = b.ring;
+    a.lock = b.lock;
+    a.wlist = b.wlist;
+    a.wtri = b.wtri;
     a.work = b.work;
     a.p_mode = b.p_mode;
     a.p_px = b.p_px;
@@ -550,9 +683,12 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
             k_bad_count<<<G, SCAN_BS, 0, s>>>(a);
             k_bad_gather<<<G, SCAN_BS, 0, s>>>(a);
             k_plan<<<plan_grid, PLAN_BS, 0, s>>>(a);
-            k_resolve<<<G, SCAN_BS, 0, s>>>(a);
-            k_commit<<<G, SCAN_BS, 0, s>>>(a);
-            k_finish<<<1, SCAN_BS, 0, s>>>(a);
+            k_resolve0<<<plan_grid, PLAN_BS, 0, s>>>(a);
+            k_reclaim<<<plan_grid, PLAN_BS, 0, s>>>(a);
+            k_resolve1<<<G, SCAN_BS, 0, s>>>(a);
+            k_compact<<<G, SCAN_BS, 0, s>>>(a);
+            k_commit<<<plan_grid, PLAN_BS, 0, s>>>(a);
+            k_finish<<<1, 1, 0, s>>>(a);
         }
         GGA_CK(cudaGetLastError());
         issued += ROUND_GROUP;

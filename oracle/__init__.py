@@ -72,6 +72,8 @@ def load():
     lib.oracle_gen_grid.argtypes = [U, U, D, D, C.c_uint64, U, U]
     lib.oracle_mesh_refine.restype = C.c_int
     lib.oracle_mesh_refine.argtypes = [P, P, P, P, P, P, U, U, D, U, U, P]
+    lib.oracle_mesh_refine_log.restype = C.c_int
+    lib.oracle_mesh_refine_log.argtypes = [P, P, P, P, P, P, U, U, D, U, U, P, P, U]
     lib.oracle_mesh_count_bad.restype = C.c_uint64
     lib.oracle_mesh_count_bad.argtypes = [U, P, P, P, D]
     lib.gga_mesh_gen_jittered.restype = C.c_int
@@ -302,12 +304,14 @@ def mesh_refine(mesh: dict, min_angle_deg: float = 25.0, max_triangles: int = 0,
     N = np.zeros(3 * tcap, np.uint32); N[:3 * ntri] = nbr
     np_, nt_ = C.c_uint32(npts), C.c_uint32(ntri)
     st = np.zeros(6, np.uint64)
-    rc = load().oracle_mesh_refine(C.byref(np_), C.byref(nt_), _p(X), _p(Y), _p(T), _p(N), pcap, tcap,
-                                   cos_bound(min_angle_deg), batch_cap, max_rounds, _p(st))
+    log = np.zeros(3 * 4096, np.uint32)
+    rc = load().oracle_mesh_refine_log(C.byref(np_), C.byref(nt_), _p(X), _p(Y), _p(T), _p(N), pcap, tcap,
+                                       cos_bound(min_angle_deg), batch_cap, max_rounds, _p(st), _p(log), 4096)
     P, Tn = np_.value, nt_.value
     return {"x": X[:P].copy(), "y": Y[:P].copy(), "tri": T[:3 * Tn].copy(), "nbr": N[:3 * Tn].copy(),
             "status": MESH_STATUS.get(rc, str(rc)), "rounds": int(st[0]), "insertions": int(st[1]),
-            "boundary_splits": int(st[2]), "failed_plans": int(st[3]), "bad_in": int(st[4]), "bad_out": int(st[5])}
+            "boundary_splits": int(st[2]), "failed_plans": int(st[3]), "bad_in": int(st[4]), "bad_out": int(st[5]),
+            "round_log": log[:3 * min(int(st[0]), 4096)].reshape(-1, 3).copy()}
 
 
 def mesh_count_bad(mesh: dict, min_angle_deg: float = 25.0) -> int:

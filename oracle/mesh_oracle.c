@@ -26,6 +26,18 @@
  * order (built with -ffp-contract=off, the kernels with --fmad=false, so no
  * multiply-add is fused on either side).
  *
+ * Claims.  A plan claims its cavity and its outer ring (the triangles across
+ * the cavity's boundary, whose neighbour links it rewrites) in two separate
+ * tables.  Two plans conflict when their cavities meet or one's cavity meets
+ * the other's ring; two rings may share a triangle, since the plans rewrite
+ * different edges of it, and then neither plan's new triangles can hold the
+ * other's point (a fan triangle's circumcircle lies inside the union of the
+ * circles of the two triangles that shared its outer edge, one in the cavity
+ * and one in the ring), so the commits equal some sequential order.  A plan
+ * wins a pass when it holds the highest key on every conflicting claim.  A
+ * second pass lets the plans that lost, and touch no first-pass winner's
+ * cavity or ring, claim again among themselves with higher keys.
+ *
  * The reference runs in float (FORD, dmr.cu:36) with a thread schedule that
  * decides which of two conflicting cavities wins, so its own output is not
  * reproducible run to run; parity with it is the mesh's properties (no bad
@@ -99,6 +111,11 @@ static uint32_t round_prio(uint32_t t, uint32_t round) {
     return (t ^ (round * 0x9E3779B9u)) * 0x85EBCA6Bu; /* a bijection of t */
 }
 
+/* pass 0 and 1 keys of a round, above every key of earlier rounds */
+static uint64_t claim_key(uint32_t t, uint32_t round, uint32_t pass) {
+    return ((uint64_t)(2 * round + pass) << 32) | round_prio(t, round);
+}
+
 /* The cavity of (px, py) grown from seed; skip_m/skip_i name the boundary
  * edge being split (left out of the fan).  Returns 0 when a limit is hit. */
 static int grow_cavity(const Mesh *m, Plan *p, uint32_t seed, uint32_t skip_m, uint32_t skip_i) {
@@ -148,7 +165,7 @@ static int fan_ok(const Mesh *m, const Plan *p) {
 
 static void plan_one(const Mesh *m, uint32_t t, uint32_t round, Plan *p) {
     p->mode = PLAN_FAIL;
-    p->key = ((uint64_t)round << 32) | round_prio(t, round);
+    p->key = claim_key(t, round, 0);
     circumcentre(m, t, &p->px, &p->py);
     uint32_t cur = t, split_m = NONE, split_i = 0, step = 0;
     for (; step < WALK_MAX; ++step) {
@@ -199,6 +216,23 @@ static void plan_one(const Mesh *m, uint32_t t, uint32_t round, Plan *p) {
     if (!fan_ok(m, p)) p->mode = PLAN_FAIL;
 }
 
+static void claim(const Mesh *m, const Plan *p, uint64_t *owner, uint64_t *ring) {
+    (void)m;
+    for (uint32_t j = 0; j < p->nc; ++j)
+        if (owner[p->cav[j]] < p->key) owner[p->cav[j]] = p->key;
+    for (uint32_t j = 0; j < p->nf; ++j)
+        if (p->fo[j] != NONE && ring[p->fo[j]] < p->key) ring[p->fo[j]] = p->key;
+}
+
+/* no higher key on this plan's cavity (in either table) or on its ring's
+ * cavity claims */
+static uint8_t holds(const Plan *p, const uint64_t *owner, const uint64_t *ring) {
+    uint32_t ok = 1;
+    for (uint32_t j = 0; j < p->nc; ++j) ok &= owner[p->cav[j]] == p->key && ring[p->cav[j]] < p->key;
+    for (uint32_t j = 0; j < p->nf; ++j) ok &= p->fo[j] == NONE || owner[p->fo[j]] < p->key;
+    return (uint8_t)ok;
+}
+
 static void commit(Mesh *m, uint8_t *bad, const Plan *p, uint32_t pid, uint32_t tbase, double cos_bound) {
     uint32_t slot[FAN_MAX];
     for (uint32_t j = 0; j < p->nf; ++j) slot[j] = j < p->nc ? p->cav[j] : tbase + (j - p->nc);
@@ -223,26 +257,35 @@ static void commit(Mesh *m, uint8_t *bad, const Plan *p, uint32_t pid, uint32_t 
 }
 
 /* stats: [0] rounds, [1] insertions, [2] boundary splits, [3] failed plans,
- *        [4] bad before, [5] bad after */
-int oracle_mesh_refine(uint32_t *npts, uint32_t *ntri, double *x, double *y, uint32_t *tri, uint32_t *nbr,
-                       uint32_t pcap, uint32_t tcap, double cos_bound, uint32_t batch_cap, uint32_t max_rounds,
-                       uint64_t *stats) {
+ *        [4] bad before, [5] bad after.
+ * log (optional, 3 words per round up to log_cap rounds): bad triangles at
+ * the round's start, plans made, plans committed (dmr.cu:323 prints the
+ * same per-iteration counts). */
+int oracle_mesh_refine_log(uint32_t *npts, uint32_t *ntri, double *x, double *y, uint32_t *tri, uint32_t *nbr,
+                           uint32_t pcap, uint32_t tcap, double cos_bound, uint32_t batch_cap, uint32_t max_rounds,
+                           uint64_t *stats, uint32_t *log, uint32_t log_cap) {
     Mesh m = {*npts, *ntri, x, y, tri, nbr};
     memset(stats, 0, 6 * sizeof(uint64_t));
     uint8_t *bad = (uint8_t *)calloc(tcap ? tcap : 1, 1);
-    uint64_t *owner = (uint64_t *)calloc(tcap ? tcap : 1, sizeof(uint64_t));
+    uint64_t *owner = (uint64_t *)calloc(tcap ? tcap : 1, sizeof(uint64_t)); /* cavity claims */
+    uint64_t *ring = (uint64_t *)calloc(tcap ? tcap : 1, sizeof(uint64_t));  /* outer-ring claims */
+    uint32_t *lock = (uint32_t *)calloc(tcap ? tcap : 1, sizeof(uint32_t));  /* round << 2 | kind of a winner's claim */
+    uint8_t *won = (uint8_t *)calloc(batch_cap ? batch_cap : 1, 1);
     uint32_t *work = (uint32_t *)malloc((size_t)(tcap ? tcap : 1) * sizeof(uint32_t));
     Plan *plans = (Plan *)malloc((size_t)(batch_cap ? batch_cap : 1) * sizeof(Plan));
     int st = ST_OK;
-    if (!bad || !owner || !work || !plans) st = ST_NOMEM;
+    if (!bad || !owner || !ring || !lock || !won || !work || !plans) st = ST_NOMEM;
     uint64_t nb = 0;
     for (uint32_t t = 0; t < m.ntri && !st; ++t) nb += bad[t] = (uint8_t)tri_bad(&m, t, cos_bound);
     stats[4] = nb;
     uint32_t round = 0;
     while (!st) {
-        uint32_t nw = 0;
+        uint32_t nw = 0, nbad = 0;
         for (uint32_t t = 0; t < m.ntri; ++t)
-            if (bad[t] && nw < batch_cap) work[nw++] = t;
+            if (bad[t]) {
+                ++nbad;
+                if (nw < batch_cap) work[nw++] = t;
+            }
         if (nw == 0) break;
         if (round == max_rounds) {
             st = ST_ROUNDS;
@@ -252,29 +295,61 @@ int oracle_mesh_refine(uint32_t *npts, uint32_t *ntri, double *x, double *y, uin
         for (uint32_t k = 0; k < nw; ++k) {
             Plan *p = plans + k;
             plan_one(&m, work[k], round, p);
-            if (p->mode == PLAN_FAIL) continue;
-            for (uint32_t j = 0; j < p->nc; ++j)
-                if (owner[p->cav[j]] < p->key) owner[p->cav[j]] = p->key;
-            for (uint32_t j = 0; j < p->nf; ++j)
-                if (p->fo[j] != NONE && owner[p->fo[j]] < p->key) owner[p->fo[j]] = p->key;
+            if (p->mode != PLAN_FAIL) claim(&m, p, owner, ring);
         }
+        /* pass 0; its winners stamp their cavity (kind 1) and ring (kind 2) */
         uint32_t wins = 0, add = 0, fails = 0;
+        const uint32_t stamp = round << 2;
         for (uint32_t k = 0; k < nw; ++k) {
             Plan *p = plans + k;
+            won[k] = 0;
             if (p->mode == PLAN_FAIL) {
                 ++fails;
                 continue;
             }
-            uint32_t ok = 1;
-            for (uint32_t j = 0; j < p->nc; ++j) ok &= owner[p->cav[j]] == p->key;
-            for (uint32_t j = 0; j < p->nf; ++j) ok &= p->fo[j] == NONE || owner[p->fo[j]] == p->key;
-            if (!ok) p->mode = PLAN_FAIL; /* lost to a higher key this round */
-            else {
-                ++wins;
-                add += p->nf - p->nc;
+            won[k] = holds(p, owner, ring);
+        }
+        for (uint32_t k = 0; k < nw; ++k) {
+            const Plan *p = plans + k;
+            if (!won[k]) continue;
+            for (uint32_t j = 0; j < p->nc; ++j) lock[p->cav[j]] = stamp | 1;
+            for (uint32_t j = 0; j < p->nf; ++j)
+                if (p->fo[j] != NONE) lock[p->fo[j]] = stamp | 2;
+        }
+        /* pass 1: plans clear of the stamps claim again */
+        for (uint32_t k = 0; k < nw; ++k) {
+            Plan *p = plans + k;
+            if (p->mode == PLAN_FAIL || won[k]) continue;
+            uint32_t blocked = 0;
+            for (uint32_t j = 0; j < p->nc; ++j) blocked |= (lock[p->cav[j]] >> 2) == round;
+            for (uint32_t j = 0; j < p->nf; ++j) blocked |= p->fo[j] != NONE && lock[p->fo[j]] == (stamp | 1);
+            if (blocked) {
+                won[k] = 2;
+                continue;
             }
+            p->key = claim_key(work[k], round, 1);
+            claim(&m, p, owner, ring);
+        }
+        for (uint32_t k = 0; k < nw; ++k) {
+            Plan *p = plans + k;
+            if (p->mode == PLAN_FAIL || won[k] == 1) continue;
+            won[k] = won[k] == 0 && holds(p, owner, ring);
+        }
+        for (uint32_t k = 0; k < nw; ++k) {
+            Plan *p = plans + k;
+            if (won[k] != 1) {
+                if (p->mode != PLAN_FAIL) p->mode = PLAN_FAIL; /* lost this round */
+                continue;
+            }
+            ++wins;
+            add += p->nf - p->nc;
         }
         stats[3] += fails;
+        if (log && round <= log_cap) {
+            log[3 * (round - 1)] = nbad;
+            log[3 * (round - 1) + 1] = nw;
+            log[3 * (round - 1) + 2] = wins;
+        }
         if (wins == 0) {
             st = ST_STALLED;
             break;
@@ -303,9 +378,19 @@ int oracle_mesh_refine(uint32_t *npts, uint32_t *ntri, double *x, double *y, uin
     *ntri = m.ntri;
     free(bad);
     free(owner);
+    free(ring);
+    free(lock);
+    free(won);
     free(work);
     free(plans);
     return st;
+}
+
+int oracle_mesh_refine(uint32_t *npts, uint32_t *ntri, double *x, double *y, uint32_t *tri, uint32_t *nbr,
+                       uint32_t pcap, uint32_t tcap, double cos_bound, uint32_t batch_cap, uint32_t max_rounds,
+                       uint64_t *stats) {
+    return oracle_mesh_refine_log(npts, ntri, x, y, tri, nbr, pcap, tcap, cos_bound, batch_cap, max_rounds, stats,
+                                  NULL, 0);
 }
 
 /* bad-triangle count of a mesh (the initial marking of dmr.cu:128-150) */

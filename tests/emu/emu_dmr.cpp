@@ -23,9 +23,9 @@ int main(int argc, char **argv) {
     const uint32_t B = bcap < tcap ? bcap : tcap;
     std::vector<double> x(pcap), y(pcap), px(B), py(B);
     std::vector<uint32_t> tri(3 * (size_t)tcap), nbr(3 * (size_t)tcap), bad(tcap), work(B), pm(B), pc((size_t)CAV_MAX * B),
-        pw(B), bsum(3 * G);
+        pw(B), bsum(3 * G), lock(tcap, 0), wlist(B), wtri(B);
     std::vector<uint4> pf((size_t)FAN_MAX * B);
-    std::vector<unsigned long long> owner(tcap, 0);
+    std::vector<unsigned long long> owner(tcap, 0), ring(tcap, 0);
     std::copy(x0.begin(), x0.end(), x.begin());
     std::copy(y0.begin(), y0.end(), y.begin());
     std::copy(t0.begin(), t0.end(), tri.begin());
@@ -34,7 +34,8 @@ int main(int argc, char **argv) {
     memset(&st, 0, sizeof st);
     st.npts = npts; st.ntri = ntri; st.pcap = pcap; st.tcap = tcap; st.bcap = B; st.max_rounds = MAX_ROUNDS;
     DmrArgs a;
-    a.x = x.data(); a.y = y.data(); a.tri = tri.data(); a.nbr = nbr.data(); a.bad = bad.data(); a.owner = owner.data();
+    a.x = x.data(); a.y = y.data(); a.tri = tri.data(); a.nbr = nbr.data(); a.bad = bad.data(); a.owner = owner.data(); a.ring = ring.data(); a.lock = lock.data();
+    a.wlist = wlist.data(); a.wtri = wtri.data();
     a.work = work.data(); a.p_mode = pm.data(); a.p_px = px.data(); a.p_py = py.data(); a.p_cav = pc.data();
     a.p_fan = pf.data(); a.p_win = pw.data(); a.bsum = bsum.data(); a.st = &st; a.cos_bound = cb; a.B = B; a.G = G;
     LAUNCH(k_mark_all, G, BS);
@@ -42,9 +43,12 @@ int main(int argc, char **argv) {
         LAUNCH(k_bad_count, G, BS);
         LAUNCH(k_bad_gather, G, BS);
         LAUNCH(k_plan, 2, PBS);
-        LAUNCH(k_resolve, G, BS);
-        LAUNCH(k_commit, G, BS);
-        LAUNCH(k_finish, 1, BS);
+        LAUNCH(k_resolve0, 2, PBS);
+        LAUNCH(k_reclaim, 2, PBS);
+        LAUNCH(k_resolve1, G, BS);
+        LAUNCH(k_compact, G, BS);
+        LAUNCH(k_commit, 2, PBS);
+        LAUNCH(k_finish, 1, 1);
     }
     wr(d + "/out_x.bin", x.data(), st.npts);
     wr(d + "/out_y.bin", y.data(), st.npts);

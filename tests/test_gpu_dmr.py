@@ -73,7 +73,7 @@ def test_refine_capacity_limit_keeps_last_complete_round(ctx):
     mesh = gga.Mesh.random(3000, seed=3)
     before = mesh.arrays()
     ntri = len(before["tri"]) // 3
-    cap = ntri + 800
+    cap = ntri + 3000
     with pytest.raises(gga.GGAError) as ex:
         ctx.refine(mesh, max_triangles=cap)
     assert ex.value.status == gga.ERR_TOO_LARGE

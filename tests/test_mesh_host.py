@@ -175,8 +175,8 @@ def test_oracle_refinement_is_deterministic_and_batch_cap_changes_only_the_sched
 def test_oracle_capacity_stop_keeps_the_last_complete_round():
     m = oracle.mesh_gen_random(1500, 3)
     ntri = len(m["tri"]) // 3
-    r = oracle.mesh_refine(m, max_triangles=ntri + 300)
-    assert r["status"] == "capacity" and ntri < len(r["tri"]) // 3 <= ntri + 300
+    r = oracle.mesh_refine(m, max_triangles=ntri + 1500)
+    assert r["status"] == "capacity" and ntri < len(r["tri"]) // 3 <= ntri + 1500
     c = _valid(r)
     assert c["bad_triangles"] == r["bad_out"] > 0
 
