@@ -28,6 +28,12 @@ parity   the GPU distances of that sample (the timed step's own call and
          likewise the 4096^2 grid configuration (grid4096: GTEPS, roofline,
          parity against an exact FIFO-BFS / Dijkstra checker).  Any mismatch
          makes the run exit non-zero after printing its line.
+mesh_refinement  Delaunay refinement (the reference's DMR program) of a
+         random 1M-point mesh of the unit square (2,000,002 triangles, about
+         35% with an angle below 25 degrees): device time, end-to-end time
+         through the C ABI, rounds, the refined mesh's checks, and the
+         oracle's serial run of the same schedule as CPU baseline and
+         bit-for-bit parity (points, triangles, neighbours).
 
 --impl reference times that CPU path alone (the reference's implementation of
 the path; it has no other runnable form on this machine) on the same metric,
@@ -74,6 +80,8 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-query and serving sections")
     ap.add_argument("--no-grid", action="store_true", help="skip the 4096^2 grid section")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="offered-load duration per Poisson rate")
+    ap.add_argument("--no-mesh", action="store_true", help="skip the Delaunay mesh refinement section")
+    ap.add_argument("--mesh-points", type=int, default=1000000, help="random points of the refinement workload")
     return ap.parse_args()
 
 
@@ -583,6 +591,51 @@ def grid_section(gga, ctx, peak: float):
     return g, out, res
 
 
+def mesh_section(gga, ctx, npoints: int, reps: int = 3):
+    """Delaunay refinement of a random-point mesh to a 25-degree minimum angle
+    (the reference's DMR run, Kepler_DMR/dmr.cu:54-398).  device_ms is the
+    rounds' CUDA-event time inside gga_mesh_refine; e2e_ms is the whole call
+    through the C ABI with the mesh in host memory (upload, rounds,
+    download).  Returns the section, the input arrays and the refined arrays."""
+    base = gga.Mesh.random(npoints, seed=1)
+    before = base.arrays()
+    del base
+    ctx.refine(gga.Mesh.random(20000, seed=2))  # warm-up: module load, memory pools
+    runs = []
+    for _ in range(reps):
+        m = gga.Mesh.from_arrays(before["x"], before["y"], before["tri"])
+        runs.append(ctx.refine(m))
+    st = runs[-1]
+    dev = sorted(r["device_ms"] for r in runs)[len(runs) // 2]
+    e2e = sorted(r["total_ms"] for r in runs)[len(runs) // 2]
+    after = m.arrays()
+    chk = m.check()
+    # the size of the reference's own recorded runs (Kepler_DMR/result.vi: input
+    # N5L.1, 956,752 triangles of which 438,841 bad, 11-13 iterations); that
+    # mesh file is not in the reference, a random mesh of the same size stands in
+    ref_runs = [ctx.refine(gga.Mesh.random(478375, seed=3)) for _ in range(2)]
+    rr = ref_runs[-1]
+    ref_sized = {"triangles_in": rr["triangles_in"], "bad_in": rr["bad_in"], "triangles_out": rr["triangles_out"],
+                 "bad_out": rr["bad_out"], "rounds": rr["rounds"], "device_ms": rr["device_ms"],
+                 "e2e_ms": rr["total_ms"],
+                 "reference_recorded": {"input": "N5L.1", "triangles_in": 956752, "bad_in": 438841,
+                                        "runtime_ms": {"r_dmr": 2670.0, "m_dmr_a": 2030.0, "m_dmr": 1810.0,
+                                                       "m_dmr_LB": 1740.0, "m_dmr_LB_D": 2760.0},
+                                        "hardware": "the thesis's Kepler GPU (result.vi)"}}
+    out = {"workload": f"random {npoints}-point Delaunay mesh of the unit square, refined to a 25-degree "
+                       f"minimum angle", "triangles_in": st["triangles_in"], "bad_in": st["bad_in"],
+           "triangles_out": st["triangles_out"], "points_out": st["points_out"], "bad_out": st["bad_out"],
+           "rounds": st["rounds"], "insertions": st["insertions"], "boundary_splits": st["boundary_splits"],
+           "failed_plans": st["failed_plans"], "device_ms": dev, "e2e_ms": e2e, "runs": reps,
+           "device_mtri_per_s": st["triangles_out"] / dev / 1e3, "dtype": "f64 (f32 filters)",
+           "identical_runs": all(r["triangles_out"] == st["triangles_out"] and r["rounds"] == st["rounds"]
+                                 for r in runs),
+           "check": {k: chk[k] for k in ("bad_triangles", "bad_orientation", "bad_neighbors",
+                                          "non_delaunay_edges", "boundary_edges")} | {"area": chk["area"]},
+           "reference_sized": ref_sized}
+    return out, before, after
+
+
 def parity_check(pairs, check_fn) -> dict:
     """pairs: {(src, algo): gpu distances}; check_fn(src, algo) -> oracle
     distances.  Counts traversals whose arrays differ anywhere."""
@@ -783,6 +836,15 @@ def run_gga(args, dist: Dist):
         except Exception as e:
             out["serving"] = {"error": repr(e)}
 
+    mesh = None
+    if not args.no_mesh and dist.rank == 0:
+        try:
+            mesh = mesh_section(gga, ctx, args.mesh_points)
+            out["mesh_refinement"] = mesh[0]
+        except Exception as e:  # reported, not fatal
+            out["mesh_refinement"] = {"error": repr(e)}
+            mesh = None
+
     parity_ok = True
     if checks:
         import oracle
@@ -827,6 +889,34 @@ def run_gga(args, dist: Dist):
                                             "every golden graph)", "oracle_s": time.perf_counter() - t0, **gp,
                                   "verify_errors": gout["bfs"]["verify_errors"] + gout["sssp"]["verify_errors"]}
                 parity_ok = parity_ok and gp["mismatches"] == 0 and gout["parity"]["verify_errors"] == 0
+        if mesh is not None:
+            # the oracle's serial restatement of the same round schedule, one
+            # host core: the CPU baseline and the bit-for-bit check
+            mout, before, after = mesh
+            box = {}
+
+            def mesh_oracle():
+                t0 = time.perf_counter()
+                box["r"] = oracle.mesh_refine(before)
+                box["s"] = time.perf_counter() - t0
+
+            th = threading.Thread(target=mesh_oracle, daemon=True)
+            th.start()
+            th.join(timeout=300)
+            if th.is_alive():
+                mout["parity"] = {"timeout_s": 300}
+                parity_ok = False
+            else:
+                want = box["r"]
+                same = all(len(after[k]) == len(want[k]) and np.array_equal(after[k], want[k])
+                           for k in ("x", "y", "tri", "nbr"))
+                mout["parity"] = {"oracle": "serial restatement of the round schedule (oracle/mesh_oracle.c)",
+                                  "identical_points_triangles_neighbours": same, "oracle_status": want["status"]}
+                mout["cpu_baseline"] = {"value_ms": box["s"] * 1e3, "cores": 1, "kind": "port",
+                                        "sample": "the whole refinement, serial"}
+                mout["vs_cpu_baseline"] = box["s"] * 1e3 / mout["device_ms"]
+                parity_ok = parity_ok and same and mout["check"]["bad_triangles"] == 0 and \
+                    mout["check"]["non_delaunay_edges"] == 0
     out["parity_ok"] = parity_ok
     ctx.close()
     return out

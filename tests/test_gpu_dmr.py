@@ -132,3 +132,32 @@ def test_refine_rejects_bad_arguments(ctx):
     with pytest.raises(gga.GGAError) as ex:
         ctx.refine(mesh, max_triangles=10)
     assert ex.value.status == gga.ERR_INVALID_ARG
+
+
+def test_dmr_cli_drop_in(tmp_path):
+    """r_dmr <basefilename> (dmr.cu:81-84): the reference's summary lines and
+    its 9-column result.vi row; GGA_DMR_OUT writes the refined mesh, which
+    equals the oracle's refinement of the input."""
+    import os
+    import subprocess
+
+    src = gga.Mesh.random(3000, seed=12)
+    base = str(tmp_path / "r3000")
+    src.save(base)
+    before = src.arrays()
+    exe = os.path.join(os.path.dirname(gga.__file__), "bin", "r_dmr")
+    env = dict(os.environ, GGA_DMR_OUT=str(tmp_path / "out"))
+    r = subprocess.run([exe, base], cwd=tmp_path, capture_output=True, text=True, timeout=120, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[0] == "reading graphs..." and lines[1].strip() == "3004 nodes"
+    assert lines[2].strip() == f"{2 * 3004 - 6} triangles."
+    assert "verification succeeded: 0 bad triangles exist." in lines
+    want = oracle.mesh_refine(before)
+    row = (tmp_path / "result.vi").read_text().strip().split(",")
+    assert row[:7] == ["r_dmr", "r3000", str(2 * 3004 - 6), str(want["bad_in"]), str(len(want["tri"]) // 3), "0",
+                       str(want["rounds"])]
+    assert float(row[7]) >= float(row[8]) > 0 and row[9] == ""
+    got = gga.Mesh.load(str(tmp_path / "out")).arrays()
+    for k in ("x", "y", "tri"):
+        np.testing.assert_array_equal(got[k], want[k], err_msg=k)

@@ -189,3 +189,16 @@ def test_oracle_refinement_other_angle_bounds(angle):
     assert _valid(r, angle)["bad_triangles"] == 0
     assert _angles_deg(r).min() >= angle - 1e-9
     assert math.isclose(oracle.cos_bound(angle), math.cos(math.radians(angle)), rel_tol=1e-15)
+
+
+def test_dmr_cli_usage_and_missing_input_need_no_device(tmp_path):
+    import os
+    import subprocess
+
+    exe = os.path.join(os.path.dirname(gga.__file__), "bin", "r_dmr")
+    if not os.path.exists(exe):
+        pytest.skip("gga_dmr not built")
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and r.stdout.startswith("Usage: ")
+    r = subprocess.run([exe, str(tmp_path / "none")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "cannot open" in r.stderr
