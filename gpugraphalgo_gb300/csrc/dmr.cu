@@ -80,6 +80,7 @@ struct DmrState {
 
 struct DmrArgs {
     double *x, *y;
+    float4 *pq;                /* per point (xh, yh, xl, yl): float pairs of the coordinates (predicate filters) */
     uint32_t *tri, *nbr, *bad;
     unsigned long long *owner; /* cavity claims */
     unsigned long long *ring;  /* outer-ring claims */
@@ -94,86 +95,136 @@ struct DmrArgs {
     uint32_t *bsum;   /* [3][G] */
     DmrState *st;
     double cos_bound;
+    float cos_bound_f; /* cos_bound rounded to float */
+    float S;           /* bound on every point's |x| and |y| (rounded up) */
     uint32_t B, G;
 };
 
 __device__ __forceinline__ void set_err(DmrState *st) { atomicCAS(&st->err, 0u, 1u); }
 
-/* Predicates.  Each takes the differences the double expression is built
- * from (computed in double, exactly as the oracle computes them), evaluates
- * the expression in single precision first, and returns that sign only when
- * it clears a forward error bound: if |F| exceeds c * eps * M (eps = 2^-24,
- * M the float sum of the absolute products, c above the bound's constant),
- * the exact value on the double inputs has F's sign with a margin far above
- * the double expression's own error, so the double expression has that sign
- * too.  Otherwise the double expression decides.  So every decision equals
- * the all-double one, while GB300's few FP64 units see a subtraction and a
- * conversion per input instead of the whole expression. */
+/* Predicates.  Every geometric decision must equal the sign of the all-double
+ * expression the oracle evaluates (on the double differences of double
+ * coordinates).  Each predicate first evaluates its expression in single
+ * precision and returns that sign only when |F| exceeds twice a bound on its
+ * distance from the exact value on the double differences.
+ *
+ * Float inputs.  Every point keeps its coordinates as float pairs (hi =
+ * x rounded to float, lo = the rest rounded to float; x = hi + lo within
+ * eps^2 |x|, eps = 2^-24), one float4 (xh, yh, xl, yl) per point.  A
+ * difference is (hi_a - hi_b) + (lo_a - lo_b) in float: within
+ * D = 2.02 eps (L + 3 eps A) of the double difference, L the largest float
+ * difference of the test and A a bound on the coordinates' magnitudes
+ * (their rounding, eps |d| each for the two float additions, eps^2 terms
+ * for the lo parts, 2^-53 |d| for the double subtraction).
+ *
+ * Bound.  A product of k differences then moves by at most
+ * k D (L + D)^(k-1), so the expression moves by the sum over its monomials
+ * (orientation: 2 of degree 2, 4 D (L + D); in-circle: 12 of degree 4,
+ * 48 D (L + D)^3; the angle test: 8 D (L + D)), plus the float evaluation's
+ * own rounding, c eps M, M the float sum of the absolute products.  Past
+ * twice that bound the exact value has F's sign with a margin far above the
+ * double expression's own error (about 11 2^-53 M), so the double
+ * expression has it too.  Otherwise, or when L leaves [1e-9, 1e8] (where
+ * float products could underflow or overflow), the double expression
+ * decides.  GB300 runs FP64 at 1/64 of FP32; with these filters its FP64
+ * pipe is left the new coordinates and the rare undecided cases, and a warp
+ * seldom has a lane that needs them. */
 constexpr float EPSF = 5.9604644775390625e-08f; /* 2^-24 */
-constexpr float TINYF = 1e-30f;                  /* below this, float rounding is not relative */
+constexpr float LMIN = 1e-9f, LMAX = 1e8f;
 
-/* sign of (u1 * v1 - u2 * v2) as double would compute it: the orientation
- * determinant (q - p) x (r - p) */
-__device__ __forceinline__ int det2_sign(double u1, double v1, double u2, double v2) {
-    const float a1 = (float)u1 * (float)v1, a2 = (float)u2 * (float)v2;
-    const float F = a1 - a2, M = fabsf(a1) + fabsf(a2);
-    if (M > TINYF && fabsf(F) > 8.0f * EPSF * M) return F > 0.0f ? 1 : -1;
-    const double D = u1 * v1 - u2 * v2;
+__device__ __forceinline__ float fmax4(float a, float b, float c, float d) {
+    return fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fabsf(c), fabsf(d)));
+}
+
+/* the point's float pair, and a double point's */
+__device__ __forceinline__ float4 fpair(const DmrArgs &a, uint32_t i) { return a.pq[i]; }
+__device__ __forceinline__ float4 fpair_of(double x, double y) {
+    const float xh = (float)x, yh = (float)y;
+    return make_float4(xh, yh, (float)(x - (double)xh), (float)(y - (double)yh));
+}
+__device__ __forceinline__ float fdx(const float4 &p, const float4 &q) { return (p.x - q.x) + (p.z - q.z); }
+__device__ __forceinline__ float fdy(const float4 &p, const float4 &q) { return (p.y - q.y) + (p.w - q.w); }
+__device__ __forceinline__ float err_d(float L, float A) { return 2.02f * EPSF * (L + 3.0f * EPSF * A); }
+
+/* sign of the orientation of (p, q, pt): (q - p) x (pt - p) */
+__device__ __forceinline__ int orient_sign(const DmrArgs &a, uint32_t p, uint32_t q, double px, double py,
+                                           const float4 &pt, float A) {
+    {
+        const float4 fp = fpair(a, p), fq = fpair(a, q);
+        const float u1 = fdx(fq, fp), v1 = fdy(pt, fp), u2 = fdy(fq, fp), v2 = fdx(pt, fp);
+        const float a1 = u1 * v1, a2 = u2 * v2, F = a1 - a2;
+        const float L = fmax4(u1, v1, u2, v2), D = err_d(L, A);
+        const float B = 4.0f * D * (L + D) + 3.0f * EPSF * (fabsf(a1) + fabsf(a2));
+        if (L > LMIN && L < LMAX && fabsf(F) > 2.01f * B) return F > 0.0f ? 1 : -1;
+    }
+    const double xp = a.x[p], yp = a.y[p], xq = a.x[q], yq = a.y[q];
+    const double D = (xq - xp) * (py - yp) - (yq - yp) * (px - xp);
     return D > 0 ? 1 : (D < 0 ? -1 : 0);
 }
 
-/* sign of the orientation of (p, q, (px, py)) */
-__device__ __forceinline__ int orient_sign(const DmrArgs &a, uint32_t p, uint32_t q, double px, double py) {
-    const double xp = a.x[p], yp = a.y[p], xq = a.x[q], yq = a.y[q];
-    return det2_sign(xq - xp, py - yp, yq - yp, px - xp);
-}
-
-/* sign of the in-circle determinant of counter-clockwise t and (px, py):
- * > 0 when the point is strictly inside t's circumcircle */
-__device__ __forceinline__ int incircle_sign(const DmrArgs &a, uint32_t t, double px, double py) {
+/* sign of the in-circle determinant of counter-clockwise t and pt: > 0 when
+ * the point is strictly inside t's circumcircle */
+__device__ __forceinline__ int incircle_sign(const DmrArgs &a, uint32_t t, double px, double py, const float4 &pt,
+                                             float A) {
     const uint32_t i0 = a.tri[3 * t], i1 = a.tri[3 * t + 1], i2 = a.tri[3 * t + 2];
-    const double adx = a.x[i0] - px, ady = a.y[i0] - py;
-    const double bdx = a.x[i1] - px, bdy = a.y[i1] - py;
-    const double cdx = a.x[i2] - px, cdy = a.y[i2] - py;
     {
-        const float ax = (float)adx, ay = (float)ady, bx = (float)bdx, by = (float)bdy, cx = (float)cdx,
-                    cy = (float)cdy;
+        const float4 f0 = fpair(a, i0), f1 = fpair(a, i1), f2 = fpair(a, i2);
+        const float ax = fdx(f0, pt), ay = fdy(f0, pt), bx = fdx(f1, pt), by = fdy(f1, pt);
+        const float cx = fdx(f2, pt), cy = fdy(f2, pt);
         const float ad = ax * ax + ay * ay, bd = bx * bx + by * by, cd = cx * cx + cy * cy;
         const float F = ax * (by * cd - bd * cy) - ay * (bx * cd - bd * cx) + ad * (bx * cy - by * cx);
         const float M = fabsf(ax) * (fabsf(by) * cd + bd * fabsf(cy)) + fabsf(ay) * (fabsf(bx) * cd + bd * fabsf(cx)) +
                         ad * (fabsf(bx * cy) + fabsf(by * cx));
-        if (M > TINYF && fabsf(F) > 32.0f * EPSF * M) return F > 0.0f ? 1 : -1;
+        const float L = fmaxf(fmax4(ax, ay, bx, by), fmaxf(fabsf(cx), fabsf(cy)));
+        const float D = err_d(L, A), LD = L + D;
+        const float B = 48.0f * D * LD * LD * LD + 12.0f * EPSF * M;
+        if (L > LMIN && L < LMAX && fabsf(F) > 2.01f * B) return F > 0.0f ? 1 : -1;
     }
+    const double adx = a.x[i0] - px, ady = a.y[i0] - py;
+    const double bdx = a.x[i1] - px, bdy = a.y[i1] - py;
+    const double cdx = a.x[i2] - px, cdy = a.y[i2] - py;
     const double ad = adx * adx + ady * ady, bd = bdx * bdx + bdy * bdy, cd = cdx * cdx + cdy * cdy;
     const double D = adx * (bdy * cd - bd * cdy) - ady * (bdx * cd - bd * cdx) + ad * (bdx * cdy - bdy * cdx);
     return D > 0 ? 1 : (D < 0 ? -1 : 0);
 }
 
-/* the angle between u and w has a cosine above cos(MINANGLE):
- * dot > cos_bound * sqrt(|u|^2 |w|^2), decided as in double */
-__device__ __forceinline__ bool angle_small(double ux, double uy, double wx, double wy, double cb) {
-    {
-        const float fux = (float)ux, fuy = (float)uy, fwx = (float)wx, fwy = (float)wy;
-        const float p1 = fux * fwx, p2 = fuy * fwy;
-        const float dot = p1 + p2;
-        const float r = (float)cb * sqrtf((fux * fux + fuy * fuy) * (fwx * fwx + fwy * fwy));
-        const float M = fabsf(p1) + fabsf(p2) + r, diff = dot - r;
-        if (M > TINYF && fabsf(diff) > 16.0f * EPSF * M) return diff > 0.0f;
-    }
+/* the angle between u and w has a cosine above cos(MINANGLE): the float
+ * decision (1 or 0) when it is certain, else -1 */
+__device__ __forceinline__ int angle_small_f(float ux, float uy, float wx, float wy, float cbf, float A) {
+    const float p1 = ux * wx, p2 = uy * wy, dot = p1 + p2;
+    const float r = cbf * sqrtf((ux * ux + uy * uy) * (wx * wx + wy * wy)), diff = dot - r;
+    const float L = fmax4(ux, uy, wx, wy), D = err_d(L, A);
+    const float B = 8.0f * D * (L + D) + 10.0f * EPSF * (fabsf(p1) + fabsf(p2) + r);
+    if (L > LMIN && L < LMAX && fabsf(diff) > 2.01f * B) return diff > 0.0f;
+    return -1;
+}
+
+__device__ __forceinline__ bool angle_small_d(double ux, double uy, double wx, double wy, double cb) {
     const double dot = ux * wx + uy * wy;
     return dot > cb * sqrt((ux * ux + uy * uy) * (wx * wx + wy * wy));
 }
 
 /* an angle whose cosine exceeds cos(MINANGLE) (checkbad, helpers.h:147-180);
- * an edge vector from q to p is the negated one from p to q, as IEEE
- * subtraction is antisymmetric, so three differences serve all angles */
+ * an edge vector from q to p is the negated one from p to q (IEEE
+ * subtraction and the float pair sums are antisymmetric), so three
+ * differences serve all angles */
 __device__ __forceinline__ uint32_t tri_bad(const DmrArgs &a, uint32_t t) {
     const uint32_t v0 = a.tri[3 * t], v1 = a.tri[3 * t + 1], v2 = a.tri[3 * t + 2];
+    const float A = 2.0f * a.S;
+    const float4 f0 = fpair(a, v0), f1 = fpair(a, v1), f2 = fpair(a, v2);
+    const float gx01 = fdx(f1, f0), gy01 = fdy(f1, f0), gx02 = fdx(f2, f0), gy02 = fdy(f2, f0);
+    const float gx12 = fdx(f2, f1), gy12 = fdy(f2, f1);
+    /* angle at v0: (v1 - v0, v2 - v0); at v1: (v2 - v1, v0 - v1); at v2: (v0 - v2, v1 - v2) */
+    const int s0 = angle_small_f(gx01, gy01, gx02, gy02, a.cos_bound_f, A);
+    const int s1 = angle_small_f(gx12, gy12, -gx01, -gy01, a.cos_bound_f, A);
+    const int s2 = angle_small_f(-gx02, -gy02, -gx12, -gy12, a.cos_bound_f, A);
+    if (s0 == 1 || s1 == 1 || s2 == 1) return 1;
+    if (s0 == 0 && s1 == 0 && s2 == 0) return 0;
     const double x0 = a.x[v0], y0 = a.y[v0], x1 = a.x[v1], y1 = a.y[v1], x2 = a.x[v2], y2 = a.y[v2];
     const double ex01 = x1 - x0, ey01 = y1 - y0, ex02 = x2 - x0, ey02 = y2 - y0, ex12 = x2 - x1, ey12 = y2 - y1;
-    /* angle at v0: (v1 - v0, v2 - v0); at v1: (v2 - v1, v0 - v1); at v2: (v0 - v2, v1 - v2) */
-    return angle_small(ex01, ey01, ex02, ey02, a.cos_bound) || angle_small(ex12, ey12, -ex01, -ey01, a.cos_bound) ||
-           angle_small(-ex02, -ey02, -ex12, -ey12, a.cos_bound);
+    return (s0 < 0 && angle_small_d(ex01, ey01, ex02, ey02, a.cos_bound)) ||
+           (s1 < 0 && angle_small_d(ex12, ey12, -ex01, -ey01, a.cos_bound)) ||
+           (s2 < 0 && angle_small_d(-ex02, -ey02, -ex12, -ey12, a.cos_bound));
 }
 
 __device__ __forceinline__ uint32_t round_prio(uint32_t t, uint32_t round) {
@@ -209,6 +260,13 @@ __device__ __forceinline__ uint32_t prefix_of(const DmrArgs &a, uint32_t row, ui
 }
 
 /* ---------------------------------------------------------------- marking */
+
+__global__ void __launch_bounds__(SCAN_BS) k_shadow(DmrArgs a) {
+    const uint32_t n = a.st->npts;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        a.pq[i] = fpair_of(a.x[i], a.y[i]);
+    }
+}
 
 __global__ void __launch_bounds__(SCAN_BS) k_mark_all(DmrArgs a) {
     const uint32_t n = a.st->ntri;
@@ -279,8 +337,9 @@ __global__ void __launch_bounds__(SCAN_BS) k_bad_gather(DmrArgs a) {
 
 /* The cavity of (px, py) grown from seed (the oracle's grow_cavity, same
  * visiting order).  Fan entries go to the plan record; cav stays local. */
-__device__ bool grow_cavity(const DmrArgs &a, uint32_t k, uint32_t ntri, double px, double py, uint32_t seed,
-                            uint32_t skip_m, uint32_t skip_i, uint32_t *cav, uint32_t &nc, uint32_t &nf) {
+__device__ bool grow_cavity(const DmrArgs &a, uint32_t k, uint32_t ntri, double px, double py, const float4 &pt,
+                            float A, uint32_t seed, uint32_t skip_m, uint32_t skip_i, uint32_t *cav, uint32_t &nc,
+                            uint32_t &nf) {
     nc = 1;
     nf = 0;
     cav[0] = seed;
@@ -296,7 +355,7 @@ __device__ bool grow_cavity(const DmrArgs &a, uint32_t k, uint32_t ntri, double 
                 bool in = false;
                 for (uint32_t j = 0; j < nc; ++j) in |= cav[j] == o;
                 if (in) continue;
-                if (incircle_sign(a, o, px, py) > 0) {
+                if (incircle_sign(a, o, px, py, pt, A) > 0) {
                     if (nc == CAV_MAX) return false;
                     cav[nc++] = o;
                     continue;
@@ -321,11 +380,11 @@ __device__ bool grow_cavity(const DmrArgs &a, uint32_t k, uint32_t ntri, double 
 }
 
 __device__ bool fan_ok(const DmrArgs &a, uint32_t k, uint32_t mode, uint32_t nc, uint32_t nf, double px,
-                       double py) {
+                       double py, const float4 &pt, float A) {
     if (nf != nc + (mode == PLAN_SPLIT ? 1u : 2u)) return false;
     for (uint32_t j = 0; j < nf; ++j) {
         const uint4 f = a.p_fan[(size_t)j * a.B + k];
-        if (orient_sign(a, f.x, f.y, px, py) <= 0) return false;
+        if (orient_sign(a, f.x, f.y, px, py, pt, A) <= 0) return false;
         for (uint32_t i = 0; i < j; ++i)
             if (a.p_fan[(size_t)i * a.B + k].x == f.x) return false;
     }
@@ -350,12 +409,15 @@ __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
         const double b2 = bx * bx + by * by, c2 = cx * cx + cy * cy;
         double px = a.x[v0] + (cy * b2 - by * c2) / d;
         double py = a.y[v0] + (bx * c2 - cx * b2) / d;
+        float4 pt = fpair_of(px, py);
+        float A = a.S + fmaxf(a.S, fmaxf(fabsf(pt.x), fabsf(pt.y)));
         uint32_t cur = t, split_m = NONE, split_i = 0, step = 0;
         bool ok = true;
         for (; step < WALK_MAX; ++step) {
             uint32_t cross = 3;
             for (uint32_t i = 0; i < 3 && cross == 3; ++i)
-                if (orient_sign(a, a.tri[3 * cur + (i + 1) % 3], a.tri[3 * cur + (i + 2) % 3], px, py) < 0) cross = i;
+                if (orient_sign(a, a.tri[3 * cur + (i + 1) % 3], a.tri[3 * cur + (i + 2) % 3], px, py, pt, A) < 0)
+                    cross = i;
             if (cross == 3) break;
             const uint32_t n = a.nbr[3 * cur + cross];
             if (n == NONE) {
@@ -372,7 +434,7 @@ __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
         }
         if (step == WALK_MAX) ok = false;
         if (ok && split_m == NONE) {
-            ok = grow_cavity(a, k, ntri, px, py, cur, NONE, 0, cav, nc, nf);
+            ok = grow_cavity(a, k, ntri, px, py, pt, A, cur, NONE, 0, cav, nc, nf);
             for (uint32_t j = 0; ok && j < nf && split_m == NONE; ++j) {
                 const uint4 f = a.p_fan[(size_t)j * a.B + k];
                 if (f.z != NONE) continue;
@@ -383,7 +445,7 @@ __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
                 }
             }
             if (ok && split_m == NONE) {
-                mode = fan_ok(a, k, PLAN_INSERT, nc, nf, px, py) ? PLAN_INSERT : PLAN_FAIL;
+                mode = fan_ok(a, k, PLAN_INSERT, nc, nf, px, py, pt, A) ? PLAN_INSERT : PLAN_FAIL;
                 ok = false; /* done */
             }
         }
@@ -391,8 +453,10 @@ __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
             const uint32_t e0 = a.tri[3 * split_m + (split_i + 1) % 3], e1 = a.tri[3 * split_m + (split_i + 2) % 3];
             px = (a.x[e0] + a.x[e1]) * 0.5;
             py = (a.y[e0] + a.y[e1]) * 0.5;
-            if (grow_cavity(a, k, ntri, px, py, split_m, split_m, split_i, cav, nc, nf))
-                mode = fan_ok(a, k, PLAN_SPLIT, nc, nf, px, py) ? PLAN_SPLIT : PLAN_FAIL;
+            pt = fpair_of(px, py);
+            A = 2.0f * a.S;
+            if (grow_cavity(a, k, ntri, px, py, pt, A, split_m, split_m, split_i, cav, nc, nf))
+                mode = fan_ok(a, k, PLAN_SPLIT, nc, nf, px, py, pt, A) ? PLAN_SPLIT : PLAN_FAIL;
         }
         a.p_mode[k] = mode | nc << 8 | nf << 16;
         if (mode == PLAN_FAIL) {
@@ -548,8 +612,10 @@ __global__ void __launch_bounds__(PLAN_BS) k_commit(DmrArgs a) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < W; i += gridDim.x * blockDim.x) {
         const uint32_t k = a.wlist[i], pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16;
         const uint32_t pid = npts + i, tb = a.wtri[i];
-        a.x[pid] = a.p_px[k];
-        a.y[pid] = a.p_py[k];
+        const double npx = a.p_px[k], npy = a.p_py[k];
+        a.x[pid] = npx;
+        a.y[pid] = npy;
+        a.pq[pid] = fpair_of(npx, npy);
         for (uint32_t j = 0; j < nf; ++j) {
             slot[j] = j < nc ? a.p_cav[(size_t)j * a.B + k] : tb + (j - nc);
             const uint4 f = a.p_fan[(size_t)j * a.B + k];
@@ -598,6 +664,7 @@ __global__ void k_finish(DmrArgs a) {
 
 struct DmrBufs {
     double *x = nullptr, *y = nullptr, *p_px = nullptr, *p_py = nullptr;
+    float4 *pq = nullptr;
     uint32_t *tri = nullptr, *nbr = nullptr, *bad = nullptr, *work = nullptr, *p_mode = nullptr, *p_cav = nullptr,
              *p_win = nullptr, *bsum = nullptr, *lock = nullptr, *wlist = nullptr, *wtri = nullptr;
     uint4 *p_fan = nullptr;
@@ -605,7 +672,7 @@ struct DmrBufs {
     DmrState *st = nullptr;
     DmrState *hst = nullptr; /* pinned */
     void free_all(cudaStream_t s) {
-        void *p[] = {x, y, p_px, p_py, tri, nbr, bad, work, p_mode, p_cav, p_win, bsum, lock, wlist, wtri, p_fan, owner,
+        void *p[] = {x, y, pq, p_px, p_py, tri, nbr, bad, work, p_mode, p_cav, p_win, bsum, lock, wlist, wtri, p_fan, owner,
                      ring, st};
         for (void *q : p)
             if (q) cudaFreeAsync(q, s);
@@ -626,7 +693,7 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     const uint32_t B = bcap < tcap ? bcap : tcap;
     const uint32_t G = (uint32_t)(c->sms > 0 ? 2 * c->sms : 304);
     gga_status r;
-    if ((r = dalloc(&b.x, pcap, s)) || (r = dalloc(&b.y, pcap, s)) || (r = dalloc(&b.tri, 3 * (size_t)tcap, s)) ||
+    if ((r = dalloc(&b.x, pcap, s)) || (r = dalloc(&b.y, pcap, s)) || (r = dalloc(&b.pq, pcap, s)) || (r = dalloc(&b.tri, 3 * (size_t)tcap, s)) ||
         (r = dalloc(&b.nbr, 3 * (size_t)tcap, s)) || (r = dalloc(&b.bad, tcap, s)) ||
         (r = dalloc(&b.owner, tcap, s)) || (r = dalloc(&b.ring, tcap, s)) || (r = dalloc(&b.lock, tcap, s)) ||
         (r = dalloc(&b.wlist, B, s)) || (r = dalloc(&b.wtri, B, s)) || (r = dalloc(&b.work, B, s)) || (r = dalloc(&b.p_mode, B, s)) ||
@@ -654,6 +721,7 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     DmrArgs a;
     a.x = b.x;
     a.y = b.y;
+    a.pq = b.pq;
     a.tri = b.tri;
     a.nbr = b.nbr;
     a.bad = b.bad;
@@ -672,11 +740,18 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     a.bsum = b.bsum;
     a.st = b.st;
     a.cos_bound = cos_bound;
+    a.cos_bound_f = (float)cos_bound;
+    /* every point's |x|, |y| (new points stay inside the input's bounding box),
+     * rounded up to float */
+    double smax = 0;
+    for (uint32_t i = 0; i < m->npts; ++i) smax = fmax(smax, fmax(fabs(m->x[i]), fabs(m->y[i])));
+    a.S = (float)(smax * (1.0 + 1.0 / 1048576.0)) + 1e-30f;
     a.B = B;
     a.G = G;
     const unsigned plan_grid = ctx_grid(c, B, PLAN_BS);
     cudaEvent_t e0 = c->ev[0], e1 = c->ev[1];
     GGA_CK(cudaEventRecord(e0, s));
+    k_shadow<<<G, SCAN_BS, 0, s>>>(a);
     k_mark_all<<<G, SCAN_BS, 0, s>>>(a);
     for (uint32_t issued = 0;;) {
         for (uint32_t g = 0; g < ROUND_GROUP; ++g) {

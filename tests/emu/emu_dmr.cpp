@@ -22,6 +22,7 @@ int main(int argc, char **argv) {
     const uint32_t npts = x0.size(), ntri = t0.size() / 3, pcap = npts + (tcap - ntri);
     const uint32_t B = bcap < tcap ? bcap : tcap;
     std::vector<double> x(pcap), y(pcap), px(B), py(B);
+    std::vector<float4> pq(pcap);
     std::vector<uint32_t> tri(3 * (size_t)tcap), nbr(3 * (size_t)tcap), bad(tcap), work(B), pm(B), pc((size_t)CAV_MAX * B),
         pw(B), bsum(3 * G), lock(tcap, 0), wlist(B), wtri(B);
     std::vector<uint4> pf((size_t)FAN_MAX * B);
@@ -38,6 +39,11 @@ int main(int argc, char **argv) {
     a.wlist = wlist.data(); a.wtri = wtri.data();
     a.work = work.data(); a.p_mode = pm.data(); a.p_px = px.data(); a.p_py = py.data(); a.p_cav = pc.data();
     a.p_fan = pf.data(); a.p_win = pw.data(); a.bsum = bsum.data(); a.st = &st; a.cos_bound = cb; a.B = B; a.G = G;
+    a.pq = pq.data(); a.cos_bound_f = (float)cb;
+    double smax = 0;
+    for (uint32_t i = 0; i < npts; ++i) smax = std::max(smax, std::max(std::fabs(x[i]), std::fabs(y[i])));
+    a.S = (float)(smax * (1.0 + 1.0 / 1048576.0)) + 1e-30f;
+    LAUNCH(k_shadow, G, BS);
     LAUNCH(k_mark_all, G, BS);
     for (uint32_t r = 0; st.stop == STOP_NONE && r < 4096; ++r) {
         LAUNCH(k_bad_count, G, BS);

@@ -55,7 +55,7 @@ def generate(which):
                                [("extern __shared__ uint32_t dyn[];", "uint32_t *dyn")])
     elif which == "dmr":
         body = transform("dmr.cu", "constexpr uint32_t NONE", "struct DmrBufs",
-                         ["k_mark_all", "k_bad_count", "k_bad_gather", "k_plan", "k_resolve0", "k_reclaim", "k_resolve1",
+                         ["k_shadow", "k_mark_all", "k_bad_count", "k_bad_gather", "k_plan", "k_resolve0", "k_reclaim", "k_resolve1",
                           "k_compact", "k_commit", "k_finish"], [])
     else:
         raise SystemExit("unknown kernel " + which)

@@ -116,6 +116,8 @@ inline uint32_t max(uint32_t a, uint32_t b) { return a > b ? a : b; }
 #define GGA_INFINITY 1000000000u
 #define GGA_MESH_NONE 0xFFFFFFFFu
 struct uint4 { uint32_t x, y, z, w; };
+struct float4 { float x, y, z, w; };
+inline float4 make_float4(float x, float y, float z, float w) { return float4{x, y, z, w}; }
 inline uint4 make_uint4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) { return uint4{x, y, z, w}; }
 enum { GGA_BFS = 0, GGA_SSSP = 1 };
 inline uint32_t ld_acquire_u32(const uint32_t *p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
