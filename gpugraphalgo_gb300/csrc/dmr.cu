@@ -69,12 +69,16 @@ constexpr uint32_t STOP_NONE = 0, STOP_DONE = 1, STOP_CAPACITY = 2, STOP_STALLED
 constexpr uint32_t SCAN_BS = 1024;          /* compaction / commit blocks */
 constexpr uint32_t PLAN_BS = 128;
 constexpr uint32_t ROUND_GROUP = 8;         /* rounds launched between host checks */
+constexpr uint32_t TAIL_BS = 1024;          /* k_tail: one block runs the small rounds */
+constexpr uint32_t PF_MAX = 32768;          /* rounds up to this many plans prefetch (k_plan<true>) */
+constexpr uint32_t TAIL_SORT = 4096;        /* its worklist capacity (shared-memory sort) */
+constexpr uint32_t TAIL_MAX = 2048;         /* bad triangles at which it takes over */
 
 struct DmrState {
     uint32_t npts, ntri, round, nw;
     uint32_t nbad, stop, winners, added;
     uint32_t pcap, tcap, bcap, max_rounds;
-    uint32_t err, bad_in, fits, pad;
+    uint32_t err, bad_in, fits, tail; /* tail: the worklist is small enough for k_tail */
     unsigned long long insertions, splits, failed;
 };
 
@@ -98,6 +102,8 @@ struct DmrArgs {
     float cos_bound_f; /* cos_bound rounded to float */
     float S;           /* bound on every point's |x| and |y| (rounded up) */
     uint32_t B, G;
+    uint32_t tail_max; /* k_tail takes over at most this many bad triangles (<= B, <= TAIL_SORT) */
+    uint32_t pf_max;   /* rounds of at most this many plans use k_plan<true> */
 };
 
 __device__ __forceinline__ void set_err(DmrState *st) { atomicCAS(&st->err, 0u, 1u); }
@@ -146,11 +152,11 @@ __device__ __forceinline__ float fdx(const float4 &p, const float4 &q) { return 
 __device__ __forceinline__ float fdy(const float4 &p, const float4 &q) { return (p.y - q.y) + (p.w - q.w); }
 __device__ __forceinline__ float err_d(float L, float A) { return 2.02f * EPSF * (L + 3.0f * EPSF * A); }
 
-/* sign of the orientation of (p, q, pt): (q - p) x (pt - p) */
-__device__ __forceinline__ int orient_sign(const DmrArgs &a, uint32_t p, uint32_t q, double px, double py,
-                                           const float4 &pt, float A) {
+/* sign of the orientation of (p, q, pt): (q - p) x (pt - p); fp, fq are
+ * p's and q's float pairs */
+__device__ __forceinline__ int orient_sign(const DmrArgs &a, uint32_t p, uint32_t q, const float4 &fp,
+                                           const float4 &fq, double px, double py, const float4 &pt, float A) {
     {
-        const float4 fp = fpair(a, p), fq = fpair(a, q);
         const float u1 = fdx(fq, fp), v1 = fdy(pt, fp), u2 = fdy(fq, fp), v2 = fdx(pt, fp);
         const float a1 = u1 * v1, a2 = u2 * v2, F = a1 - a2;
         const float L = fmax4(u1, v1, u2, v2), D = err_d(L, A);
@@ -162,11 +168,10 @@ __device__ __forceinline__ int orient_sign(const DmrArgs &a, uint32_t p, uint32_
     return D > 0 ? 1 : (D < 0 ? -1 : 0);
 }
 
-/* sign of the in-circle determinant of counter-clockwise t and pt: > 0 when
- * the point is strictly inside t's circumcircle */
-__device__ __forceinline__ int incircle_sign(const DmrArgs &a, uint32_t t, double px, double py, const float4 &pt,
-                                             float A) {
-    const uint32_t i0 = a.tri[3 * t], i1 = a.tri[3 * t + 1], i2 = a.tri[3 * t + 2];
+/* sign of the in-circle determinant of the counter-clockwise triangle
+ * (i0, i1, i2) and pt: > 0 when the point is strictly inside its circumcircle */
+__device__ __forceinline__ int incircle_sign(const DmrArgs &a, uint32_t i0, uint32_t i1, uint32_t i2, double px,
+                                             double py, const float4 &pt, float A) {
     {
         const float4 f0 = fpair(a, i0), f1 = fpair(a, i1), f2 = fpair(a, i2);
         const float ax = fdx(f0, pt), ay = fdy(f0, pt), bx = fdx(f1, pt), by = fdy(f1, pt);
@@ -283,7 +288,7 @@ __global__ void __launch_bounds__(SCAN_BS) k_mark_all(DmrArgs a) {
 
 __global__ void __launch_bounds__(SCAN_BS) k_bad_count(DmrArgs a) {
     __shared__ uint32_t ws[32];
-    if (a.st->stop != STOP_NONE || a.st->err) return;
+    if (a.st->stop != STOP_NONE || a.st->err || a.st->tail) return;
     uint32_t lo, hi, c = 0;
     chunk_of(a.st->ntri, blockIdx.x, a.G, lo, hi);
     for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) c += a.bad[t];
@@ -294,7 +299,7 @@ __global__ void __launch_bounds__(SCAN_BS) k_bad_count(DmrArgs a) {
 __global__ void __launch_bounds__(SCAN_BS) k_bad_gather(DmrArgs a) {
     __shared__ uint32_t ws[32];
     DmrState *st = a.st;
-    if (st->stop != STOP_NONE) return;
+    if (st->stop != STOP_NONE || st->tail) return;
     if (st->err) { /* an id out of range: nothing reads the mesh after this */
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             st->nw = 0;
@@ -312,6 +317,9 @@ __global__ void __launch_bounds__(SCAN_BS) k_bad_gather(DmrArgs a) {
         } else if (st->round >= st->max_rounds) {
             st->nw = 0;
             st->stop = STOP_ROUNDS;
+        } else if (total <= a.tail_max) { /* k_tail runs this round and the next ones */
+            st->nw = total;
+            st->tail = 1;
         } else {
             st->round += 1;
             st->nw = total < st->bcap ? total : st->bcap;
@@ -337,143 +345,243 @@ __global__ void __launch_bounds__(SCAN_BS) k_bad_gather(DmrArgs a) {
 
 /* The cavity of (px, py) grown from seed (the oracle's grow_cavity, same
  * visiting order).  Fan entries go to the plan record; cav stays local. */
+/* The cavity of (px, py) grown from seed (the oracle's grow_cavity, same
+ * visiting order).  Fan entries go to the plan record; cav stays local.
+ * With PF (rounds of up to pf_max plans, whose time is the latency of their
+ * longest plan) each member's vertex and neighbour ids and its neighbours'
+ * vertex and neighbour ids are loaded together before the member's three
+ * edges are decided, so a member costs two rounds of dependent loads plus
+ * the in-circle tests' coordinates, not three per edge, and the fan's
+ * validity test is taken as the entries are made (shape_ok); without it (the
+ * big rounds, where registers decide occupancy) ids are loaded as needed and
+ * fan_ok tests the entries afterwards.  Both decide alike. */
+template <bool PF>
 __device__ bool grow_cavity(const DmrArgs &a, uint32_t k, uint32_t ntri, double px, double py, const float4 &pt,
                             float A, uint32_t seed, uint32_t skip_m, uint32_t skip_i, uint32_t *cav, uint32_t &nc,
-                            uint32_t &nf) {
+                            uint32_t &nf, bool &shape_ok, uint32_t *fav) {
     nc = 1;
     nf = 0;
+    shape_ok = true;
     cav[0] = seed;
     for (uint32_t q = 0; q < nc; ++q) {
         const uint32_t c = cav[q];
-        for (uint32_t i = 0; i < 3; ++i) {
-            const uint32_t o = a.nbr[3 * c + i];
-            if (o != NONE) {
-                if (o >= ntri) {
-                    set_err(a.st);
-                    return false;
+        if constexpr (!PF) { /* ids loaded as each edge needs them */
+            for (uint32_t i = 0; i < 3; ++i) {
+                const uint32_t o = a.nbr[3 * c + i];
+                if (o != NONE) {
+                    if (o >= ntri) {
+                        set_err(a.st);
+                        return false;
+                    }
+                    bool in = false;
+                    for (uint32_t j = 0; j < nc; ++j) in |= cav[j] == o;
+                    if (in) continue;
+                    if (incircle_sign(a, a.tri[3 * o], a.tri[3 * o + 1], a.tri[3 * o + 2], px, py, pt, A) > 0) {
+                        if (nc == CAV_MAX) return false;
+                        cav[nc++] = o;
+                        continue;
+                    }
                 }
-                bool in = false;
-                for (uint32_t j = 0; j < nc; ++j) in |= cav[j] == o;
-                if (in) continue;
-                if (incircle_sign(a, o, px, py, pt, A) > 0) {
-                    if (nc == CAV_MAX) return false;
-                    cav[nc++] = o;
-                    continue;
+                if (c == skip_m && i == skip_i) continue;
+                if (nf == FAN_MAX) return false;
+                uint32_t e = c; /* member id when the edge is on the domain boundary */
+                if (o != NONE) {
+                    e = 0;
+                    while (e < 3 && a.nbr[3 * o + e] != c) ++e;
+                    if (e == 3) {
+                        set_err(a.st); /* neighbour links not mutual */
+                        return false;
+                    }
+                }
+                a.p_fan[(size_t)nf * a.B + k] =
+                    make_uint4(a.tri[3 * c + (i + 1) % 3], a.tri[3 * c + (i + 2) % 3], o, e);
+                ++nf;
+            }
+        } else { /* every id of the member and its neighbours in two rounds of loads */
+            uint32_t cv[3], cn[3], ov[3][3], on[3][3];
+#pragma unroll
+            for (uint32_t i = 0; i < 3; ++i) {
+                cv[i] = a.tri[3 * c + i];
+                cn[i] = a.nbr[3 * c + i];
+            }
+#pragma unroll
+            for (uint32_t i = 0; i < 3; ++i) {
+                const bool valid = cn[i] < ntri; /* NONE and out-of-range ids load nothing */
+#pragma unroll
+                for (uint32_t j = 0; j < 3; ++j) {
+                    ov[i][j] = valid ? a.tri[3 * cn[i] + j] : 0u;
+                    on[i][j] = valid ? a.nbr[3 * cn[i] + j] : 0u;
                 }
             }
-            if (c == skip_m && i == skip_i) continue;
-            if (nf == FAN_MAX) return false;
-            uint32_t e = c; /* member id when the edge is on the domain boundary */
-            if (o != NONE) {
-                e = 0;
-                while (e < 3 && a.nbr[3 * o + e] != c) ++e;
-                if (e == 3) {
-                    set_err(a.st); /* neighbour links not mutual */
-                    return false;
+            const float4 cp[3] = {fpair(a, cv[0]), fpair(a, cv[1]), fpair(a, cv[2])};
+#pragma unroll
+            for (uint32_t i = 0; i < 3; ++i) {
+                const uint32_t o = cn[i];
+                if (o != NONE) {
+                    if (o >= ntri) {
+                        set_err(a.st);
+                        return false;
+                    }
+                    bool in = false;
+                    for (uint32_t j = 0; j < nc; ++j) in |= cav[j] == o;
+                    if (in) continue;
+                    if (incircle_sign(a, ov[i][0], ov[i][1], ov[i][2], px, py, pt, A) > 0) {
+                        if (nc == CAV_MAX) return false;
+                        cav[nc++] = o;
+                        continue;
+                    }
                 }
+                if (c == skip_m && i == skip_i) continue;
+                if (nf == FAN_MAX) return false;
+                uint32_t e = c; /* member id when the edge is on the domain boundary */
+                if (o != NONE) {
+                    e = on[i][0] == c ? 0u : (on[i][1] == c ? 1u : (on[i][2] == c ? 2u : 3u));
+                    if (e == 3) {
+                        set_err(a.st); /* neighbour links not mutual */
+                        return false;
+                    }
+                }
+                const uint32_t i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+                if (shape_ok) { /* the fan's validity test as the entries are made */
+                    shape_ok = orient_sign(a, cv[i1], cv[i2], cp[i1], cp[i2], px, py, pt, A) > 0;
+                    for (uint32_t j = 0; j < nf && shape_ok; ++j) shape_ok = fav[j] != cv[i1];
+                }
+                fav[nf] = cv[i1];
+                a.p_fan[(size_t)nf * a.B + k] = make_uint4(cv[i1], cv[i2], o, e);
+                ++nf;
             }
-            a.p_fan[(size_t)nf * a.B + k] = make_uint4(a.tri[3 * c + (i + 1) % 3], a.tri[3 * c + (i + 2) % 3], o, e);
-            ++nf;
         }
     }
     return true;
 }
 
-__device__ bool fan_ok(const DmrArgs &a, uint32_t k, uint32_t mode, uint32_t nc, uint32_t nf, double px,
-                       double py, const float4 &pt, float A) {
+/* A fan from the point over the cavity boundary is a valid triangulation only
+ * if the boundary is one simple cycle the point sees from inside: as many
+ * edges as the cavity has triangles plus 2 (plus 1 for a split), each seeing
+ * the point on its inner side, no two starting at the same vertex.  PF took
+ * the last two tests during growth (shape_ok); otherwise they run here over
+ * the plan record. */
+template <bool PF>
+__device__ bool fan_ok(const DmrArgs &a, uint32_t k, uint32_t mode, uint32_t nc, uint32_t nf, double px, double py,
+                       const float4 &pt, float A, bool shape_ok) {
     if (nf != nc + (mode == PLAN_SPLIT ? 1u : 2u)) return false;
-    for (uint32_t j = 0; j < nf; ++j) {
-        const uint4 f = a.p_fan[(size_t)j * a.B + k];
-        if (orient_sign(a, f.x, f.y, px, py, pt, A) <= 0) return false;
-        for (uint32_t i = 0; i < j; ++i)
-            if (a.p_fan[(size_t)i * a.B + k].x == f.x) return false;
+    if constexpr (PF) {
+        return shape_ok;
+    } else {
+        for (uint32_t j = 0; j < nf; ++j) {
+            const uint4 f = a.p_fan[(size_t)j * a.B + k];
+            if (orient_sign(a, f.x, f.y, fpair(a, f.x), fpair(a, f.y), px, py, pt, A) <= 0) return false;
+            for (uint32_t i = 0; i < j; ++i)
+                if (a.p_fan[(size_t)i * a.B + k].x == f.x) return false;
+        }
+        return true;
     }
-    return true;
 }
 
+/* Plan k (bad triangle t) of a round: the insertion point, its cavity and
+ * outer ring in the plan record, and the first-pass claims.  Returns true
+ * when the plan failed (no claims made). */
+template <bool PF>
+__device__ bool plan_one(const DmrArgs &a, uint32_t k, uint32_t t, uint32_t round, uint32_t ntri, uint32_t *cav,
+                         uint32_t *fav) {
+    DmrState *st = a.st;
+    uint32_t mode = PLAN_FAIL, nc = 0, nf = 0;
+    const unsigned long long key = claim_key(t, round, 0);
+    /* circumcentre (same expression order as the oracle) */
+    const uint32_t v0 = a.tri[3 * t], v1 = a.tri[3 * t + 1], v2 = a.tri[3 * t + 2];
+    const double bx = a.x[v1] - a.x[v0], by = a.y[v1] - a.y[v0];
+    const double cx = a.x[v2] - a.x[v0], cy = a.y[v2] - a.y[v0];
+    const double d = 2.0 * (bx * cy - by * cx);
+    const double b2 = bx * bx + by * by, c2 = cx * cx + cy * cy;
+    double px = a.x[v0] + (cy * b2 - by * c2) / d;
+    double py = a.y[v0] + (bx * c2 - cx * b2) / d;
+    float4 pt = fpair_of(px, py);
+    float A = a.S + fmaxf(a.S, fmaxf(fabsf(pt.x), fabsf(pt.y)));
+    uint32_t cur = t, split_m = NONE, split_i = 0, step = 0;
+    bool ok = true, shape_ok = true;
+    for (; step < WALK_MAX; ++step) {
+        uint32_t cross = 3, n;
+        if constexpr (PF) { /* the triangle's ids and coordinates in one round of loads */
+            const uint32_t w0 = a.tri[3 * cur], w1 = a.tri[3 * cur + 1], w2 = a.tri[3 * cur + 2];
+            const uint32_t n0 = a.nbr[3 * cur], n1 = a.nbr[3 * cur + 1], n2 = a.nbr[3 * cur + 2];
+            const float4 g0 = fpair(a, w0), g1 = fpair(a, w1), g2 = fpair(a, w2);
+            if (orient_sign(a, w1, w2, g1, g2, px, py, pt, A) < 0) cross = 0;
+            else if (orient_sign(a, w2, w0, g2, g0, px, py, pt, A) < 0) cross = 1;
+            else if (orient_sign(a, w0, w1, g0, g1, px, py, pt, A) < 0) cross = 2;
+            n = cross == 0 ? n0 : (cross == 1 ? n1 : n2);
+        } else {
+            for (uint32_t i = 0; i < 3 && cross == 3; ++i) {
+                const uint32_t p = a.tri[3 * cur + (i + 1) % 3], q = a.tri[3 * cur + (i + 2) % 3];
+                if (orient_sign(a, p, q, fpair(a, p), fpair(a, q), px, py, pt, A) < 0) cross = i;
+            }
+            n = cross < 3 ? a.nbr[3 * cur + cross] : NONE;
+        }
+        if (cross == 3) break;
+        if (n == NONE) {
+            split_m = cur;
+            split_i = cross;
+            break;
+        }
+        if (n >= ntri) {
+            set_err(st);
+            ok = false;
+            break;
+        }
+        cur = n;
+    }
+    if (step == WALK_MAX) ok = false;
+    if (ok && split_m == NONE) {
+        ok = grow_cavity<PF>(a, k, ntri, px, py, pt, A, cur, NONE, 0, cav, nc, nf, shape_ok, fav);
+        for (uint32_t j = 0; ok && j < nf && split_m == NONE; ++j) {
+            const uint4 f = a.p_fan[(size_t)j * a.B + k];
+            if (f.z != NONE) continue;
+            if ((px - a.x[f.x]) * (px - a.x[f.y]) + (py - a.y[f.x]) * (py - a.y[f.y]) < 0) {
+                split_m = f.w;
+                for (uint32_t i = 0; i < 3; ++i)
+                    if (a.tri[3 * split_m + (i + 1) % 3] == f.x) split_i = i;
+            }
+        }
+        if (ok && split_m == NONE) {
+            mode = fan_ok<PF>(a, k, PLAN_INSERT, nc, nf, px, py, pt, A, shape_ok) ? PLAN_INSERT : PLAN_FAIL;
+            ok = false; /* done */
+        }
+    }
+    if (ok) { /* split_m's edge split_i, at its midpoint */
+        const uint32_t e0 = a.tri[3 * split_m + (split_i + 1) % 3], e1 = a.tri[3 * split_m + (split_i + 2) % 3];
+        px = (a.x[e0] + a.x[e1]) * 0.5;
+        py = (a.y[e0] + a.y[e1]) * 0.5;
+        pt = fpair_of(px, py);
+        A = 2.0f * a.S;
+        if (grow_cavity<PF>(a, k, ntri, px, py, pt, A, split_m, split_m, split_i, cav, nc, nf, shape_ok, fav))
+            mode = fan_ok<PF>(a, k, PLAN_SPLIT, nc, nf, px, py, pt, A, shape_ok) ? PLAN_SPLIT : PLAN_FAIL;
+    }
+    a.p_mode[k] = mode | nc << 8 | nf << 16;
+    if (mode == PLAN_FAIL) return true;
+    a.p_px[k] = px;
+    a.p_py[k] = py;
+    for (uint32_t j = 0; j < nc; ++j) {
+        a.p_cav[(size_t)j * a.B + k] = cav[j];
+        atomicMax(a.owner + cav[j], key);
+    }
+    for (uint32_t j = 0; j < nf; ++j) {
+        const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+        if (o != NONE) atomicMax(a.ring + o, key);
+    }
+    return false;
+}
+
+/* PF: the variant for rounds of up to pf_max plans; both are launched every
+ * round and the one that does not fit returns at once. */
+template <bool PF>
 __global__ void __launch_bounds__(PLAN_BS) k_plan(DmrArgs a) {
     DmrState *st = a.st;
-    if (st->stop != STOP_NONE) return;
+    if (st->stop != STOP_NONE || st->tail) return;
     const uint32_t nw = st->nw, ntri = st->ntri, round = st->round;
-    uint32_t cav[CAV_MAX];
+    if ((nw <= a.pf_max) != PF) return;
+    uint32_t cav[CAV_MAX], fav[FAN_MAX];
     uint32_t fails = 0;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
-        const uint32_t t = a.work[k];
-        uint32_t mode = PLAN_FAIL, nc = 0, nf = 0;
-        const unsigned long long key = claim_key(t, round, 0);
-        /* circumcentre (same expression order as the oracle) */
-        const uint32_t v0 = a.tri[3 * t], v1 = a.tri[3 * t + 1], v2 = a.tri[3 * t + 2];
-        const double bx = a.x[v1] - a.x[v0], by = a.y[v1] - a.y[v0];
-        const double cx = a.x[v2] - a.x[v0], cy = a.y[v2] - a.y[v0];
-        const double d = 2.0 * (bx * cy - by * cx);
-        const double b2 = bx * bx + by * by, c2 = cx * cx + cy * cy;
-        double px = a.x[v0] + (cy * b2 - by * c2) / d;
-        double py = a.y[v0] + (bx * c2 - cx * b2) / d;
-        float4 pt = fpair_of(px, py);
-        float A = a.S + fmaxf(a.S, fmaxf(fabsf(pt.x), fabsf(pt.y)));
-        uint32_t cur = t, split_m = NONE, split_i = 0, step = 0;
-        bool ok = true;
-        for (; step < WALK_MAX; ++step) {
-            uint32_t cross = 3;
-            for (uint32_t i = 0; i < 3 && cross == 3; ++i)
-                if (orient_sign(a, a.tri[3 * cur + (i + 1) % 3], a.tri[3 * cur + (i + 2) % 3], px, py, pt, A) < 0)
-                    cross = i;
-            if (cross == 3) break;
-            const uint32_t n = a.nbr[3 * cur + cross];
-            if (n == NONE) {
-                split_m = cur;
-                split_i = cross;
-                break;
-            }
-            if (n >= ntri) {
-                set_err(st);
-                ok = false;
-                break;
-            }
-            cur = n;
-        }
-        if (step == WALK_MAX) ok = false;
-        if (ok && split_m == NONE) {
-            ok = grow_cavity(a, k, ntri, px, py, pt, A, cur, NONE, 0, cav, nc, nf);
-            for (uint32_t j = 0; ok && j < nf && split_m == NONE; ++j) {
-                const uint4 f = a.p_fan[(size_t)j * a.B + k];
-                if (f.z != NONE) continue;
-                if ((px - a.x[f.x]) * (px - a.x[f.y]) + (py - a.y[f.x]) * (py - a.y[f.y]) < 0) {
-                    split_m = f.w;
-                    for (uint32_t i = 0; i < 3; ++i)
-                        if (a.tri[3 * split_m + (i + 1) % 3] == f.x) split_i = i;
-                }
-            }
-            if (ok && split_m == NONE) {
-                mode = fan_ok(a, k, PLAN_INSERT, nc, nf, px, py, pt, A) ? PLAN_INSERT : PLAN_FAIL;
-                ok = false; /* done */
-            }
-        }
-        if (ok) { /* split_m's edge split_i, at its midpoint */
-            const uint32_t e0 = a.tri[3 * split_m + (split_i + 1) % 3], e1 = a.tri[3 * split_m + (split_i + 2) % 3];
-            px = (a.x[e0] + a.x[e1]) * 0.5;
-            py = (a.y[e0] + a.y[e1]) * 0.5;
-            pt = fpair_of(px, py);
-            A = 2.0f * a.S;
-            if (grow_cavity(a, k, ntri, px, py, pt, A, split_m, split_m, split_i, cav, nc, nf))
-                mode = fan_ok(a, k, PLAN_SPLIT, nc, nf, px, py, pt, A) ? PLAN_SPLIT : PLAN_FAIL;
-        }
-        a.p_mode[k] = mode | nc << 8 | nf << 16;
-        if (mode == PLAN_FAIL) {
-            ++fails;
-            continue;
-        }
-        a.p_px[k] = px;
-        a.p_py[k] = py;
-        for (uint32_t j = 0; j < nc; ++j) {
-            a.p_cav[(size_t)j * a.B + k] = cav[j];
-            atomicMax(a.owner + cav[j], key);
-        }
-        for (uint32_t j = 0; j < nf; ++j) {
-            const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
-            if (o != NONE) atomicMax(a.ring + o, key);
-        }
-    }
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x)
+        fails += plan_one<PF>(a, k, a.work[k], round, ntri, cav, fav);
     if (fails) atomicAdd(&st->failed, (unsigned long long)fails);
 }
 
@@ -494,63 +602,80 @@ __device__ __forceinline__ bool holds(const DmrArgs &a, uint32_t k, uint32_t nc,
     return true;
 }
 
+/* First pass: k wins if it holds every conflicting claim; a winner stamps
+ * its cavity (kind 1) and ring (kind 2) in the lock table. */
+__device__ __forceinline__ void resolve0_one(const DmrArgs &a, uint32_t k, uint32_t round) {
+    const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16, stamp = round << 2;
+    const uint32_t win = (pm & 0xFF) != PLAN_FAIL && holds(a, k, nc, nf, claim_key(a.work[k], round, 0));
+    a.p_win[k] = win;
+    if (!win) return;
+    for (uint32_t j = 0; j < nc; ++j) a.lock[a.p_cav[(size_t)j * a.B + k]] = stamp | 1;
+    for (uint32_t j = 0; j < nf; ++j) {
+        const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+        if (o != NONE) a.lock[o] = stamp | 2;
+    }
+}
+
+/* Second pass: a plan that lost and touches no stamp claims again with a
+ * higher key; one that touches a stamp is out of the round (p_win = 2). */
+__device__ __forceinline__ void reclaim_one(const DmrArgs &a, uint32_t k, uint32_t round) {
+    const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16, stamp = round << 2;
+    if ((pm & 0xFF) == PLAN_FAIL || a.p_win[k]) return;
+    bool blocked = false;
+    for (uint32_t j = 0; j < nc && !blocked; ++j) blocked = (a.lock[a.p_cav[(size_t)j * a.B + k]] >> 2) == round;
+    for (uint32_t j = 0; j < nf && !blocked; ++j) {
+        const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+        blocked = o != NONE && a.lock[o] == (stamp | 1);
+    }
+    if (blocked) {
+        a.p_win[k] = 2;
+        return;
+    }
+    const unsigned long long key = claim_key(a.work[k], round, 1);
+    for (uint32_t j = 0; j < nc; ++j) atomicMax(a.owner + a.p_cav[(size_t)j * a.B + k], key);
+    for (uint32_t j = 0; j < nf; ++j) {
+        const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
+        if (o != NONE) atomicMax(a.ring + o, key);
+    }
+}
+
+/* Final verdict of k (1 = commits this round) and the triangles it adds. */
+__device__ __forceinline__ uint32_t resolve1_one(const DmrArgs &a, uint32_t k, uint32_t round, uint32_t &need) {
+    const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16, w = a.p_win[k];
+    const uint32_t win = w == 1 || (w == 0 && (pm & 0xFF) != PLAN_FAIL &&
+                                    holds(a, k, nc, nf, claim_key(a.work[k], round, 1)));
+    a.p_win[k] = win;
+    need = win ? nf - nc : 0;
+    return win;
+}
+
 __global__ void __launch_bounds__(PLAN_BS) k_resolve0(DmrArgs a) {
     DmrState *st = a.st;
-    if (st->stop != STOP_NONE) return;
-    const uint32_t nw = st->nw, round = st->round, stamp = round << 2;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
-        const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16;
-        const uint32_t win = (pm & 0xFF) != PLAN_FAIL && holds(a, k, nc, nf, claim_key(a.work[k], round, 0));
-        a.p_win[k] = win;
-        if (!win) continue;
-        for (uint32_t j = 0; j < nc; ++j) a.lock[a.p_cav[(size_t)j * a.B + k]] = stamp | 1;
-        for (uint32_t j = 0; j < nf; ++j) {
-            const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
-            if (o != NONE) a.lock[o] = stamp | 2;
-        }
-    }
+    if (st->stop != STOP_NONE || st->tail) return;
+    const uint32_t nw = st->nw, round = st->round;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x)
+        resolve0_one(a, k, round);
 }
 
 __global__ void __launch_bounds__(PLAN_BS) k_reclaim(DmrArgs a) {
     DmrState *st = a.st;
-    if (st->stop != STOP_NONE) return;
-    const uint32_t nw = st->nw, round = st->round, stamp = round << 2;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
-        const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16;
-        if ((pm & 0xFF) == PLAN_FAIL || a.p_win[k]) continue;
-        bool blocked = false;
-        for (uint32_t j = 0; j < nc && !blocked; ++j) blocked = (a.lock[a.p_cav[(size_t)j * a.B + k]] >> 2) == round;
-        for (uint32_t j = 0; j < nf && !blocked; ++j) {
-            const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
-            blocked = o != NONE && a.lock[o] == (stamp | 1);
-        }
-        if (blocked) {
-            a.p_win[k] = 2;
-            continue;
-        }
-        const unsigned long long key = claim_key(a.work[k], round, 1);
-        for (uint32_t j = 0; j < nc; ++j) atomicMax(a.owner + a.p_cav[(size_t)j * a.B + k], key);
-        for (uint32_t j = 0; j < nf; ++j) {
-            const uint32_t o = a.p_fan[(size_t)j * a.B + k].z;
-            if (o != NONE) atomicMax(a.ring + o, key);
-        }
-    }
+    if (st->stop != STOP_NONE || st->tail) return;
+    const uint32_t nw = st->nw, round = st->round;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x)
+        reclaim_one(a, k, round);
 }
 
 __global__ void __launch_bounds__(SCAN_BS) k_resolve1(DmrArgs a) {
     __shared__ uint32_t ws[32];
     DmrState *st = a.st;
-    if (st->stop != STOP_NONE || st->nw == 0) return;
+    if (st->stop != STOP_NONE || st->tail || st->nw == 0) return;
     const uint32_t round = st->round;
     uint32_t lo, hi, wins = 0, need = 0;
     chunk_of(st->nw, blockIdx.x, a.G, lo, hi);
     for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
-        const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16, w = a.p_win[k];
-        const uint32_t win = w == 1 || (w == 0 && (pm & 0xFF) != PLAN_FAIL &&
-                                        holds(a, k, nc, nf, claim_key(a.work[k], round, 1)));
-        a.p_win[k] = win;
-        wins += win;
-        need += win ? nf - nc : 0;
+        uint32_t nd;
+        wins += resolve1_one(a, k, round, nd);
+        need += nd;
     }
     wins = block_sum(wins, ws);
     need = block_sum(need, ws);
@@ -571,7 +696,7 @@ __device__ __forceinline__ bool round_fits(const DmrArgs &a, uint32_t *ws, uint3
 __global__ void __launch_bounds__(SCAN_BS) k_compact(DmrArgs a) {
     __shared__ uint32_t ws[32];
     DmrState *st = a.st;
-    if (st->stop != STOP_NONE || st->nw == 0) return;
+    if (st->stop != STOP_NONE || st->tail || st->nw == 0) return;
     uint32_t W, A;
     const bool fits = round_fits(a, ws, W, A);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -603,43 +728,50 @@ __global__ void __launch_bounds__(SCAN_BS) k_compact(DmrArgs a) {
     }
 }
 
+/* Winner k takes point pid and triangles from tb on: its cavity becomes a
+ * fan from the new point, the outer ring is relinked and the new triangles
+ * are re-marked.  Returns true for a boundary split. */
+__device__ bool commit_one(const DmrArgs &a, uint32_t k, uint32_t pid, uint32_t tb, uint32_t *slot, uint32_t *fa,
+                           uint32_t *fb) {
+    const uint32_t pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16;
+    const double npx = a.p_px[k], npy = a.p_py[k];
+    a.x[pid] = npx;
+    a.y[pid] = npy;
+    a.pq[pid] = fpair_of(npx, npy);
+    for (uint32_t j = 0; j < nf; ++j) {
+        slot[j] = j < nc ? a.p_cav[(size_t)j * a.B + k] : tb + (j - nc);
+        const uint4 f = a.p_fan[(size_t)j * a.B + k];
+        fa[j] = f.x;
+        fb[j] = f.y;
+    }
+    for (uint32_t j = 0; j < nf; ++j) {
+        const uint4 f = a.p_fan[(size_t)j * a.B + k];
+        const uint32_t s = slot[j];
+        uint32_t n0 = NONE, n1 = NONE;
+        for (uint32_t q = 0; q < nf; ++q) {
+            if (fa[q] == fb[j]) n0 = slot[q];
+            if (fb[q] == fa[j]) n1 = slot[q];
+        }
+        a.tri[3 * (size_t)s] = f.x;
+        a.tri[3 * (size_t)s + 1] = f.y;
+        a.tri[3 * (size_t)s + 2] = pid;
+        a.nbr[3 * (size_t)s] = n0;
+        a.nbr[3 * (size_t)s + 1] = n1;
+        a.nbr[3 * (size_t)s + 2] = f.z;
+        if (f.z != NONE) a.nbr[3 * (size_t)f.z + f.w] = s;
+    }
+    for (uint32_t j = 0; j < nf; ++j) a.bad[slot[j]] = tri_bad(a, slot[j]);
+    return (pm & 0xFF) == PLAN_SPLIT;
+}
+
 __global__ void __launch_bounds__(PLAN_BS) k_commit(DmrArgs a) {
     DmrState *st = a.st;
-    if (st->stop != STOP_NONE || st->nw == 0 || !st->fits) return;
+    if (st->stop != STOP_NONE || st->tail || st->nw == 0 || !st->fits) return;
     const uint32_t W = st->winners, npts = st->npts;
     uint32_t ins = 0, spl = 0;
     uint32_t slot[FAN_MAX], fa[FAN_MAX], fb[FAN_MAX];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < W; i += gridDim.x * blockDim.x) {
-        const uint32_t k = a.wlist[i], pm = a.p_mode[k], nc = (pm >> 8) & 0xFF, nf = pm >> 16;
-        const uint32_t pid = npts + i, tb = a.wtri[i];
-        const double npx = a.p_px[k], npy = a.p_py[k];
-        a.x[pid] = npx;
-        a.y[pid] = npy;
-        a.pq[pid] = fpair_of(npx, npy);
-        for (uint32_t j = 0; j < nf; ++j) {
-            slot[j] = j < nc ? a.p_cav[(size_t)j * a.B + k] : tb + (j - nc);
-            const uint4 f = a.p_fan[(size_t)j * a.B + k];
-            fa[j] = f.x;
-            fb[j] = f.y;
-        }
-        for (uint32_t j = 0; j < nf; ++j) {
-            const uint4 f = a.p_fan[(size_t)j * a.B + k];
-            const uint32_t s = slot[j];
-            uint32_t n0 = NONE, n1 = NONE;
-            for (uint32_t q = 0; q < nf; ++q) {
-                if (fa[q] == fb[j]) n0 = slot[q];
-                if (fb[q] == fa[j]) n1 = slot[q];
-            }
-            a.tri[3 * (size_t)s] = f.x;
-            a.tri[3 * (size_t)s + 1] = f.y;
-            a.tri[3 * (size_t)s + 2] = pid;
-            a.nbr[3 * (size_t)s] = n0;
-            a.nbr[3 * (size_t)s + 1] = n1;
-            a.nbr[3 * (size_t)s + 2] = f.z;
-            if (f.z != NONE) a.nbr[3 * (size_t)f.z + f.w] = s;
-        }
-        for (uint32_t j = 0; j < nf; ++j) a.bad[slot[j]] = tri_bad(a, slot[j]);
-        if ((pm & 0xFF) == PLAN_SPLIT) ++spl;
+        if (commit_one(a, a.wlist[i], npts + i, a.wtri[i], slot, fa, fb)) ++spl;
         else ++ins;
     }
     if (ins) atomicAdd(&st->insertions, (unsigned long long)ins);
@@ -648,7 +780,7 @@ __global__ void __launch_bounds__(PLAN_BS) k_commit(DmrArgs a) {
 
 __global__ void k_finish(DmrArgs a) {
     DmrState *st = a.st;
-    if (st->stop != STOP_NONE) return;
+    if (st->stop != STOP_NONE || st->tail) return;
     if (st->err) {
         st->stop = STOP_ERROR;
         return;
@@ -659,6 +791,163 @@ __global__ void k_finish(DmrArgs a) {
     else {
         st->npts += st->winners;
         st->ntri += st->added;
+    }
+}
+
+/* ------------------------------------------------------------- the tail */
+
+/* Once at most tail_max triangles are bad, one block runs whole rounds with
+ * the same per-plan functions, separated by __syncthreads instead of kernel
+ * boundaries, and builds the next worklist from the triangles the round can
+ * have changed: the previous worklist (losers and failed plans stay bad),
+ * the winners' rewritten cavity slots and the appended ones, each kept if
+ * bad, sorted and made unique in shared memory.  That is every bad triangle
+ * in ascending id, the same worklist a full compaction gives, so the rounds
+ * equal the multi-kernel ones.  When the next worklist would exceed
+ * tail_max the block hands back (tail = 0) and the full compaction resumes. */
+__global__ void __launch_bounds__(TAIL_BS, 1) k_tail(DmrArgs a) {
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t srt[TAIL_SORT];
+    __shared__ uint32_t s_cnt;
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE || !st->tail) return;
+    const uint32_t tid = threadIdx.x, nthr = blockDim.x;
+    uint32_t cav[CAV_MAX], slot[FAN_MAX], fa[FAN_MAX], fb[FAN_MAX];
+    for (uint32_t guard = 0; guard <= MAX_ROUNDS; ++guard) {
+        __syncthreads();
+        const uint32_t nw = st->nw, ntri = st->ntri, npts = st->npts, round0 = st->round, err = st->err;
+        __syncthreads(); /* every thread has read the state before thread 0 writes it */
+        if (err) {
+            if (tid == 0) st->stop = STOP_ERROR;
+            return;
+        }
+        if (nw == 0) {
+            if (tid == 0) st->stop = STOP_DONE;
+            return;
+        }
+        if (round0 >= st->max_rounds) {
+            if (tid == 0) st->stop = STOP_ROUNDS;
+            return;
+        }
+        const uint32_t round = round0 + 1;
+        if (tid == 0) st->round = round;
+        uint32_t fails = 0;
+        for (uint32_t k = tid; k < nw; k += nthr) fails += plan_one<false>(a, k, a.work[k], round, ntri, cav, fa);
+        fails = block_sum(fails, ws);
+        if (tid == 0 && fails) st->failed += fails;
+        for (uint32_t k = tid; k < nw; k += nthr) resolve0_one(a, k, round);
+        __syncthreads();
+        for (uint32_t k = tid; k < nw; k += nthr) reclaim_one(a, k, round);
+        __syncthreads();
+        uint32_t W = 0, A = 0;
+        for (uint32_t k0 = 0; k0 < nw; k0 += nthr) {
+            const uint32_t k = k0 + tid;
+            uint32_t win = 0, need = 0, wt, at;
+            if (k < nw) win = resolve1_one(a, k, round, need);
+            const uint32_t wpre = block_exclusive_scan(win, ws, &wt);
+            const uint32_t apre = block_exclusive_scan(need, ws, &at);
+            if (win) {
+                a.wlist[W + wpre] = k;
+                a.wtri[W + wpre] = ntri + A + apre;
+            }
+            W += wt;
+            A += at;
+        }
+        __syncthreads();
+        if (W == 0) {
+            if (tid == 0) {
+                st->winners = 0;
+                st->stop = STOP_STALLED;
+            }
+            return;
+        }
+        if ((uint64_t)npts + W > st->pcap || (uint64_t)ntri + A > st->tcap) {
+            if (tid == 0) {
+                st->winners = W;
+                st->added = A;
+                st->stop = STOP_CAPACITY;
+            }
+            return;
+        }
+        uint32_t ins = 0, spl = 0;
+        for (uint32_t i = tid; i < W; i += nthr) {
+            if (commit_one(a, a.wlist[i], npts + i, a.wtri[i], slot, fa, fb)) ++spl;
+            else ++ins;
+        }
+        ins = block_sum(ins, ws);
+        spl = block_sum(spl, ws);
+        /* the next worklist's candidates */
+        if (tid == 0) s_cnt = 0;
+        __syncthreads();
+        for (uint32_t k = tid; k < nw; k += nthr) {
+            const uint32_t t = a.work[k];
+            if (a.bad[t]) {
+                const uint32_t q = atomicAdd(&s_cnt, 1u);
+                if (q < TAIL_SORT) srt[q] = t;
+            }
+        }
+        for (uint32_t i = tid; i < W; i += nthr) {
+            const uint32_t k = a.wlist[i], nc = (a.p_mode[k] >> 8) & 0xFF;
+            for (uint32_t j = 0; j < nc; ++j) {
+                const uint32_t t = a.p_cav[(size_t)j * a.B + k];
+                if (a.bad[t]) {
+                    const uint32_t q = atomicAdd(&s_cnt, 1u);
+                    if (q < TAIL_SORT) srt[q] = t;
+                }
+            }
+        }
+        for (uint32_t t = ntri + tid; t < ntri + A; t += nthr)
+            if (a.bad[t]) {
+                const uint32_t q = atomicAdd(&s_cnt, 1u);
+                if (q < TAIL_SORT) srt[q] = t;
+            }
+        __syncthreads();
+        const uint32_t c = s_cnt;
+        if (tid == 0) {
+            st->npts = npts + W;
+            st->ntri = ntri + A;
+            st->winners = W;
+            st->added = A;
+            st->insertions += ins;
+            st->splits += spl;
+        }
+        if (c > TAIL_SORT) { /* more than one block sorts: hand back */
+            if (tid == 0) st->tail = 0;
+            return;
+        }
+        uint32_t n2 = 1;
+        while (n2 < c) n2 <<= 1;
+        for (uint32_t i = c + tid; i < n2; i += nthr) srt[i] = NONE;
+        __syncthreads();
+        for (uint32_t kk = 2; kk <= n2; kk <<= 1) /* bitonic sort, ascending */
+            for (uint32_t j = kk >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = tid; i < n2; i += nthr) {
+                    const uint32_t ij = i ^ j;
+                    if (ij > i) {
+                        const uint32_t u = srt[i], v = srt[ij];
+                        if ((u > v) == ((i & kk) == 0)) {
+                            srt[i] = v;
+                            srt[ij] = u;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        uint32_t nn = 0;
+        for (uint32_t i0 = 0; i0 < c; i0 += nthr) { /* unique, into the worklist */
+            const uint32_t i = i0 + tid;
+            const uint32_t keep = i < c && (i == 0 || srt[i] != srt[i - 1]);
+            uint32_t tot;
+            const uint32_t pos = block_exclusive_scan(keep, ws, &tot);
+            if (keep) a.work[nn + pos] = srt[i];
+            nn += tot;
+        }
+        if (tid == 0) {
+            st->nw = nn;
+            st->nbad = nn;
+            if (nn > a.tail_max) st->tail = 0; /* the full compaction takes it from here */
+        }
+        if (nn > a.tail_max) return;
     }
 }
 
@@ -748,6 +1037,8 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     a.S = (float)(smax * (1.0 + 1.0 / 1048576.0)) + 1e-30f;
     a.B = B;
     a.G = G;
+    a.tail_max = B < TAIL_MAX ? B : TAIL_MAX;
+    a.pf_max = PF_MAX;
     const unsigned plan_grid = ctx_grid(c, B, PLAN_BS);
     cudaEvent_t e0 = c->ev[0], e1 = c->ev[1];
     GGA_CK(cudaEventRecord(e0, s));
@@ -757,7 +1048,8 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
         for (uint32_t g = 0; g < ROUND_GROUP; ++g) {
             k_bad_count<<<G, SCAN_BS, 0, s>>>(a);
             k_bad_gather<<<G, SCAN_BS, 0, s>>>(a);
-            k_plan<<<plan_grid, PLAN_BS, 0, s>>>(a);
+            k_plan<false><<<plan_grid, PLAN_BS, 0, s>>>(a);
+            k_plan<true><<<plan_grid, PLAN_BS, 0, s>>>(a);
             k_resolve0<<<plan_grid, PLAN_BS, 0, s>>>(a);
             k_reclaim<<<plan_grid, PLAN_BS, 0, s>>>(a);
             k_resolve1<<<G, SCAN_BS, 0, s>>>(a);
@@ -769,6 +1061,12 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
         issued += ROUND_GROUP;
         GGA_CK(cudaMemcpyAsync(b.hst, b.st, sizeof(DmrState), cudaMemcpyDeviceToHost, s));
         GGA_CK(cudaStreamSynchronize(s));
+        if (b.hst->stop == STOP_NONE && b.hst->tail) {
+            k_tail<<<1, TAIL_BS, 0, s>>>(a);
+            GGA_CK(cudaGetLastError());
+            GGA_CK(cudaMemcpyAsync(b.hst, b.st, sizeof(DmrState), cudaMemcpyDeviceToHost, s));
+            GGA_CK(cudaStreamSynchronize(s));
+        }
         if (b.hst->stop != STOP_NONE || issued > MAX_ROUNDS + ROUND_GROUP) break;
     }
     GGA_CK(cudaEventRecord(e1, s));

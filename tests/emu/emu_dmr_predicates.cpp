@@ -69,13 +69,13 @@ int main(int argc, char **argv) {
                          cdy = y[2] - py;
             const double ad = adx * adx + ady * ady, bd = bdx * bdx + bdy * bdy, cd = cdx * cdx + cdy * cdy;
             const int want = sgn(adx * (bdy * cd - bd * cdy) - ady * (bdx * cd - bd * cdx) + ad * (bdx * cdy - bdy * cdx));
-            bad_ic += incircle_sign(a, 0, px, py, pt, A) != want;
+            bad_ic += incircle_sign(a, 0, 1, 2, px, py, pt, A) != want;
         }
         {
             const float4 qt = fpair_of(qx, qy);
             const float A = a.S + fmaxf(a.S, fmaxf(fabsf(qt.x), fabsf(qt.y)));
             const int want = sgn((x[1] - x[0]) * (qy - y[0]) - (y[1] - y[0]) * (qx - x[0]));
-            bad_or += orient_sign(a, 0, 1, qx, qy, qt, A) != want;
+            bad_or += orient_sign(a, 0, 1, pq[0], pq[1], qx, qy, qt, A) != want;
         }
         {
             /* angle test on the triangle: compare with the double rule */

@@ -149,29 +149,35 @@ def test_batch_kernel_text(emu, case):
 
 
 # Mesh refinement kernels (dmr.cu): every round's kernels run as emulated
-# threads (3 blocks of 64 for the compactions and commits, 2 x 32 planning
-# threads), and the refined mesh must equal the oracle's serial restatement
-# of the same schedule bit for bit: points, triangles and neighbours.
-DMR_CASES = [("jittered", 1 << 20), ("jittered", 7), ("random", 1 << 20)]
+# threads (3 blocks of 64 for the compactions, 2 x 32 planning and commit
+# threads, one block of 64 for the tail kernel), and the refined mesh must
+# equal the oracle's serial restatement of the same schedule bit for bit:
+# points, triangles and neighbours.  tail_max 0 keeps every round on the
+# multi-kernel path, 2048 hands the small rounds to the one-block tail
+# kernel, 12 makes it hand back and take over again; pf 8 plans rounds of
+# more than 8 bad triangles with the lean variant of k_plan.
+DMR_CASES = [("jittered", 1 << 20, 0, 32768), ("jittered", 7, 2048, 32768), ("random", 1 << 20, 0, 8),
+             ("random", 1 << 20, 12, 8), ("random", 1 << 20, 2048, 32768)]
 
 
-@pytest.mark.parametrize("case", DMR_CASES, ids=[f"{m}-cap{c}" for m, c in DMR_CASES])
+@pytest.mark.parametrize("case", DMR_CASES, ids=[f"{m}-cap{c}-tail{t}-pf{f}" for m, c, t, f in DMR_CASES])
 def test_dmr_kernel_text(emu, case):
     root, bins = emu
-    kind, bcap = case
+    kind, bcap, tail, pf = case
     mesh = oracle.mesh_gen_jittered(14, 12, 0.35, 2) if kind == "jittered" else oracle.mesh_gen_random(120, 5)
-    d = root / f"dmr_{kind}_{bcap}"
+    d = root / f"dmr_{kind}_{bcap}_{tail}_{pf}"
     d.mkdir()
     for k in ("x", "y", "tri", "nbr"):
         mesh[k].tofile(d / f"{k}.bin")
     tcap = 4 * (len(mesh["tri"]) // 3) + 65536
-    r = subprocess.run([bins["dmr"], str(d), "3", "64", "32", str(bcap), str(tcap), oracle.cos_bound(25.0).hex()],
-                       capture_output=True, text=True, timeout=600)
+    r = subprocess.run([bins["dmr"], str(d), "3", "64", "32", str(bcap), str(tcap), oracle.cos_bound(25.0).hex(),
+                        str(tail), str(pf)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     fields = dict(zip(r.stdout.split()[0::2], r.stdout.split()[1::2]))
     want = oracle.mesh_refine(mesh, batch_cap=bcap)
     assert want["status"] == "ok" and want["bad_out"] == 0
     assert fields["stop"] == "1" and fields["err"] == "0"  # done, no index error
+    assert (fields["tails"] != "0") == (tail > 0)
     assert int(fields["rounds"]) == want["rounds"] and int(fields["ins"]) == want["insertions"]
     assert int(fields["splits"]) == want["boundary_splits"] and int(fields["bad_in"]) == want["bad_in"]
     for k, dt in (("x", np.float64), ("y", np.float64), ("tri", np.uint32), ("nbr", np.uint32)):
