@@ -627,6 +627,7 @@ def mesh_section(gga, ctx, npoints: int, reps: int = 3):
            "triangles_out": st["triangles_out"], "points_out": st["points_out"], "bad_out": st["bad_out"],
            "rounds": st["rounds"], "insertions": st["insertions"], "boundary_splits": st["boundary_splits"],
            "failed_plans": st["failed_plans"], "device_ms": dev, "e2e_ms": e2e, "runs": reps,
+           "e2e_breakdown_ms": {k: st[k] for k in ("alloc_ms", "upload_ms", "device_ms", "download_ms")},
            "device_mtri_per_s": st["triangles_out"] / dev / 1e3, "dtype": "f64 (f32 filters)",
            "identical_runs": all(r["triangles_out"] == st["triangles_out"] and r["rounds"] == st["rounds"]
                                  for r in runs),

@@ -157,6 +157,9 @@ class RefineStats(C.Structure):
         ("failed_plans", u64),
         ("total_ms", C.c_double),
         ("device_ms", C.c_double),
+        ("alloc_ms", C.c_double),
+        ("upload_ms", C.c_double),
+        ("download_ms", C.c_double),
     ]
 
 

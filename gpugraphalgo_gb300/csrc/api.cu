@@ -47,6 +47,17 @@ gga_status gga_ctx_create(int device, gga_ctx **out) {
     for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->user_ev[i]);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->dflag, 64 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->hflag, 64 * sizeof(uint32_t));
+    if (e == cudaSuccess) {
+        /* keep up to 4 GiB of freed stream-ordered memory in this process's
+         * pool, so the working buffers of back-to-back calls (a refinement's
+         * plan records, scan temporaries) are not unmapped and mapped again */
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = 4ull << 30, cur = 0;
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur);
+            if (cur < keep) cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
     if (e != cudaSuccess) {
         gga_ctx_destroy(c);
         return gga_fail(GGA_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));

@@ -80,6 +80,7 @@ struct DmrState {
     uint32_t pcap, tcap, bcap, max_rounds;
     uint32_t err, bad_in, fits, tail; /* tail: the worklist is small enough for k_tail */
     unsigned long long insertions, splits, failed;
+    uint32_t pad_s, pad_t; /* host side: the coordinate bound's bits read back */
 };
 
 struct DmrArgs {
@@ -266,11 +267,19 @@ __device__ __forceinline__ uint32_t prefix_of(const DmrArgs &a, uint32_t row, ui
 
 /* ---------------------------------------------------------------- marking */
 
-__global__ void __launch_bounds__(SCAN_BS) k_shadow(DmrArgs a) {
+/* float pairs of the points, and a bound on every |x|, |y| (rounded up; new
+ * points stay inside the input's bounding box) as the bits of a
+ * non-negative float, whose integer order is its value order */
+__global__ void __launch_bounds__(SCAN_BS) k_shadow(DmrArgs a, uint32_t *sbits) {
     const uint32_t n = a.st->npts;
+    float m = 0.0f;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        a.pq[i] = fpair_of(a.x[i], a.y[i]);
+        const double x = a.x[i], y = a.y[i];
+        a.pq[i] = fpair_of(x, y);
+        m = fmaxf(m, __double2float_ru(fmax(fabs(x), fabs(y))));
     }
+    for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, d));
+    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(sbits, __float_as_uint(m));
 }
 
 __global__ void __launch_bounds__(SCAN_BS) k_mark_all(DmrArgs a) {
@@ -982,6 +991,7 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     const uint32_t B = bcap < tcap ? bcap : tcap;
     const uint32_t G = (uint32_t)(c->sms > 0 ? 2 * c->sms : 304);
     gga_status r;
+    double tp = gga_now_ms();
     if ((r = dalloc(&b.x, pcap, s)) || (r = dalloc(&b.y, pcap, s)) || (r = dalloc(&b.pq, pcap, s)) || (r = dalloc(&b.tri, 3 * (size_t)tcap, s)) ||
         (r = dalloc(&b.nbr, 3 * (size_t)tcap, s)) || (r = dalloc(&b.bad, tcap, s)) ||
         (r = dalloc(&b.owner, tcap, s)) || (r = dalloc(&b.ring, tcap, s)) || (r = dalloc(&b.lock, tcap, s)) ||
@@ -999,13 +1009,17 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     b.hst->bcap = B;
     b.hst->max_rounds = MAX_ROUNDS;
     GGA_CK(cudaMemcpyAsync(b.st, b.hst, sizeof(DmrState), cudaMemcpyHostToDevice, s));
+    GGA_CK(cudaMemsetAsync(b.owner, 0, (size_t)tcap * sizeof(unsigned long long), s));
+    GGA_CK(cudaMemsetAsync(b.ring, 0, (size_t)tcap * sizeof(unsigned long long), s));
+    GGA_CK(cudaMemsetAsync(b.lock, 0, (size_t)tcap * sizeof(uint32_t), s));
+    GGA_CK(cudaMemsetAsync(b.bsum, 0, sizeof(uint32_t), s));
+    GGA_CK(cudaStreamSynchronize(s));
+    out->alloc_ms = gga_now_ms() - tp;
+    tp = gga_now_ms();
     GGA_CK(cudaMemcpyAsync(b.x, m->x, (size_t)m->npts * sizeof(double), cudaMemcpyHostToDevice, s));
     GGA_CK(cudaMemcpyAsync(b.y, m->y, (size_t)m->npts * sizeof(double), cudaMemcpyHostToDevice, s));
     GGA_CK(cudaMemcpyAsync(b.tri, m->tri, (size_t)m->ntri * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     GGA_CK(cudaMemcpyAsync(b.nbr, m->nbr, (size_t)m->ntri * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    GGA_CK(cudaMemsetAsync(b.owner, 0, (size_t)tcap * sizeof(unsigned long long), s));
-    GGA_CK(cudaMemsetAsync(b.ring, 0, (size_t)tcap * sizeof(unsigned long long), s));
-    GGA_CK(cudaMemsetAsync(b.lock, 0, (size_t)tcap * sizeof(uint32_t), s));
 
     DmrArgs a;
     a.x = b.x;
@@ -1030,19 +1044,25 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     a.st = b.st;
     a.cos_bound = cos_bound;
     a.cos_bound_f = (float)cos_bound;
-    /* every point's |x|, |y| (new points stay inside the input's bounding box),
-     * rounded up to float */
-    double smax = 0;
-    for (uint32_t i = 0; i < m->npts; ++i) smax = fmax(smax, fmax(fabs(m->x[i]), fabs(m->y[i])));
-    a.S = (float)(smax * (1.0 + 1.0 / 1048576.0)) + 1e-30f;
+    a.S = 0.0f; /* set from k_shadow's bound below; no kernel before it reads S */
     a.B = B;
     a.G = G;
     a.tail_max = B < TAIL_MAX ? B : TAIL_MAX;
     a.pf_max = PF_MAX;
     const unsigned plan_grid = ctx_grid(c, B, PLAN_BS);
     cudaEvent_t e0 = c->ev[0], e1 = c->ev[1];
+    /* the float pairs and the coordinate bound S (read back: it is a launch
+     * argument of every later kernel) */
+    k_shadow<<<G, SCAN_BS, 0, s>>>(a, b.bsum);
+    GGA_CK(cudaMemcpyAsync(&b.hst->pad_s, b.bsum, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GGA_CK(cudaStreamSynchronize(s));
+    out->upload_ms = gga_now_ms() - tp;
+    {
+        float sm;
+        memcpy(&sm, &b.hst->pad_s, sizeof sm);
+        a.S = sm * (1.0f + 1.0f / 1048576.0f) + 1e-30f;
+    }
     GGA_CK(cudaEventRecord(e0, s));
-    k_shadow<<<G, SCAN_BS, 0, s>>>(a);
     k_mark_all<<<G, SCAN_BS, 0, s>>>(a);
     for (uint32_t issued = 0;;) {
         for (uint32_t g = 0; g < ROUND_GROUP; ++g) {
@@ -1073,12 +1093,14 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     const DmrState h = *b.hst;
     if (h.err || h.stop == STOP_ERROR)
         return gga_fail(GGA_ERR_FORMAT, "mesh refinement: a triangle or neighbour id out of range");
+    tp = gga_now_ms();
     if ((r = gga_mesh_resize(m, h.npts, h.ntri))) return r;
     GGA_CK(cudaMemcpyAsync(m->x, b.x, (size_t)h.npts * sizeof(double), cudaMemcpyDeviceToHost, s));
     GGA_CK(cudaMemcpyAsync(m->y, b.y, (size_t)h.npts * sizeof(double), cudaMemcpyDeviceToHost, s));
     GGA_CK(cudaMemcpyAsync(m->tri, b.tri, (size_t)h.ntri * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     GGA_CK(cudaMemcpyAsync(m->nbr, b.nbr, (size_t)h.ntri * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     GGA_CK(cudaStreamSynchronize(s));
+    out->download_ms = gga_now_ms() - tp;
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     out->triangles_out = h.ntri;

@@ -27,22 +27,39 @@
  *     whose smallest angle is below the bound (the reference's checkbad rule,
  *     MINANGLE 25 in dmr.cu:32).
  */
+#define _GNU_SOURCE
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/mman.h>
 
 #include "gga_internal.h"
+
+/* Large mesh arrays are 2 MiB aligned and marked for transparent huge pages
+ * where the kernel offers them, so filling a fresh array (a refined mesh
+ * copied back from the GPU) takes one page fault per 2 MiB instead of one
+ * per base page.  Released with free(). */
+static void *mesh_array(size_t bytes) {
+    if (bytes == 0) bytes = 1;
+    if (bytes < (4u << 20)) return malloc(bytes);
+    void *p = NULL;
+    if (posix_memalign(&p, 2u << 20, bytes)) return NULL;
+#ifdef MADV_HUGEPAGE
+    madvise(p, bytes, MADV_HUGEPAGE);
+#endif
+    return p;
+}
 
 static gga_status mesh_alloc(uint32_t npts, uint32_t ntri, gga_mesh **out) {
     gga_mesh *m = (gga_mesh *)calloc(1, sizeof *m);
     if (!m) return gga_fail(GGA_ERR_NO_MEMORY, "mesh");
     m->npts = npts;
     m->ntri = ntri;
-    m->x = (double *)malloc((size_t)(npts ? npts : 1) * sizeof(double));
-    m->y = (double *)malloc((size_t)(npts ? npts : 1) * sizeof(double));
-    m->tri = (uint32_t *)malloc((size_t)(ntri ? ntri : 1) * 3 * sizeof(uint32_t));
-    m->nbr = (uint32_t *)malloc((size_t)(ntri ? ntri : 1) * 3 * sizeof(uint32_t));
+    m->x = (double *)mesh_array((size_t)npts * sizeof(double));
+    m->y = (double *)mesh_array((size_t)npts * sizeof(double));
+    m->tri = (uint32_t *)mesh_array((size_t)ntri * 3 * sizeof(uint32_t));
+    m->nbr = (uint32_t *)mesh_array((size_t)ntri * 3 * sizeof(uint32_t));
     if (!m->x || !m->y || !m->tri || !m->nbr) {
         gga_mesh_free(m);
         return gga_fail(GGA_ERR_NO_MEMORY, "mesh arrays (%u points, %u triangles)", npts, ntri);
@@ -52,10 +69,10 @@ static gga_status mesh_alloc(uint32_t npts, uint32_t ntri, gga_mesh **out) {
 }
 
 gga_status gga_mesh_resize(gga_mesh *m, uint32_t npts, uint32_t ntri) {
-    double *x = (double *)malloc((size_t)(npts ? npts : 1) * sizeof(double));
-    double *y = (double *)malloc((size_t)(npts ? npts : 1) * sizeof(double));
-    uint32_t *tri = (uint32_t *)malloc((size_t)(ntri ? ntri : 1) * 3 * sizeof(uint32_t));
-    uint32_t *nbr = (uint32_t *)malloc((size_t)(ntri ? ntri : 1) * 3 * sizeof(uint32_t));
+    double *x = (double *)mesh_array((size_t)npts * sizeof(double));
+    double *y = (double *)mesh_array((size_t)npts * sizeof(double));
+    uint32_t *tri = (uint32_t *)mesh_array((size_t)ntri * 3 * sizeof(uint32_t));
+    uint32_t *nbr = (uint32_t *)mesh_array((size_t)ntri * 3 * sizeof(uint32_t));
     if (!x || !y || !tri || !nbr) {
         free(x);
         free(y);

@@ -495,8 +495,11 @@ typedef struct gga_refine_stats {
     uint64_t insertions;             /* circumcentres inserted */
     uint64_t boundary_splits;        /* boundary edges split at their midpoint */
     uint64_t failed_plans;           /* insertions given up (walk, cavity or shape limits) */
-    double total_ms;                 /* upload + refinement + download */
+    double total_ms;                 /* the whole call: allocation, upload, refinement, download */
     double device_ms;                /* refinement rounds on the device */
+    double alloc_ms;                 /* device buffers and their initialisation */
+    double upload_ms;                /* mesh to the device */
+    double download_ms;              /* refined mesh to the host arrays */
 } gga_refine_stats;
 
 /* Reads "<base>.node" and "<base>.ele" (Triangle format, as readNodes /

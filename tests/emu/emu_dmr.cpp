@@ -47,10 +47,9 @@ int main(int argc, char **argv) {
     a.pq = pq.data(); a.cos_bound_f = (float)cb;
     a.tail_max = (uint32_t)std::min<long>(std::min<long>(tmax, B), TAIL_SORT);
     a.pf_max = (uint32_t)pfmax;
-    double smax = 0;
-    for (uint32_t i = 0; i < npts; ++i) smax = std::max(smax, std::max(std::fabs(x[i]), std::fabs(y[i])));
-    a.S = (float)(smax * (1.0 + 1.0 / 1048576.0)) + 1e-30f;
-    LAUNCH(k_shadow, G, BS);
+    uint32_t sbits = 0;
+    run_grid(G, BS, [&](int b) { switch (b) { case 0: k_shadow<0>(a, &sbits); break; case 1: k_shadow<1>(a, &sbits); break; case 2: k_shadow<2>(a, &sbits); break; default: k_shadow<3>(a, &sbits); } });
+    a.S = __uint_as_float(sbits) * (1.0f + 1.0f / 1048576.0f) + 1e-30f;
     LAUNCH(k_mark_all, G, BS);
     uint32_t tails = 0;
     for (uint32_t r = 0; st.stop == STOP_NONE && r < 4096; ++r) {
