@@ -537,13 +537,15 @@ class Context:
                  for r in recs[: min(nrec.value, cap)]], out)
 
     def refine(self, mesh: "Mesh", min_angle_deg: float = DMR_MIN_ANGLE, max_triangles: int = 0,
-               batch_cap: int = 0) -> dict:
+               batch_cap: int = 0, tail_max: int = 0, prefetch_max: int = 0) -> dict:
         """Delaunay refinement of `mesh` in place on this context's GPU until no
         angle is below min_angle_deg (the reference's dmr <basefile> run);
-        returns the refinement statistics (myresult's fields and timings)."""
+        returns the refinement statistics (myresult's fields and timings).
+        tail_max / prefetch_max move work between the engine's kernels
+        (gga_mesh_refine_ex) without changing the result."""
         st = N.RefineStats()
-        _check(N.load().gga_mesh_refine(self._h, mesh.handle, min_angle_deg, max_triangles, batch_cap,
-                                        C.byref(st)), "refine")
+        p = N.RefineParams(min_angle_deg, max_triangles, batch_cap, tail_max, prefetch_max)
+        _check(N.load().gga_mesh_refine_ex(self._h, mesh.handle, C.byref(p), C.byref(st)), "refine")
         return {k: getattr(st, k) for k, _ in st._fields_}
 
     def msbfs(self, graph: Graph, srcs: Sequence[int], stats: bool = False, out=None):

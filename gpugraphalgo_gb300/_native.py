@@ -163,6 +163,11 @@ class RefineStats(C.Structure):
     ]
 
 
+class RefineParams(C.Structure):
+    _fields_ = [("min_angle_deg", C.c_double), ("max_triangles", u32), ("batch_cap", u32), ("tail_max", u32),
+                ("prefetch_max", u32)]
+
+
 PD = C.POINTER(C.c_double)
 
 # name -> (restype, argtypes); every symbol declared in include/gga.h
@@ -230,6 +235,7 @@ SIGNATURES = {
     "gga_mesh_arrays": (C.c_int, [P, C.POINTER(PD), C.POINTER(PD), C.POINTER(PU32), C.POINTER(PU32)]),
     "gga_mesh_check": (C.c_int, [P, C.c_double, C.POINTER(MeshCheck)]),
     "gga_mesh_refine": (C.c_int, [P, P, C.c_double, u32, u32, C.POINTER(RefineStats)]),
+    "gga_mesh_refine_ex": (C.c_int, [P, P, C.POINTER(RefineParams), C.POINTER(RefineStats)]),
 }
 
 _lib = None

@@ -984,8 +984,8 @@ template <class T> gga_status dalloc(T **p, size_t n, cudaStream_t s) {
     return GGA_OK;
 }
 
-gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, uint32_t bcap, DmrBufs &b,
-                      gga_refine_stats *out) {
+gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, uint32_t bcap, uint32_t tail_max,
+                      uint32_t pf_max, DmrBufs &b, gga_refine_stats *out) {
     cudaStream_t s = c->st;
     const uint32_t pcap = (uint32_t)(m->npts + (uint64_t)(tcap - m->ntri));
     const uint32_t B = bcap < tcap ? bcap : tcap;
@@ -1047,8 +1047,8 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     a.S = 0.0f; /* set from k_shadow's bound below; no kernel before it reads S */
     a.B = B;
     a.G = G;
-    a.tail_max = B < TAIL_MAX ? B : TAIL_MAX;
-    a.pf_max = PF_MAX;
+    a.tail_max = tail_max == 0xFFFFFFFFu ? 0u : min(min(tail_max ? tail_max : TAIL_MAX, TAIL_SORT), B);
+    a.pf_max = pf_max ? pf_max : PF_MAX;
     const unsigned plan_grid = ctx_grid(c, B, PLAN_BS);
     cudaEvent_t e0 = c->ev[0], e1 = c->ev[1];
     /* the float pairs and the coordinate bound S (read back: it is a launch
@@ -1129,12 +1129,14 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
 
 } // namespace
 
-extern "C" gga_status gga_mesh_refine(gga_ctx *c, gga_mesh *m, double min_angle_deg, uint32_t max_triangles,
-                                      uint32_t batch_cap, gga_refine_stats *st) {
+extern "C" gga_status gga_mesh_refine_ex(gga_ctx *c, gga_mesh *m, const gga_refine_params *p,
+                                         gga_refine_stats *st) {
     const double t0 = gga_now_ms();
-    if (!c || !m) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    if (!c || !m || !p) return gga_fail(GGA_ERR_INVALID_ARG, "NULL argument");
+    double min_angle_deg = p->min_angle_deg;
     if (!(min_angle_deg < 60.0)) return gga_fail(GGA_ERR_INVALID_ARG, "min angle %g (must be below 60)", min_angle_deg);
     if (min_angle_deg <= 0) min_angle_deg = GGA_DMR_MIN_ANGLE;
+    const uint32_t max_triangles = p->max_triangles, batch_cap = p->batch_cap;
     const uint64_t dflt = 4ull * m->ntri + 65536;
     const uint64_t tcap64 = max_triangles ? max_triangles : (dflt < 0x3FFFFFFFull ? dflt : 0x3FFFFFFFull);
     if (tcap64 < m->ntri) return gga_fail(GGA_ERR_INVALID_ARG, "max_triangles %u < %u", max_triangles, m->ntri);
@@ -1149,8 +1151,18 @@ extern "C" gga_status gga_mesh_refine(gga_ctx *c, gga_mesh *m, double min_angle_
     if ((s = ctx_activate(c))) return s;
     DmrBufs b;
     s = refine_run(c, m, cos(min_angle_deg * (3.14159265358979323846 / 180.0)), (uint32_t)tcap64,
-                   batch_cap ? batch_cap : (1u << 20), b, out);
+                   batch_cap ? batch_cap : (1u << 20), p->tail_max, p->prefetch_max, b, out);
     b.free_all(c->st);
     out->total_ms = gga_now_ms() - t0;
     return s;
+}
+
+extern "C" gga_status gga_mesh_refine(gga_ctx *c, gga_mesh *m, double min_angle_deg, uint32_t max_triangles,
+                                      uint32_t batch_cap, gga_refine_stats *st) {
+    gga_refine_params p;
+    memset(&p, 0, sizeof p);
+    p.min_angle_deg = min_angle_deg;
+    p.max_triangles = max_triangles;
+    p.batch_cap = batch_cap;
+    return gga_mesh_refine_ex(c, m, &p, st);
 }

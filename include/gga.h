@@ -541,6 +541,21 @@ gga_status gga_mesh_check(const gga_mesh *m, double min_angle_deg, gga_mesh_chec
 gga_status gga_mesh_refine(gga_ctx *ctx, gga_mesh *m, double min_angle_deg, uint32_t max_triangles,
                            uint32_t batch_cap, gga_refine_stats *st);
 
+/* gga_mesh_refine with the engine's schedule knobs, which change where the
+ * work runs, never the result: tail_max is the number of bad triangles at
+ * which one block takes over the rounds (0 = 2048; capped at 4096 and at the
+ * batch cap; 0xFFFFFFFF keeps every round on the multi-kernel path);
+ * prefetch_max is the largest round planned by the prefetching kernel
+ * variant (0 = 32,768; 1 plans every larger round with the lean one). */
+typedef struct gga_refine_params {
+    double min_angle_deg;   /* <= 0: GGA_DMR_MIN_ANGLE */
+    uint32_t max_triangles; /* 0: 4 x the input + 65,536 */
+    uint32_t batch_cap;     /* 0: 1,048,576 */
+    uint32_t tail_max;      /* 0: 2048; 0xFFFFFFFF: never */
+    uint32_t prefetch_max;  /* 0: 32,768 */
+} gga_refine_params;
+gga_status gga_mesh_refine_ex(gga_ctx *ctx, gga_mesh *m, const gga_refine_params *p, gga_refine_stats *st);
+
 #ifdef __cplusplus
 }
 #endif

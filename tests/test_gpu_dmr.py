@@ -51,6 +51,20 @@ def test_refine_matches_oracle_bit_for_bit(ctx, kind, size, bcap):
     _assert_valid(mesh, area)
 
 
+@pytest.mark.parametrize("tail_max,prefetch_max", [(0xFFFFFFFF, 0), (16, 0), (0, 1), (0, 1 << 30), (7, 1)],
+                         ids=["no-tail", "tail-hand-back", "lean-plans", "prefetch-plans", "hand-back-lean"])
+def test_refine_schedule_knobs_never_change_the_result(ctx, tail_max, prefetch_max):
+    """Every round on the multi-kernel path, the one-block tail kernel taking
+    over and handing back, and either planning variant: the same mesh as the
+    oracle's."""
+    mesh = gga.Mesh.random(12000, seed=21)
+    before = mesh.arrays()
+    st = ctx.refine(mesh, tail_max=tail_max, prefetch_max=prefetch_max)
+    want = oracle.mesh_refine(before)
+    _assert_same(mesh.arrays(), want)
+    assert st["rounds"] == want["rounds"] and st["bad_out"] == 0
+
+
 def test_refine_is_repeatable(ctx):
     a, b = gga.Mesh.random(5000, seed=2), gga.Mesh.random(5000, seed=2)
     ctx.refine(a)
