@@ -1,14 +1,16 @@
 /*
  * Delaunay mesh refinement on the GPU (the reference's DMR program,
  * Programs/CUDA_src/Kepler_DMR/dmr.cu:54-398 with its refine kernels in
- * m_refine.h), redesigned as rounds of nine short kernels over a mesh kept
- * resident in HBM.
+ * m_refine.h), redesigned as rounds of short kernels over a mesh kept
+ * resident in HBM, and a one-block kernel for the small last rounds.
  *
  * Round (all state on the device; the host only launches):
  *   k_bad_count / k_bad_gather  worklist = the bad triangles in ascending id
  *                               (two-pass chunked compaction; at most
  *                               batch_cap of them);
- *   k_plan      one thread per bad triangle: circumcentre, straight walk to
+ *   k_plan      one thread per bad triangle (a lean variant for big rounds, a
+ *               prefetching one for rounds of up to pf_max plans; both are
+ *               launched, one returns): circumcentre, straight walk to
  *               the triangle that holds it (or to the boundary edge the walk
  *               leaves through), cavity growth by the in-circle test, the
  *               boundary-encroachment rule, and 64-bit atomicMax claims of
@@ -26,6 +28,9 @@
  *               new point, relinks the outer ring and re-marks the new
  *               triangles;
  *   k_finish    advances the point/triangle counts and the stop word.
+ * k_tail       once at most tail_max triangles are bad, one block runs whole
+ *              rounds with the same per-plan functions between __syncthreads
+ *              and rebuilds the worklist from the triangles a round can change.
  * Two rings may share a triangle (their plans rewrite different edges of it),
  * and then neither plan's new triangles can hold the other's point, so the
  * commits of one round equal some sequential order of insertions.
