@@ -332,16 +332,36 @@ static double urand(uint64_t *s) {
 }
 
 /* Lawson flips: while an interior edge has its neighbour's far vertex inside
- * the circumcircle, replace the edge by the other diagonal of the quad. */
+ * the circumcircle, replace the edge by the other diagonal of the quad.  The
+ * stack holds (triangle, edge) codes, each at most once (queued flags), so
+ * it never holds more than 3 * ntri entries. */
 static gga_status lawson(gga_mesh *m) {
+    const size_t ncode = (size_t)m->ntri * 4; /* code = t << 2 | i, i < 3 */
     uint32_t *stack = (uint32_t *)malloc(((size_t)m->ntri * 3 + 1) * sizeof(uint32_t));
-    if (!stack) return gga_fail(GGA_ERR_NO_MEMORY, "flip stack");
+    uint8_t *queued = (uint8_t *)calloc(ncode ? ncode : 1, 1);
+    if (!stack || !queued) {
+        free(stack);
+        free(queued);
+        return gga_fail(GGA_ERR_NO_MEMORY, "flip stack");
+    }
     size_t sp = 0;
     for (uint32_t t = 0; t < m->ntri; ++t)
-        for (uint32_t i = 0; i < 3; ++i) stack[sp++] = (t << 2) | i;
+        for (uint32_t i = 0; i < 3; ++i) {
+            stack[sp++] = (t << 2) | i;
+            queued[(t << 2) | i] = 1;
+        }
+#define LAWSON_PUSH(code)                                                                                             \
+    do {                                                                                                               \
+        const uint32_t c_ = (code);                                                                                    \
+        if (!queued[c_]) {                                                                                             \
+            queued[c_] = 1;                                                                                            \
+            stack[sp++] = c_;                                                                                          \
+        }                                                                                                              \
+    } while (0)
     uint64_t flips = 0;
     while (sp) {
         const uint32_t code = stack[--sp], t = code >> 2, i = code & 3;
+        queued[code] = 0;
         const uint32_t u = m->nbr[3 * t + i];
         if (u == GGA_MESH_NONE) continue;
         uint32_t *tv = m->tri + 3 * (size_t)t, *uv = m->tri + 3 * (size_t)u;
@@ -374,13 +394,15 @@ static gga_status lawson(gga_mesh *m) {
         if (nb_ca != GGA_MESH_NONE)
             for (int k = 0; k < 3; ++k)
                 if (m->nbr[3 * nb_ca + k] == t) m->nbr[3 * nb_ca + k] = u;
-        stack[sp++] = (t << 2) | 0;
-        stack[sp++] = (t << 2) | 2;
-        stack[sp++] = (u << 2) | 0;
-        stack[sp++] = (u << 2) | 1;
+        LAWSON_PUSH((t << 2) | 0);
+        LAWSON_PUSH((t << 2) | 2);
+        LAWSON_PUSH((u << 2) | 0);
+        LAWSON_PUSH((u << 2) | 1);
         if (++flips > 64ull * m->ntri + 1024) break; /* safety net */
     }
+#undef LAWSON_PUSH
     free(stack);
+    free(queued);
     return GGA_OK;
 }
 

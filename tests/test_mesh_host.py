@@ -202,3 +202,49 @@ def test_dmr_cli_usage_and_missing_input_need_no_device(tmp_path):
     assert r.returncode == 1 and r.stdout.startswith("Usage: ")
     r = subprocess.run([exe, str(tmp_path / "none")], capture_output=True, text=True, timeout=60)
     assert r.returncode == 2 and "cannot open" in r.stderr
+
+
+def _golden_dmr():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "dmr_io.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("name", ["jittered6x5", "random60"])
+def test_loader_matches_the_reference_readers(tmp_path, name):
+    """tests/golden/dmr_io.json holds what the reference's own readNodes /
+    readTriangles (helpers.h:5-63, compiled from its sources) parsed from these
+    files: the same points (the reference reads them as float), the same
+    triangles, and its .poly segments are this library's boundary edges."""
+    fx = _golden_dmr()[name]
+    for ext in ("node", "ele", "poly"):
+        (tmp_path / f"m.{ext}").write_text(fx[ext])
+    a = gga.Mesh.load(str(tmp_path / "m")).arrays()
+    nele = len(a["tri"]) // 3
+    assert fx["ref_nnodes"] == len(a["x"])
+    np.testing.assert_array_equal(a["x"].astype(np.float32), np.array(fx["ref_x"], np.float32))
+    np.testing.assert_array_equal(a["y"].astype(np.float32), np.array(fx["ref_y"], np.float32))
+    ref_tri = np.array(fx["ref_tri"], np.uint32).reshape(-1, 3)
+    np.testing.assert_array_equal(ref_tri[:nele].ravel(), a["tri"])
+    segs = ref_tri[nele:]
+    assert fx["ref_ntriangles"] == nele + len(segs) and (segs[:, 2] == 1234567890).all()  # INVALIDID third node
+    t, n = a["tri"].reshape(-1, 3), a["nbr"].reshape(-1, 3)
+    ours = {tuple(sorted((int(t[k, (i + 1) % 3]), int(t[k, (i + 2) % 3]))))
+            for k in range(nele) for i in range(3) if n[k, i] == gga.MESH_NONE}
+    assert ours == {tuple(sorted(map(int, s[:2]))) for s in segs}
+
+
+def test_cli_result_row_matches_the_reference_writer():
+    """The row format of gga_dmr.c's result.vi line, applied to the fields the
+    fixture gave the reference's own getname / writeResult (myresult.h:13-52),
+    reproduces the rows that writer appended."""
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(gga.__file__), "csrc", "gga_dmr.c")).read()
+    fmt = re.search(r'fprintf\(fp, "([^"]*)\\n"', src).group(1).replace("%llu", "%u")
+    fx = _golden_dmr()
+    rows = fx["result_vi"].splitlines()
+    for line, name in zip(rows, ["jittered6x5", "random60"]):
+        f = fx[name]["row_fields"]
+        assert fmt % ("r_dmr", name, *f[:5], float(f[5]), float(f[6])) == line
