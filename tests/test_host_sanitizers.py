@@ -1,9 +1,12 @@
-"""The host mesh code (csrc/mesh_host.c, with csrc/graph_host.c's helpers) and
-the oracle's refinement (oracle/mesh_oracle.c) built with AddressSanitizer
-and UndefinedBehaviorSanitizer and run over a sweep of generated meshes, a
-file round trip and refinements (tests/asan/mesh_sweep.c).  A heap overflow
-in the jittered generator's flip stack was found this way; the sweep keeps
-the host side free of out-of-bounds accesses."""
+"""Host code built with AddressSanitizer and UndefinedBehaviorSanitizer and run
+over sweeps of inputs: the mesh code (csrc/mesh_host.c) with the oracle's
+refinement (oracle/mesh_oracle.c) over generated meshes, a file round trip
+and refinements (tests/asan/mesh_sweep.c); the graph code (csrc/graph_host.c)
+with the BFS/SSSP oracle over R-MAT and grid graphs, .gr round trips,
+truncated .gr files, split rules, node splits and traversals
+(tests/asan/graph_sweep.c).  A heap overflow in the jittered generator's flip
+stack was found this way; the sweeps keep the host side free of
+out-of-bounds accesses and undefined behaviour."""
 from __future__ import annotations
 
 import os
@@ -16,14 +19,22 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CS = os.path.join(ROOT, "gpugraphalgo_gb300", "csrc")
 
 
-def test_mesh_host_and_oracle_under_sanitizers(tmp_path):
+SWEEPS = {
+    "mesh": ["tests/asan/mesh_sweep.c", "gpugraphalgo_gb300/csrc/mesh_host.c", "gpugraphalgo_gb300/csrc/graph_host.c",
+             "oracle/mesh_oracle.c"],
+    "graph": ["tests/asan/graph_sweep.c", "gpugraphalgo_gb300/csrc/graph_host.c", "oracle/gga_oracle.c",
+              "oracle/gen_inputs.c"],
+}
+
+
+@pytest.mark.parametrize("which", sorted(SWEEPS))
+def test_host_code_under_sanitizers(tmp_path, which):
     if shutil.which("gcc") is None:
         pytest.skip("gcc not available")
-    exe = str(tmp_path / "mesh_sweep")
+    exe = str(tmp_path / f"{which}_sweep")
     cmd = ["gcc", "-g", "-O1", "-std=c11", "-pthread", "-ffp-contract=off", "-fsanitize=address,undefined",
-           "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer", "-I", CS,
-           os.path.join(ROOT, "tests", "asan", "mesh_sweep.c"), os.path.join(CS, "mesh_host.c"),
-           os.path.join(CS, "graph_host.c"), os.path.join(ROOT, "oracle", "mesh_oracle.c"), "-lm", "-o", exe]
+           "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer", "-I", CS] + \
+        [os.path.join(ROOT, f) for f in SWEEPS[which]] + ["-lm", "-o", exe]
     b = subprocess.run(cmd, capture_output=True, text=True)
     if b.returncode != 0 and "sanitize" in b.stderr:
         pytest.skip("the compiler has no sanitizer runtime")
