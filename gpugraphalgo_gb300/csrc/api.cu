@@ -85,6 +85,7 @@ void gga_ctx_destroy(gga_ctx *c) {
     cudaFreeHost(m.hacc);
     if (m.copy) cudaStreamDestroy(m.copy);
     frontier_scratch_free(&c->fs);
+    if (c->stage) cudaFreeHost(c->stage);
     cudaFree(c->dflag);
     cudaFreeHost(c->hflag);
     cudaFree(c->heavy);

@@ -47,6 +47,8 @@ struct gga_ctx {
     std::vector<uint32_t> trace_rounds; /* 5 words per round of the last traced solve */
     std::vector<uint32_t> trace_cta;    /* busy kilocycles per CTA */
     std::string tune_report;            /* JSON of the last gga_autotune's trials */
+    void *stage = nullptr;              /* pinned staging for large device-to-host results (mesh refinement) */
+    size_t stage_bytes = 0;
     std::mutex mu;
 };
 

@@ -56,7 +56,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
+#include <thread>
+#include <vector>
 
 #include "ctx.cuh"
 #include "gga_device.cuh"
@@ -984,6 +987,53 @@ struct DmrBufs {
     }
 };
 
+/* Device-to-host copy of a large result into pageable memory: chunks go to
+ * two pinned buffers kept in the context (pinned once, reused), and while the
+ * next chunk's DMA runs, host threads copy the finished one to its place
+ * (and take the destination's first-touch page faults in parallel).  The
+ * driver's own pageable path copies with one host thread. */
+constexpr size_t STAGE_CHUNK = 32u << 20;
+
+gga_status copy_to_host(gga_ctx *c, cudaStream_t s, void *dst, const void *src, size_t bytes) {
+    if (bytes < (8u << 20)) { /* small: the plain path */
+        GGA_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+        GGA_CK(cudaStreamSynchronize(s));
+        return GGA_OK;
+    }
+    if (c->stage_bytes < 2 * STAGE_CHUNK) {
+        if (c->stage) cudaFreeHost(c->stage);
+        c->stage = nullptr;
+        c->stage_bytes = 0;
+        GGA_CK(cudaMallocHost(&c->stage, 2 * STAGE_CHUNK));
+        c->stage_bytes = 2 * STAGE_CHUNK;
+    }
+    cudaEvent_t done[2] = {c->ev[2], c->ev[3]};
+    const size_t nchunk = (bytes + STAGE_CHUNK - 1) / STAGE_CHUNK;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned nt = std::max(1u, std::min(16u, hw ? hw / 2 : 4u));
+    auto issue = [&](size_t i) -> cudaError_t {
+        const size_t off = i * STAGE_CHUNK, len = std::min(STAGE_CHUNK, bytes - off);
+        cudaError_t e = cudaMemcpyAsync((char *)c->stage + (i & 1) * STAGE_CHUNK, (const char *)src + off, len,
+                                        cudaMemcpyDeviceToHost, s);
+        return e == cudaSuccess ? cudaEventRecord(done[i & 1], s) : e;
+    };
+    GGA_CK(issue(0));
+    for (size_t i = 0; i < nchunk; ++i) {
+        GGA_CK(cudaEventSynchronize(done[i & 1]));
+        if (i + 1 < nchunk) GGA_CK(issue(i + 1)); /* buffer (i+1)&1 was drained in iteration i-1 */
+        const size_t off = i * STAGE_CHUNK, len = std::min(STAGE_CHUNK, bytes - off);
+        const char *from = (const char *)c->stage + (i & 1) * STAGE_CHUNK;
+        char *to = (char *)dst + off;
+        const size_t per = (len + nt - 1) / nt;
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nt && t * per < len; ++t)
+            th.emplace_back([=] { memcpy(to + t * per, from + t * per, std::min(per, len - t * per)); });
+        memcpy(to, from, std::min(per, len));
+        for (auto &x : th) x.join();
+    }
+    return GGA_OK;
+}
+
 template <class T> gga_status dalloc(T **p, size_t n, cudaStream_t s) {
     GGA_CK(cudaMallocAsync((void **)p, (n ? n : 1) * sizeof(T), s));
     return GGA_OK;
@@ -1100,11 +1150,11 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
         return gga_fail(GGA_ERR_FORMAT, "mesh refinement: a triangle or neighbour id out of range");
     tp = gga_now_ms();
     if ((r = gga_mesh_resize(m, h.npts, h.ntri))) return r;
-    GGA_CK(cudaMemcpyAsync(m->x, b.x, (size_t)h.npts * sizeof(double), cudaMemcpyDeviceToHost, s));
-    GGA_CK(cudaMemcpyAsync(m->y, b.y, (size_t)h.npts * sizeof(double), cudaMemcpyDeviceToHost, s));
-    GGA_CK(cudaMemcpyAsync(m->tri, b.tri, (size_t)h.ntri * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    GGA_CK(cudaMemcpyAsync(m->nbr, b.nbr, (size_t)h.ntri * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    GGA_CK(cudaStreamSynchronize(s));
+    if ((r = copy_to_host(c, s, m->x, b.x, (size_t)h.npts * sizeof(double))) ||
+        (r = copy_to_host(c, s, m->y, b.y, (size_t)h.npts * sizeof(double))) ||
+        (r = copy_to_host(c, s, m->tri, b.tri, (size_t)h.ntri * 3 * sizeof(uint32_t))) ||
+        (r = copy_to_host(c, s, m->nbr, b.nbr, (size_t)h.ntri * 3 * sizeof(uint32_t))))
+        return r;
     out->download_ms = gga_now_ms() - tp;
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
