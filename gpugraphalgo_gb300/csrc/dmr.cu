@@ -8,6 +8,8 @@
  *   k_bad_count / k_bad_gather  worklist = the bad triangles in ascending id
  *                               (two-pass chunked compaction; at most
  *                               batch_cap of them);
+ *   k_decide    one warp: done, out of rounds, over to k_tail, or the round's
+ *               worklist length;
  *   k_plan      one thread per bad triangle (a lean variant for big rounds, a
  *               prefetching one for rounds of up to pf_max plans; both are
  *               launched, one returns): circumcentre, straight walk to
@@ -313,38 +315,16 @@ __global__ void __launch_bounds__(SCAN_BS) k_bad_count(DmrArgs a) {
     if (threadIdx.x == 0) a.bsum[blockIdx.x] = c;
 }
 
+/* The worklist: the bad triangles in ascending id, at most bcap of them.
+ * Writes no state word: every block reads the same stop, tail and err at
+ * entry, so a block never splits between returning and entering the scans. */
 __global__ void __launch_bounds__(SCAN_BS) k_bad_gather(DmrArgs a) {
     __shared__ uint32_t ws[32];
-    DmrState *st = a.st;
-    if (st->stop != STOP_NONE || st->tail) return;
-    if (st->err) { /* an id out of range: nothing reads the mesh after this */
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            st->nw = 0;
-            st->stop = STOP_ERROR;
-        }
-        return;
-    }
-    const uint32_t total = prefix_of(a, 0, a.G, ws);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        st->nbad = total;
-        if (st->round == 0) st->bad_in = total;
-        if (total == 0) {
-            st->nw = 0;
-            st->stop = STOP_DONE;
-        } else if (st->round >= st->max_rounds) {
-            st->nw = 0;
-            st->stop = STOP_ROUNDS;
-        } else if (total <= a.tail_max) { /* k_tail runs this round and the next ones */
-            st->nw = total;
-            st->tail = 1;
-        } else {
-            st->round += 1;
-            st->nw = total < st->bcap ? total : st->bcap;
-        }
-    }
-    if (total == 0) return;
+    const DmrState *st = a.st;
+    if (st->stop != STOP_NONE || st->tail || st->err) return;
     uint32_t base = prefix_of(a, 0, blockIdx.x, ws);
-    if (base >= st->bcap) return;
+    const uint32_t bcap = st->bcap;
+    if (base >= bcap) return;
     uint32_t lo, hi;
     chunk_of(st->ntri, blockIdx.x, a.G, lo, hi);
     for (uint32_t t0 = lo; t0 < hi; t0 += blockDim.x) {
@@ -352,9 +332,43 @@ __global__ void __launch_bounds__(SCAN_BS) k_bad_gather(DmrArgs a) {
         const uint32_t f = t < hi ? a.bad[t] : 0;
         uint32_t tot;
         const uint32_t pos = base + block_exclusive_scan(f, ws, &tot);
-        if (f && pos < st->bcap) a.work[pos] = t;
+        if (f && pos < bcap) a.work[pos] = t;
         base += tot;
         __syncthreads();
+    }
+}
+
+/* One warp decides the round from the bad count: done, out of rounds, over to
+ * k_tail (which then runs this round and the next ones), or the next round
+ * of at most bcap plans. */
+__global__ void k_decide(DmrArgs a) {
+    DmrState *st = a.st;
+    if (st->stop != STOP_NONE || st->tail) return;
+    if (st->err) { /* an id out of range: nothing reads the mesh after this */
+        if (threadIdx.x == 0) {
+            st->nw = 0;
+            st->stop = STOP_ERROR;
+        }
+        return;
+    }
+    uint32_t total = 0;
+    for (uint32_t j = threadIdx.x; j < a.G; j += 32) total += a.bsum[j];
+    for (int d = 16; d > 0; d >>= 1) total += __shfl_down_sync(0xffffffffu, total, d);
+    if (threadIdx.x != 0) return;
+    st->nbad = total;
+    if (st->round == 0) st->bad_in = total;
+    if (total == 0) {
+        st->nw = 0;
+        st->stop = STOP_DONE;
+    } else if (st->round >= st->max_rounds) {
+        st->nw = 0;
+        st->stop = STOP_ROUNDS;
+    } else if (total <= a.tail_max) {
+        st->nw = total;
+        st->tail = 1;
+    } else {
+        st->round += 1;
+        st->nw = total < st->bcap ? total : st->bcap;
     }
 }
 
@@ -1123,6 +1137,7 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
         for (uint32_t g = 0; g < ROUND_GROUP; ++g) {
             k_bad_count<<<G, SCAN_BS, 0, s>>>(a);
             k_bad_gather<<<G, SCAN_BS, 0, s>>>(a);
+            k_decide<<<1, 32, 0, s>>>(a);
             k_plan<false><<<plan_grid, PLAN_BS, 0, s>>>(a);
             k_plan<true><<<plan_grid, PLAN_BS, 0, s>>>(a);
             k_resolve0<<<plan_grid, PLAN_BS, 0, s>>>(a);

@@ -55,6 +55,7 @@ int main(int argc, char **argv) {
     for (uint32_t r = 0; st.stop == STOP_NONE && r < 4096; ++r) {
         LAUNCH(k_bad_count, G, BS);
         LAUNCH(k_bad_gather, G, BS);
+        LAUNCH(k_decide, 1, 32);
         LAUNCH_PF(false, 2, PBS);
         LAUNCH_PF(true, 2, PBS);
         LAUNCH(k_resolve0, 2, PBS);
