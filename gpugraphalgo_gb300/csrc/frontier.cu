@@ -619,18 +619,29 @@ __device__ __forceinline__ void expand_units(const Args &a, Ctrl &C, const Stage
             }
             /* updates in phases, so a thread's atomics for its PB edges are in
              * flight together instead of one dependent pair after another:
-             * first the distance atomicMin / visited atomicOr of every edge,
+             * first the distance reduction / visited atomicOr of every edge,
              * then the stamp / far-bit atomic of every improved one, then the
-             * shared-memory staging.  Relaxation is atomicMin on uint32
-             * distances as M_my_drelax does (cudaKernels.h:323-330); the
-             * probe (a recent read of dist[v] or of the visited word) may be
-             * stale but never lower than the truth, so it only filters. */
+             * shared-memory staging.  Relaxation is a min on uint32
+             * distances as M_my_drelax's atomicMin is (cudaKernels.h:323-330);
+             * the probe (a recent read of dist[v] or of the visited word) may
+             * be stale but never lower than the truth.  SSSP takes an edge
+             * whose offer beats the probe as improving v without waiting for
+             * the old value: the min goes out as a fire-and-forget red.min,
+             * and v is queued (once per round, by its stamp) even if a
+             * concurrent offer landed lower.  Its expansion reads dist[v]
+             * then, so the extra entry relaxes with the true value, and an
+             * entry queued by a lower offer exists whenever one landed; the
+             * distances reached are the same, one dependent L2 round trip
+             * sooner per edge. */
             uint32_t won = 0; /* bit q: edge q improved v (SSSP) or visited it first (BFS) */
 #pragma unroll
             for (uint32_t q = 0; q < PB; ++q) {
                 if (!act[q]) continue;
                 if (SSSP) {
-                    if (alt[q] < probe[q] && alt[q] < atomicMin(a.dist + v[q], alt[q])) won |= 1u << q;
+                    if (alt[q] < probe[q]) {
+                        red_min_u32(a.dist + v[q], alt[q]);
+                        won |= 1u << q;
+                    }
                 } else {
                     const uint32_t bit = 1u << (v[q] & 31);
                     if (!(probe[q] & bit) && !(atomicOr(a.bits + (v[q] >> 5), bit) & bit)) won |= 1u << q;

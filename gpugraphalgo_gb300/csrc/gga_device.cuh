@@ -112,6 +112,11 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
+/* Fire-and-forget min (the same relaxed, device-scope semantics as an
+ * atomicMin whose old value is not read). */
+__device__ __forceinline__ void red_min_u32(uint32_t *p, uint32_t v) {
+    asm volatile("red.relaxed.gpu.global.min.u32 [%0], %1;" ::"l"(p), "r"(v));
+}
 __device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }

@@ -126,6 +126,7 @@ inline uint4 make_uint4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) { return
 enum { GGA_BFS = 0, GGA_SSSP = 1 };
 inline uint32_t ld_acquire_u32(const uint32_t *p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
 inline uint32_t ld_relaxed_u32(const uint32_t *p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
+inline void red_min_u32(uint32_t *p, uint32_t v) { atomicMin(p, v); }
 inline unsigned long long ld_relaxed_u64(const unsigned long long *p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
 inline uint64_t global_timer_ns() { return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch()).count(); }
 inline uint32_t lane_id() { return threadIdx.x & 31u; }
