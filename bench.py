@@ -765,6 +765,7 @@ def run_gga(args, dist: Dist):
         src_list = [int(s) for s in srcs]
         e2e_steps = max(5, min(args.steps, 10))
         phases = {"release": 0.0, "upload": 0.0, "prepare": 0.0, "bfs": 0.0, "sssp": 0.0}
+        per_step = {k: [] for k in phases}
 
         def e2e_warm():  # untimed: first touch of the page-locked output rows
             for algo in ("bfs", "sssp"):
@@ -790,6 +791,7 @@ def run_gga(args, dist: Dist):
             for k, dt in (("release", tb - ta), ("upload", tc - tb), ("prepare", td - tc), ("bfs", te - td),
                           ("sssp", tf - te)):
                 phases[k] += dt
+                per_step[k].append(round(dt * 1e3, 2))
         ctx.synchronize()
         dt = time.perf_counter() - t0
         dt_max = dist.max(dt)
@@ -798,6 +800,7 @@ def run_gga(args, dist: Dist):
                       "d2h_bytes_per_step": 4 * info["nodes_orig"] * 2 * len(srcs),
                       "steps": e2e_steps, "ms_per_step": dt * 1e3 / e2e_steps,
                       "breakdown_ms_per_step": {k: v * 1e3 / e2e_steps for k, v in phases.items()},
+                      "phase_ms_each_step": per_step,
                       "device_ms_per_step": ms_max / args.steps}
         g.cudaCopy(ctx)
         ctx.prepare(g, "bfs")

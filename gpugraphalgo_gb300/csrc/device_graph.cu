@@ -110,6 +110,15 @@ static void dev_free_split(DevGraph *d) {
     d->ns = d->mda = d->npar = 0;
 }
 
+/* The base arrays and the light/heavy order come from the device's
+ * stream-ordered pool (the context keeps up to 4 GiB of it mapped), so a
+ * graph released and uploaded again reuses the same memory instead of
+ * mapping fresh pages.  Released after a device synchronize, as cudaFree
+ * would: no launch on any stream still reads them. */
+static void pool_release(void *p) {
+    if (p) cudaFreeAsync(p, 0);
+}
+
 static void dev_graph_release(gga_graph *g) {
     DevGraph *d = (DevGraph *)g->dev;
     if (!d) return;
@@ -117,8 +126,10 @@ static void dev_graph_release(gga_graph *g) {
     cudaGetDevice(&prev);
     cudaSetDevice(d->device);
     dev_free_split(d);
-    cudaFree(d->off); cudaFree(d->col); cudaFree(d->wt);
-    cudaFree(d->lcol); cudaFree(d->lwt); cudaFree(d->light);
+    cudaDeviceSynchronize();
+    pool_release(d->off); pool_release(d->col); pool_release(d->wt);
+    pool_release(d->lcol); pool_release(d->lwt); pool_release(d->light);
+    cudaStreamSynchronize(0);
     if (prev >= 0) cudaSetDevice(prev);
     free(d);
     g->dev = nullptr;
@@ -302,12 +313,13 @@ gga_status dev_graph_light_heavy(gga_graph *g, uint32_t delta, cudaStream_t st) 
     const size_t mpad = ((size_t)d->m + 4) & ~(size_t)3;
     cudaError_t e = cudaSuccess;
     if (!d->lcol) {
-        e = cudaMalloc((void **)&d->lcol, mpad * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMalloc((void **)&d->lwt, mpad * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMalloc((void **)&d->light, ((size_t)d->n + 1) * sizeof(uint32_t));
+        e = cudaMallocAsync((void **)&d->lcol, mpad * sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = cudaMallocAsync((void **)&d->lwt, mpad * sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = cudaMallocAsync((void **)&d->light, ((size_t)d->n + 1) * sizeof(uint32_t), st);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            cudaFree(d->lcol); cudaFree(d->lwt); cudaFree(d->light);
+            cudaStreamSynchronize(st);
+            pool_release(d->lcol); pool_release(d->lwt); pool_release(d->light);
             d->lcol = d->lwt = d->light = nullptr;
             return gga_fail(GGA_ERR_CUDA, "light/heavy order (%u edges): %s", d->m, cudaGetErrorString(e));
         }
@@ -419,9 +431,9 @@ gga_status dev_graph_ensure(gga_graph *g, int device, cudaStream_t st) {
         d->symmetric = g->symmetric;
         d->wsymmetric = g->wsymmetric;
         size_t mpad = ((size_t)g->m + 4) & ~(size_t)3; /* room for 16-byte vector loads */
-        cudaError_t e = cudaMalloc((void **)&d->off, ((size_t)g->n + 1) * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMalloc((void **)&d->col, mpad * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMalloc((void **)&d->wt, mpad * sizeof(uint32_t));
+        cudaError_t e = cudaMallocAsync((void **)&d->off, ((size_t)g->n + 1) * sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = cudaMallocAsync((void **)&d->col, mpad * sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = cudaMallocAsync((void **)&d->wt, mpad * sizeof(uint32_t), st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(d->off, g->off, ((size_t)g->n + 1) * sizeof(uint32_t),
                                 cudaMemcpyHostToDevice, st);
@@ -433,7 +445,12 @@ gga_status dev_graph_ensure(gga_graph *g, int device, cudaStream_t st) {
         if (e == cudaSuccess) e = cudaMemsetAsync(d->wt + g->m, 0, (mpad - g->m) * sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
-            cudaFree(d->off); cudaFree(d->col); cudaFree(d->wt);
+            const cudaError_t e0 = e;
+            cudaGetLastError();
+            cudaStreamSynchronize(st);
+            pool_release(d->off); pool_release(d->col); pool_release(d->wt);
+            cudaStreamSynchronize(0);
+            e = e0;
             free(d);
             s = gga_fail(GGA_ERR_CUDA, "graph upload (%u vertices, %u edges): %s", g->n, g->m,
                          cudaGetErrorString(e));
