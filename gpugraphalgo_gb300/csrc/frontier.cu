@@ -1301,10 +1301,11 @@ gga_status frontier_verdict(const FrontierCtl &h) {
  * larger graphs are rejected with GGA_ERR_TOO_LARGE.  All calls share the
  * one array, so calls whose work overlaps on the GPU (different host
  * threads, or different streams without ordering between them) race and
- * corrupt each other's results; serialise them.  The first call on each
- * device looks up the array's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture begins.  Each call is
- * synchronous: it returns once the traversal on `stream` has finished.  The
+ * corrupt each other's results; serialise them.  Each call is synchronous
+ * (it waits for the traversal on `stream` and reads its status back), so it
+ * must not be made while any stream of the device is being captured into a
+ * CUDA graph; the first call on a device also looks up the array's device
+ * address (cudaGetSymbolAddress).  The
  * caller's CSR is not validated on the host (it is device memory): a column
  * id >= n is caught in the kernel, which skips that edge and makes the call
  * return GGA_ERR_FORMAT.

@@ -386,10 +386,10 @@ gga_status gga_write_result_row(const char *path, const gga_result_row *row);
  * are device pointers: d_offsets[n+1] and d_cols[m] a 0-based CSR, d_dist[n]
  * BFS levels (GGA_INFINITY where unreached).  `stream` is a cudaStream_t
  * (NULL = default stream) on the current device.  All calls share the one
- * array: calls that overlap on the GPU race, so serialise them.  The first
- * call on a device looks up the array's address; make it before any stream
- * capture begins.  The call is synchronous: it returns after the traversal on
- * `stream` has finished.  A column id >= n in the caller's CSR returns
+ * array: calls that overlap on the GPU race, so serialise them.  The call is
+ * synchronous: it returns after the traversal on `stream` has finished, so it
+ * must not be made while a stream of the device is being captured into a
+ * CUDA graph.  A column id >= n in the caller's CSR returns
  * GGA_ERR_FORMAT (the kernel checks every edge target before using it). */
 gga_status gga_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_cols, uint32_t n, uint32_t m,
                            uint32_t src, uint32_t *d_dist, void *stream);
