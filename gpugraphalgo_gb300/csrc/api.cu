@@ -86,6 +86,7 @@ void gga_ctx_destroy(gga_ctx *c) {
     if (m.copy) cudaStreamDestroy(m.copy);
     frontier_scratch_free(&c->fs);
     if (c->stage) cudaFreeHost(c->stage);
+    if (c->dmr_state) cudaFreeHost(c->dmr_state);
     cudaFree(c->dflag);
     cudaFreeHost(c->hflag);
     cudaFree(c->heavy);

@@ -47,8 +47,9 @@ struct gga_ctx {
     std::vector<uint32_t> trace_rounds; /* 5 words per round of the last traced solve */
     std::vector<uint32_t> trace_cta;    /* busy kilocycles per CTA */
     std::string tune_report;            /* JSON of the last gga_autotune's trials */
-    void *stage = nullptr;              /* pinned staging for large device-to-host results (mesh refinement) */
+    void *stage = nullptr;              /* pinned staging for large host<->device copies (mesh refinement) */
     size_t stage_bytes = 0;
+    void *dmr_state = nullptr;          /* pinned host copy of the mesh refinement's round state */
     std::mutex mu;
 };
 

@@ -990,41 +990,86 @@ struct DmrBufs {
     uint4 *p_fan = nullptr;
     unsigned long long *owner = nullptr, *ring = nullptr;
     DmrState *st = nullptr;
-    DmrState *hst = nullptr; /* pinned */
+    DmrState *hst = nullptr; /* pinned, owned by the context */
     void free_all(cudaStream_t s) {
         void *p[] = {x, y, pq, p_px, p_py, tri, nbr, bad, work, p_mode, p_cav, p_win, bsum, lock, wlist, wtri, p_fan, owner,
                      ring, st};
         for (void *q : p)
             if (q) cudaFreeAsync(q, s);
-        if (hst) cudaFreeHost(hst);
         cudaStreamSynchronize(s);
     }
 };
 
-/* Device-to-host copy of a large result into pageable memory: chunks go to
- * two pinned buffers kept in the context (pinned once, reused), and while the
- * next chunk's DMA runs, host threads copy the finished one to its place
- * (and take the destination's first-touch page faults in parallel).  The
- * driver's own pageable path copies with one host thread. */
+/* Large copies between pageable host memory and the device go through two
+ * pinned buffers kept in the context (pinned once, reused): host threads copy
+ * one chunk while the DMA of the other runs (and take a fresh destination's
+ * first-touch page faults in parallel).  The driver's own pageable path
+ * ran at 150 GB/s in a fresh process but at about 10 GB/s late in a long one
+ * that had page-locked gigabytes, which this path does not depend on. */
 constexpr size_t STAGE_CHUNK = 32u << 20;
 
+gga_status stage_ensure(gga_ctx *c) {
+    if (c->stage_bytes >= 2 * STAGE_CHUNK) return GGA_OK;
+    if (c->stage) cudaFreeHost(c->stage);
+    c->stage = nullptr;
+    c->stage_bytes = 0;
+    GGA_CK(cudaMallocHost(&c->stage, 2 * STAGE_CHUNK));
+    c->stage_bytes = 2 * STAGE_CHUNK;
+    return GGA_OK;
+}
+
+unsigned stage_threads() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    return std::max(1u, std::min(16u, hw ? hw / 2 : 4u));
+}
+
+void par_memcpy(char *to, const char *from, size_t len, unsigned nt) {
+    const size_t per = (len + nt - 1) / nt;
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt && t * per < len; ++t)
+        th.emplace_back([=] { memcpy(to + t * per, from + t * per, std::min(per, len - t * per)); });
+    memcpy(to, from, std::min(per, len));
+    for (auto &x : th) x.join();
+}
+
+/* Host-to-device: chunk i is copied into buffer i & 1 once that buffer's
+ * previous DMA has finished, then sent.  The last DMAs may still run when
+ * this returns; later work on `s` is ordered after them, and the next use of
+ * a buffer waits for its event. */
+gga_status copy_to_device(gga_ctx *c, cudaStream_t s, void *dst, const void *src, size_t bytes) {
+    if (bytes < (8u << 20)) { /* small: the plain path */
+        GGA_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+        return GGA_OK;
+    }
+    gga_status r = stage_ensure(c);
+    if (r) return r;
+    cudaEvent_t done[2] = {c->ev[2], c->ev[3]};
+    const size_t nchunk = (bytes + STAGE_CHUNK - 1) / STAGE_CHUNK;
+    const unsigned nt = stage_threads();
+    for (size_t i = 0; i < nchunk; ++i) {
+        const size_t off = i * STAGE_CHUNK, len = std::min(STAGE_CHUNK, bytes - off);
+        char *buf = (char *)c->stage + (i & 1) * STAGE_CHUNK;
+        GGA_CK(cudaEventSynchronize(done[i & 1])); /* the buffer's previous DMA (this call or an earlier one) */
+        par_memcpy(buf, (const char *)src + off, len, nt);
+        GGA_CK(cudaMemcpyAsync((char *)dst + off, buf, len, cudaMemcpyHostToDevice, s));
+        GGA_CK(cudaEventRecord(done[i & 1], s));
+    }
+    return GGA_OK;
+}
+
+/* Device-to-host: the DMA of chunk i + 1 runs while host threads copy chunk
+ * i out of its buffer. */
 gga_status copy_to_host(gga_ctx *c, cudaStream_t s, void *dst, const void *src, size_t bytes) {
     if (bytes < (8u << 20)) { /* small: the plain path */
         GGA_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
         GGA_CK(cudaStreamSynchronize(s));
         return GGA_OK;
     }
-    if (c->stage_bytes < 2 * STAGE_CHUNK) {
-        if (c->stage) cudaFreeHost(c->stage);
-        c->stage = nullptr;
-        c->stage_bytes = 0;
-        GGA_CK(cudaMallocHost(&c->stage, 2 * STAGE_CHUNK));
-        c->stage_bytes = 2 * STAGE_CHUNK;
-    }
+    gga_status r = stage_ensure(c);
+    if (r) return r;
     cudaEvent_t done[2] = {c->ev[2], c->ev[3]};
     const size_t nchunk = (bytes + STAGE_CHUNK - 1) / STAGE_CHUNK;
-    const unsigned hw = std::thread::hardware_concurrency();
-    const unsigned nt = std::max(1u, std::min(16u, hw ? hw / 2 : 4u));
+    const unsigned nt = stage_threads();
     auto issue = [&](size_t i) -> cudaError_t {
         const size_t off = i * STAGE_CHUNK, len = std::min(STAGE_CHUNK, bytes - off);
         cudaError_t e = cudaMemcpyAsync((char *)c->stage + (i & 1) * STAGE_CHUNK, (const char *)src + off, len,
@@ -1036,14 +1081,7 @@ gga_status copy_to_host(gga_ctx *c, cudaStream_t s, void *dst, const void *src, 
         GGA_CK(cudaEventSynchronize(done[i & 1]));
         if (i + 1 < nchunk) GGA_CK(issue(i + 1)); /* buffer (i+1)&1 was drained in iteration i-1 */
         const size_t off = i * STAGE_CHUNK, len = std::min(STAGE_CHUNK, bytes - off);
-        const char *from = (const char *)c->stage + (i & 1) * STAGE_CHUNK;
-        char *to = (char *)dst + off;
-        const size_t per = (len + nt - 1) / nt;
-        std::vector<std::thread> th;
-        for (unsigned t = 1; t < nt && t * per < len; ++t)
-            th.emplace_back([=] { memcpy(to + t * per, from + t * per, std::min(per, len - t * per)); });
-        memcpy(to, from, std::min(per, len));
-        for (auto &x : th) x.join();
+        par_memcpy((char *)dst + off, (const char *)c->stage + (i & 1) * STAGE_CHUNK, len, nt);
     }
     return GGA_OK;
 }
@@ -1069,7 +1107,8 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
         (r = dalloc(&b.p_fan, (size_t)FAN_MAX * B, s)) || (r = dalloc(&b.p_win, B, s)) ||
         (r = dalloc(&b.bsum, 3 * (size_t)G, s)) || (r = dalloc(&b.st, 1, s)))
         return r;
-    GGA_CK(cudaMallocHost((void **)&b.hst, sizeof(DmrState)));
+    if (!c->dmr_state) GGA_CK(cudaMallocHost(&c->dmr_state, sizeof(DmrState)));
+    b.hst = (DmrState *)c->dmr_state;
     memset(b.hst, 0, sizeof(DmrState));
     b.hst->npts = m->npts;
     b.hst->ntri = m->ntri;
@@ -1085,10 +1124,11 @@ gga_status refine_run(gga_ctx *c, gga_mesh *m, double cos_bound, uint32_t tcap, 
     GGA_CK(cudaStreamSynchronize(s));
     out->alloc_ms = gga_now_ms() - tp;
     tp = gga_now_ms();
-    GGA_CK(cudaMemcpyAsync(b.x, m->x, (size_t)m->npts * sizeof(double), cudaMemcpyHostToDevice, s));
-    GGA_CK(cudaMemcpyAsync(b.y, m->y, (size_t)m->npts * sizeof(double), cudaMemcpyHostToDevice, s));
-    GGA_CK(cudaMemcpyAsync(b.tri, m->tri, (size_t)m->ntri * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    GGA_CK(cudaMemcpyAsync(b.nbr, m->nbr, (size_t)m->ntri * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    if ((r = copy_to_device(c, s, b.x, m->x, (size_t)m->npts * sizeof(double))) ||
+        (r = copy_to_device(c, s, b.y, m->y, (size_t)m->npts * sizeof(double))) ||
+        (r = copy_to_device(c, s, b.tri, m->tri, (size_t)m->ntri * 3 * sizeof(uint32_t))) ||
+        (r = copy_to_device(c, s, b.nbr, m->nbr, (size_t)m->ntri * 3 * sizeof(uint32_t))))
+        return r;
 
     DmrArgs a;
     a.x = b.x;
