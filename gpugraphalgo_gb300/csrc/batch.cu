@@ -409,7 +409,11 @@ __global__ void __launch_bounds__(MQ_BS, 4) k_mq(MqArgs a) {
                     bool push = false;
                     if (Q.algo == GGA_SSSP) {
                         const uint32_t alt = t_a[lo] + __ldg(Q.wt + ei);
-                        if (alt < __ldcg(dist + v) && alt < atomicMin(dist + v, alt)) {
+                        /* an offer that beats the probe: fire-and-forget min, and v
+                         * is queued by its stamp without waiting for the old value
+                         * (its expansion reads the distance then) */
+                        if (alt < __ldcg(dist + v)) {
+                            red_min_u32(dist + v, alt);
                             const uint32_t thr = a.nearfar ? C.thr[q] : NONE;
                             if (alt < thr) {
                                 push = atomicExch(aux + v, round + 1) != round + 1;

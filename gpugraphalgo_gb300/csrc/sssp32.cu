@@ -248,10 +248,18 @@ __global__ void __launch_bounds__(SU_BS, 4) k_sssp32(SuArgs a) {
                     }
 #pragma unroll
                     for (uint32_t q = 0; q < SU_EB; ++q) {
+                        /* an offer that beats the probed distance goes out as a
+                         * fire-and-forget red.min and marks v for the next round
+                         * without waiting for the old value: if a concurrent offer
+                         * landed lower, v's expansion next round reads that value,
+                         * so the mark costs at most a redundant relaxation */
                         bool imp = false;
                         if ((m[q] >> lane) & 1u) {
                             const uint32_t alt = du[q] + w[q];
-                            if (alt < dv[q]) imp = alt < atomicMin(a.D + (size_t)v[q] * 32 + lane, alt);
+                            if (alt < dv[q]) {
+                                red_min_u32(a.D + (size_t)v[q] * 32 + lane, alt);
+                                imp = true;
+                            }
                         }
                         const uint32_t im = __ballot_sync(FULL, imp);
                         if (im && lane == 0 && atomicOr(Mn + v[q], im) == 0) {
