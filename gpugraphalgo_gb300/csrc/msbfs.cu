@@ -110,8 +110,21 @@ __device__ __forceinline__ void ms_checkpoint(const MsArgs &a, MsCtrl &C, uint32
  * ORs its vertices' neighbours' seen masks, 4 per vertex per step, until the
  * vertex has every source; vertices that gained bits get them in nxt (this
  * lane is their only writer this level) and join the next candidate list
- * through one warp-aggregated atomicAdd.  Trip counts are warp-uniform; the
- * per-lane scans reconverge before the ballots. */
+ * through one warp-aggregated atomicAdd.  A vertex with more than MS_HEAVY
+ * neighbours is scanned by the whole warp instead, 32 x NB neighbours a step
+ * with the masks OR-reduced across the warp, so one lane's long row does not
+ * hold its warp, block and the level's grid barrier (on R-MAT 20 the blocks
+ * waited 44% of the kernel at that barrier).  Either scan stops once the
+ * vertex has every source, and then acc & ~seen is the same whichever
+ * neighbours were read.  Trip counts are warp-uniform; the per-lane scans
+ * reconverge before the ballots. */
+constexpr uint32_t MS_HEAVY = 64;
+
+__device__ __forceinline__ unsigned long long warp_or64(unsigned long long x) {
+    for (int d = 16; d > 0; d >>= 1) x |= __shfl_down_sync(FULL, x, d);
+    return __shfl_sync(FULL, x, 0);
+}
+
 __device__ __forceinline__ void ms_bottom_up(const MsArgs &a, uint32_t np, unsigned long long &relaxed) {
     constexpr uint32_t NV = 2, NB = 4;
     const uint32_t lane = threadIdx.x & 31u;
@@ -120,7 +133,7 @@ __device__ __forceinline__ void ms_bottom_up(const MsArgs &a, uint32_t np, unsig
     for (uint64_t w = gw; w < steps; w += nw) {
         uint32_t v[NV], cur[NV], e1[NV];
         unsigned long long sv[NV], acc[NV];
-        bool open[NV];
+        bool open[NV], heavy[NV];
 #pragma unroll
         for (uint32_t k = 0; k < NV; ++k) {
             const uint64_t vk = w * 32 * NV + 32 * k + lane;
@@ -133,12 +146,13 @@ __device__ __forceinline__ void ms_bottom_up(const MsArgs &a, uint32_t np, unsig
                 cur[k] = __ldg(a.off + vk);
                 e1[k] = __ldg(a.off + vk + 1);
             }
+            heavy[k] = open[k] && e1[k] - cur[k] > MS_HEAVY;
         }
         for (;;) {
             bool act[NV], any = false;
 #pragma unroll
             for (uint32_t k = 0; k < NV; ++k) {
-                act[k] = open[k] && cur[k] < e1[k] && (acc[k] | sv[k]) != a.all;
+                act[k] = open[k] && !heavy[k] && cur[k] < e1[k] && (acc[k] | sv[k]) != a.all;
                 any |= act[k];
             }
             if (!any) break;
@@ -155,6 +169,35 @@ __device__ __forceinline__ void ms_bottom_up(const MsArgs &a, uint32_t np, unsig
                 if (act[k]) {
                     relaxed += min(NB, e1[k] - cur[k]);
                     cur[k] += NB;
+                }
+            }
+        }
+        /* the heavy rows, one at a time by the whole warp */
+#pragma unroll
+        for (uint32_t k = 0; k < NV; ++k) {
+            for (unsigned hm = __ballot_sync(FULL, heavy[k]); hm; hm &= hm - 1) {
+                const int owner = __ffs(hm) - 1;
+                const uint32_t hb = __shfl_sync(FULL, cur[k], owner), he = __shfl_sync(FULL, e1[k], owner);
+                const unsigned long long hs = __shfl_sync(FULL, sv[k], owner);
+                unsigned long long hacc = 0;
+                uint32_t hend = hb;
+                for (uint32_t base = hb; base < he; base += 32 * NB) { /* warp-uniform */
+                    uint32_t u[NB];
+#pragma unroll
+                    for (uint32_t q = 0; q < NB; ++q) {
+                        const uint32_t j = base + q * 32 + lane;
+                        u[q] = j < he ? __ldg(a.col + j) : NONE;
+                    }
+#pragma unroll
+                    for (uint32_t q = 0; q < NB; ++q)
+                        if (u[q] != NONE) hacc |= __ldcg(a.seen + u[q]);
+                    hacc = warp_or64(hacc);
+                    hend = min(base + 32 * NB, he);
+                    if ((hacc | hs) == a.all) break;
+                }
+                if (lane == (uint32_t)owner) {
+                    acc[k] = hacc;
+                    relaxed += hend - hb;
                 }
             }
         }
