@@ -262,10 +262,19 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
                 f = __ldcg(a.nxt + v) & ~s0;
                 a.nxt[v] = 0;
                 a.seen[v] = s0 | f;
-                uint32_t *lv = a.dist + (size_t)v * a.ns; /* this vertex's levels: one short span */
-                for (unsigned long long mm = f; mm; mm &= mm - 1) lv[__ffsll((long long)mm) - 1] = L;
                 b = __ldg(a.off + v);
                 d = f ? __ldg(a.off + v + 1) - b : 0u;
+            }
+            /* the new levels, one vertex at a time by the whole warp: lane j
+             * writes sources j and j + 32 of the vertex's span (two coalesced
+             * masked stores), not one lane looping over its vertex's bits */
+            for (unsigned lm = __ballot_sync(FULL, f != 0); lm; lm &= lm - 1) {
+                const int src = __ffs(lm) - 1;
+                const uint32_t vv = __shfl_sync(FULL, v, src);
+                const unsigned long long ff = __shfl_sync(FULL, f, src);
+                uint32_t *lv = a.dist + (size_t)vv * a.ns;
+                if (lane < a.ns && ((ff >> lane) & 1ull)) lv[lane] = L;
+                if (lane + 32 < a.ns && ((ff >> (lane + 32)) & 1ull)) lv[lane + 32] = L;
             }
             const unsigned has = __ballot_sync(FULL, d > 0);
             uint32_t incl = d;
