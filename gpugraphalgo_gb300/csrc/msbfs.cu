@@ -83,6 +83,8 @@ struct MsArgs {
 
 struct MsCtrl {
     uint32_t nn, base, unit, i0, cnt, ncand, nitems, total;
+    unsigned long long xbase;  /* settle: the block's slice of the expansion list */
+    unsigned long long ws64[32];
 };
 
 __device__ __forceinline__ void ms_err(MsCtl *c, uint32_t code) { atomicCAS(&c->err, GGA_DEV_OK, code); }
@@ -251,9 +253,9 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
             break;
         }
         if (blockIdx.x == 0 && tid == 0) ctl->work[p] = 0;
-        /* warp-uniform trip count: every lane of a warp runs each iteration */
-        for (uint64_t base = (uint64_t)blockIdx.x * MB_BS + (tid & ~31u); base < ncand; base += gthreads) {
-            const uint64_t i = base + lane;
+        /* block-uniform trip count: every thread of a block runs each iteration */
+        for (uint64_t base = (uint64_t)blockIdx.x * MB_BS; base < ncand; base += gthreads) {
+            const uint64_t i = base + tid;
             uint32_t v = 0, b = 0, d = 0;
             unsigned long long f = 0;
             if (i < ncand) {
@@ -276,21 +278,16 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
                 if (lane < a.ns && ((ff >> lane) & 1ull)) lv[lane] = L;
                 if (lane + 32 < a.ns && ((ff >> (lane + 32)) & 1ull)) lv[lane + 32] = L;
             }
-            const unsigned has = __ballot_sync(FULL, d > 0);
-            uint32_t incl = d;
-#pragma unroll
-            for (int k = 1; k < 32; k <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL, incl, k);
-                if (lane >= (uint32_t)k) incl += y;
-            }
-            const uint32_t wtot = __shfl_sync(FULL, incl, 31);
-            unsigned long long old = 0;
-            if (lane == 0 && has)
-                old = atomicAdd(&ctl->xctr[p], ((unsigned long long)__popc(has) << 32) | (unsigned long long)wtot);
-            old = __shfl_sync(FULL, old, 0);
+            /* one list allocation per block: a block scan of (entries << 32 | edges)
+             * and one atomicAdd, not one per warp on the same counter */
+            unsigned long long tot;
+            const unsigned long long run = block_exclusive_scan64(d > 0 ? (1ull << 32) | d : 0ull, C.ws64, &tot);
+            if (tid == 0) C.xbase = tot ? atomicAdd(&ctl->xctr[p], tot) : 0ull;
+            __syncthreads(); /* read before the next iteration's scan lets thread 0 write it again */
+            const unsigned long long old = C.xbase;
             if (d > 0) {
-                const uint32_t idx = (uint32_t)(old >> 32) + (uint32_t)__popc(has & lanemask_lt());
-                const uint32_t o = (uint32_t)old + incl - d;
+                const uint32_t idx = (uint32_t)(old >> 32) + (uint32_t)(run >> 32);
+                const uint32_t o = (uint32_t)old + (uint32_t)run;
                 if (idx < a.n) {
                     a.xv[idx] = v;
                     a.xo[idx] = o;
