@@ -248,13 +248,14 @@ __global__ void __launch_bounds__(SU_BS, 4) k_sssp32(SuArgs a) {
                         du[q] = on ? __ldcg(a.D + (size_t)u[q] * 32 + lane) : 0u;
                         dv[q] = on ? __ldcg(a.D + (size_t)v[q] * 32 + lane) : 0u;
                     }
+                    /* an offer that beats the probed distance goes out as a
+                     * fire-and-forget red.min and marks v for the next round
+                     * without waiting for the old value: if a concurrent offer
+                     * landed lower, v's expansion next round reads that value,
+                     * so the mark costs at most a redundant relaxation */
+                    uint32_t imq[SU_EB];
 #pragma unroll
                     for (uint32_t q = 0; q < SU_EB; ++q) {
-                        /* an offer that beats the probed distance goes out as a
-                         * fire-and-forget red.min and marks v for the next round
-                         * without waiting for the old value: if a concurrent offer
-                         * landed lower, v's expansion next round reads that value,
-                         * so the mark costs at most a redundant relaxation */
                         bool imp = false;
                         if ((m[q] >> lane) & 1u) {
                             const uint32_t alt = du[q] + w[q];
@@ -263,18 +264,28 @@ __global__ void __launch_bounds__(SU_BS, 4) k_sssp32(SuArgs a) {
                                 imp = true;
                             }
                         }
-                        const uint32_t im = __ballot_sync(FULL, imp);
-                        if (im && lane == 0 && atomicOr(Mn + v[q], im) == 0) {
-                            const uint32_t b = __ldg(a.off + v[q]), d = __ldg(a.off + v[q] + 1) - b;
-                            if (d) {
-                                const uint32_t slot = atomicAdd(&C.nn, 1u);
-                                if (slot < SU_SCAP) {
-                                    sv[slot] = v[q];
-                                    sb[slot] = b;
-                                    sd[slot] = d;
-                                } else {
-                                    su_err(ctl, GGA_DEV_OVERFLOW);
-                                }
+                        imq[q] = __ballot_sync(FULL, imp);
+                    }
+                    /* lane q ORs edge q's improved lanes into v's next mask, so the
+                     * step's SU_EB atomics are in flight together; the lane whose
+                     * OR found the mask empty stages v */
+                    uint32_t mim = 0, mv = 0;
+#pragma unroll
+                    for (uint32_t q = 0; q < SU_EB; ++q)
+                        if (lane == q) {
+                            mim = imq[q];
+                            mv = v[q];
+                        }
+                    if (mim && atomicOr(Mn + mv, mim) == 0) {
+                        const uint32_t b = __ldg(a.off + mv), d = __ldg(a.off + mv + 1) - b;
+                        if (d) {
+                            const uint32_t slot = atomicAdd(&C.nn, 1u);
+                            if (slot < SU_SCAP) {
+                                sv[slot] = mv;
+                                sb[slot] = b;
+                                sd[slot] = d;
+                            } else {
+                                su_err(ctl, GGA_DEV_OVERFLOW);
                             }
                         }
                     }
