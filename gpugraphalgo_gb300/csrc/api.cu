@@ -48,12 +48,18 @@ gga_status gga_ctx_create(int device, gga_ctx **out) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->dflag, 64 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->hflag, 64 * sizeof(uint32_t));
     if (e == cudaSuccess) {
-        /* keep up to 4 GiB of freed stream-ordered memory in this process's
-         * pool, so the working buffers of back-to-back calls (a refinement's
-         * plan records, scan temporaries) are not unmapped and mapped again */
+        /* keep up to 4 GiB (GGA_POOL_KEEP_GIB) of freed stream-ordered
+         * memory in this process's pool, so the working buffers of
+         * back-to-back calls (a refinement's plan records, a re-uploaded
+         * graph, scan temporaries) are not unmapped and mapped again */
         cudaMemPool_t pool;
         if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
             uint64_t keep = 4ull << 30, cur = 0;
+            const char *env = getenv("GGA_POOL_KEEP_GIB");
+            if (env && *env) {
+                const long gib = strtol(env, nullptr, 10);
+                if (gib >= 0 && gib <= 1024) keep = (uint64_t)gib << 30;
+            }
             cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur);
             if (cur < keep) cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
