@@ -844,23 +844,30 @@ def run_gga(args, dist: Dist):
         # both sides of the batched comparisons use each graph's own defaults,
         # not the parameters tuned for the R-MAT-22 step above
         ctx.reset_params()
+        gc.collect()
+        gc.disable()  # timed sections: no interpreter collection pauses in the measured calls
         try:
             out["batched"] = batch_section(gga, ctx)
         except Exception as e:  # reported, not fatal
             out["batched"] = {"error": repr(e)}
+        gc.collect()
         try:
             out["serving"] = serving_section(gga, ctx, args.serve_seconds, dist.local_rank)
         except Exception as e:
             out["serving"] = {"error": repr(e)}
+        gc.enable()
 
     mesh = None
     if not args.no_mesh and dist.rank == 0:
+        gc.collect()
+        gc.disable()
         try:
             mesh = mesh_section(gga, ctx, args.mesh_points)
             out["mesh_refinement"] = mesh[0]
         except Exception as e:  # reported, not fatal
             out["mesh_refinement"] = {"error": repr(e)}
             mesh = None
+        gc.enable()
 
     parity_ok = True
     if checks:
