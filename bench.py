@@ -80,6 +80,7 @@ def parse_args():
     ap.add_argument("--autotune-trials", type=int, default=1)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-query and serving sections")
     ap.add_argument("--no-grid", action="store_true", help="skip the 4096^2 grid section")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving section (keep the batched one)")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="offered-load duration per Poisson rate")
     ap.add_argument("--no-mesh", action="store_true", help="skip the Delaunay mesh refinement section")
     ap.add_argument("--mesh-points", type=int, default=1000000, help="random points of the refinement workload")
@@ -851,10 +852,11 @@ def run_gga(args, dist: Dist):
         except Exception as e:  # reported, not fatal
             out["batched"] = {"error": repr(e)}
         gc.collect()
-        try:
-            out["serving"] = serving_section(gga, ctx, args.serve_seconds, dist.local_rank)
-        except Exception as e:
-            out["serving"] = {"error": repr(e)}
+        if not args.no_serving:
+            try:
+                out["serving"] = serving_section(gga, ctx, args.serve_seconds, dist.local_rank)
+            except Exception as e:
+                out["serving"] = {"error": repr(e)}
         gc.enable()
 
     mesh = None
