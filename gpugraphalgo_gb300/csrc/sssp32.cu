@@ -5,11 +5,13 @@
  * distances of a vertex are one 128-byte line and a warp reads or updates
  * them in one coalesced access.  A queue entry is a vertex u whose distance
  * improved for some sources in the previous round, with the mask of those
- * sources; a warp takes one edge (u, v, w) at a time and lane s relaxes
- * D[v][s] from D[u][s] + w (atomicMin on uint32, as M_my_drelax does,
- * cudaKernels.h:323-330) when bit s of u's mask is set.  The improved lanes'
- * bits are OR-ed into v's mask for the next round; the warp whose OR found the
- * mask empty enqueues v.  So one read of an edge serves every source whose
+ * sources; for each edge (u, v, w) of a warp step (SU_EB of them in flight)
+ * lane s relaxes D[v][s] from D[u][s] + w when bit s of u's mask is set (a
+ * min on uint32, as M_my_drelax's atomicMin is, cudaKernels.h:323-330, sent
+ * as a fire-and-forget red.min once it beats the probed D[v][s]).  The
+ * improved lanes' bits are OR-ed into v's mask for the next round, one edge's
+ * OR per lane; the lane whose OR found the mask empty enqueues v.  So one
+ * read of an edge serves every source whose
  * frontier holds its tail, where 32 single-source runs read it up to 32
  * times.  Per source this is the improved-vertex frontier (Bellman-Ford
  * order), which converges to the unique shortest distances: every answer
