@@ -8,12 +8,12 @@
  *
  *   settle(L): every candidate vertex v (nxt[v] became non-zero during the
  *     previous expand) takes its new bits f = nxt[v] & ~seen[v], records level
- *     L for each set bit (vertex-major, the vertex's levels in one short
- *     span; one tiled transpose gives the source-major output), folds f into
- *     seen[v] and, if it has out-edges, is appended to the expansion list with
- *     its frontier mask f and an exclusive edge offset (warp-aggregated 64-bit
- *     atomicAdd of (entries << 32 | edges), so entry index and edge offset
- *     grow together).
+ *     L for each set bit (vertex-major, the vertex's levels in one short span,
+ *     written by the whole warp; one tiled transpose gives the source-major
+ *     output), folds f into seen[v] and, if it has out-edges, is appended to
+ *     the expansion list with its frontier mask f and an exclusive edge offset
+ *     (a block scan and one 64-bit atomicAdd of (entries << 32 | edges) per
+ *     block, so entry index and edge offset grow together).
  *   expand(L): the expansion list's edges are cut into fixed units of
  *     MB_UNIT edges; CTAs take units by ticket, load the unit's entries into
  *     shared memory and give one edge to each thread: for the edge (u, v) the
