@@ -523,3 +523,32 @@ def test_convergence_rejects_frontier(ctx):
     with pytest.raises(gga.GGAError) as ex:
         ctx.convergence(g, "bfs", 0, np.zeros(g.n, np.uint32), "frontier")
     assert ex.value.status == gga.ERR_INVALID_ARG
+
+
+def test_release_and_upload_again_reuses_the_pool(ctx):
+    """gga_graph_release_device returns the device arrays (the CSR and the
+    light/heavy order) to the stream-ordered pool and the next upload takes
+    them again; over several cycles, with a mesh refinement using the same
+    pool in between, every traversal still equals the oracle's."""
+    g = gga.Graph.rmat(15, 16, seed=8)
+    off, col, wt = g.csr()
+    og = oracle.OracleGraph.from_csr(off, col, wt)
+    srcs = [int(s) for s in np.nonzero(np.diff(off.astype(np.int64)) > 0)[0][:3]]
+    want = {(a, s): og.shortest(a, s) for a in ("bfs", "sssp") for s in srcs}
+    g.pin(True)
+    for cycle in range(4):
+        g.release_device()
+        g.cudaCopy(ctx)
+        ctx.prepare(g, "bfs")
+        ctx.prepare(g, "sssp")
+        for (a, s), w in want.items():
+            np.testing.assert_array_equal(ctx.solve(g, a, s), w, err_msg=f"cycle {cycle} {a} {s}")
+        out = gga.pinned_empty((len(srcs), g.n))
+        ctx.solve_many(g, "sssp", srcs, out=out)
+        for i, s in enumerate(srcs):
+            np.testing.assert_array_equal(out[i], want[("sssp", s)])
+        if cycle == 1:
+            m = gga.Mesh.random(3000, seed=cycle)
+            ctx.refine(m)
+            assert m.check()["bad_triangles"] == 0
+    g.pin(False)
