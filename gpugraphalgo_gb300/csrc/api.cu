@@ -813,7 +813,8 @@ gga_status gga_autotune(gga_ctx *c, gga_graph *g, uint32_t trials, gga_params *c
         char key[64];
         /* 1. CTA size and SSSP bucket width (edge units, unsplit CSR) */
         const uint32_t base = ctx_profile_delta(g);
-        const uint32_t deltas[] = {base / 4 ? base / 4 : 1, base / 2 ? base / 2 : 1, base * 3 / 4 ? base * 3 / 4 : 1,
+        const uint32_t deltas[] = {base / 4 ? base / 4 : 1,         base * 3 / 8 ? base * 3 / 8 : 1,
+                                   base / 2 ? base / 2 : 1,         base * 3 / 4 ? base * 3 / 4 : 1,
                                    base, base * 3 / 2, base * 2, base * 4, 0};
         double best_s = 1e30;
         for (uint32_t bs : {256u, 512u})

@@ -883,7 +883,7 @@ gga_status gga_multi_solve(gga_ctx *c, uint32_t nq, const gga_query *queries, gg
         r.algo = q.algo;
         r.src = q.src;
         r.delta = q.algo == GGA_SSSP ? ctx_batch_delta(q.graph) : 0;
-        r.tail_at = r.delta && (uint64_t)d->m >= 8ull * d->n ? d->n / 4 : 0; /* as in the single-source engine */
+        r.tail_at = r.delta && (uint64_t)d->m >= 8ull * d->n ? d->n / 4 : 0; /* graphs averaging 8+ edges per vertex */
         mq_state_layout(&r, b->pool + at);
         at += mq_state_words(d->n, q.algo);
         slots[i] = i;

@@ -1207,10 +1207,12 @@ gga_status frontier_run(FrontierScratch *s, const GraphView &view, const uint32_
     /* the tail by default only where vertices average 8+ edges: on R-MAT the
      * vertices left are low-degree and mostly final (SSSP 2.27 -> 1.40 ms at
      * R-MAT 22), but on a 4096^2 grid the label-correcting rounds redo whole
-     * wavefronts (9.2 -> 18.1 ms) */
+     * wavefronts (9.2 -> 18.1 ms); it starts once the far pile is below n / 2
+     * (measured against n / 4 on R-MAT 18-22: as fast or faster at every
+     * bucket width, R-MAT 22 with its best width 1.23 -> 1.19 ms) */
     if (sssp && a.delta && p.sssp_tail != 1) {
         if (p.sssp_tail) a.tail_at = view.n / p.sssp_tail;
-        else if ((uint64_t)view.m >= 8ull * view.n) a.tail_at = view.n / 4u;
+        else if ((uint64_t)view.m >= 8ull * view.n) a.tail_at = view.n / 2u;
     }
     a.bu = !sssp && view.cc == nullptr && view.symmetric && p.bfs_direction == 0;
     if (sssp && lh.light && a.delta) {

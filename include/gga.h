@@ -268,7 +268,7 @@ typedef struct gga_params {
      * entries and the pile smaller than the largest it has been, the
      * threshold goes to infinity and the remaining vertices run as one
      * label-correcting frontier over whole rows (no more buckets).  0 = k of
-     * 4 on graphs averaging 8 or more edges per vertex, never on sparser
+     * 2 on graphs averaging 8 or more edges per vertex, never on sparser
      * ones (grids); 1 = never; k > 1 = that k.  Distances are the same. */
     uint32_t sssp_tail;
     /* Expansion strategy of GGA_VARIANT_AUTO (gga_autotune picks it per graph
