@@ -47,7 +47,7 @@
 namespace {
 
 constexpr uint32_t MB_BS = 256;
-constexpr uint32_t MB_ITERS = 8;
+constexpr uint32_t MB_ITERS = 4; /* 1024-edge units (measured: 2048 0.53 ms, 1024 0.50, 512 0.52 for 64 sources on R-MAT 20) */
 constexpr uint32_t MB_UNIT = MB_BS * MB_ITERS;
 constexpr uint32_t MB_BATCH = 4;
 constexpr uint32_t MB_SCAP = MB_BS * (MB_BATCH + 1);
