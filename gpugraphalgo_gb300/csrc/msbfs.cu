@@ -182,19 +182,19 @@ __device__ __forceinline__ void ms_bottom_up(const MsArgs &a, uint32_t np, unsig
                 const uint32_t hb = __shfl_sync(FULL, cur[k], owner), he = __shfl_sync(FULL, e1[k], owner);
                 const unsigned long long hs = __shfl_sync(FULL, sv[k], owner);
                 unsigned long long hacc = 0;
-                uint32_t hend = hb;
-                for (uint32_t base = hb; base < he; base += 32 * NB) { /* warp-uniform */
+                uint64_t hend = hb;
+                for (uint64_t base = hb; base < he; base += 32 * NB) { /* warp-uniform; 64-bit: no wrap near 2^32 edges */
                     uint32_t u[NB];
 #pragma unroll
                     for (uint32_t q = 0; q < NB; ++q) {
-                        const uint32_t j = base + q * 32 + lane;
+                        const uint64_t j = base + q * 32 + lane;
                         u[q] = j < he ? __ldg(a.col + j) : NONE;
                     }
 #pragma unroll
                     for (uint32_t q = 0; q < NB; ++q)
                         if (u[q] != NONE) hacc |= __ldcg(a.seen + u[q]);
                     hacc = warp_or64(hacc);
-                    hend = min(base + 32 * NB, he);
+                    hend = min(base + 32 * NB, (uint64_t)he);
                     if ((hacc | hs) == a.all) break;
                 }
                 if (lane == (uint32_t)owner) {
