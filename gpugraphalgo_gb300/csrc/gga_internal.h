@@ -16,7 +16,9 @@ extern "C" {
 
 /* Vertex and edge limits: ids, offsets and counts are uint32 on the device. */
 #define GGA_MAX_NODES 0x80000000u
-#define GGA_MAX_EDGES 0xFFFFFFF0u
+/* edges: 8192 short of 2^32, so that a unit's 32-bit edge positions (a unit
+ * start plus up to 4095) cannot wrap */
+#define GGA_MAX_EDGES 0xFFFFE000u
 
 /* Host-side graph.  The CSR is 0-based: vertex u owns edges
  * [off[u], off[u+1]).  The reference keeps the same arrays 1-based with a null

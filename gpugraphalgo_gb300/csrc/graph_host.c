@@ -458,7 +458,7 @@ static gga_status csr_from_pairs(uint32_t n, const uint32_t *a, const uint32_t *
         }
     }
     toff[n] = s;
-    if (s > 0xFFFFFFF0ull) {
+    if (s > GGA_MAX_EDGES) {
         free(cnts); free(toff); free(udeg);
         return gga_fail(GGA_ERR_TOO_LARGE, "%llu directed edges", (unsigned long long)s);
     }
