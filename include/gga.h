@@ -49,7 +49,7 @@ typedef enum gga_status {
     GGA_ERR_NO_DEVICE = 7,   /* no CUDA device / extension unusable */
     GGA_ERR_TIMEOUT = 8,     /* a bounded device-side wait ran out; context stays usable */
     GGA_ERR_ADMISSION = 9,   /* request exceeds the configured device-memory cap */
-    GGA_ERR_TOO_LARGE = 10,  /* graph exceeds the uint32 vertex/edge limits */
+    GGA_ERR_TOO_LARGE = 10,  /* graph exceeds the limits: 2^31 vertices, 2^32 - 8192 edges */
     GGA_ERR_NOT_READY = 11,  /* serving ticket not finished yet */
     GGA_ERR_UNSUPPORTED = 12,
     GGA_ERR_NO_PROGRESS = 13 /* mesh refinement: every remaining insertion failed, or the round cap */
