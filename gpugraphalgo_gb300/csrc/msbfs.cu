@@ -400,19 +400,22 @@ __global__ void __launch_bounds__(MB_BS, 4) k_msbfs(MsArgs a) {
     if (blockIdx.x == 0 && tid == 0) ctl->levels = L;
 }
 
-__global__ void k_ms_fill(uint32_t *p, size_t count, uint32_t value) {
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
-        p[i] = value;
-}
-
-/* Source-major output: out[s * n + v] = lvl[v * ns + s], through a shared
- * tile of 32 vertices x ns sources (coalesced reads and writes). */
-__global__ void k_ms_transpose(const uint32_t *lvl, uint32_t n, uint32_t ns, uint32_t *out) {
+/* Source-major output: out[s * n + v] = lvl[v * ns + s] where source s
+ * reached v (bit s of seen[v]) and MYINFINITY elsewhere, through a shared
+ * tile of 32 vertices x ns sources (coalesced reads and writes).  Settle
+ * writes each reached (vertex, source) level exactly once, so the level array
+ * needs no fill before the launch: the entries of unreached pairs are never
+ * read. */
+__global__ void k_ms_transpose(const uint32_t *lvl, const unsigned long long *seen, uint32_t n, uint32_t ns,
+                               uint32_t *out) {
     __shared__ uint32_t tile[32][65];
     const uint32_t tx = threadIdx.x & 31, ty = threadIdx.x >> 5; /* 32 x 8 threads */
     for (uint64_t v0 = (uint64_t)blockIdx.x * 32; v0 < n; v0 += (uint64_t)gridDim.x * 32) {
         const uint32_t nv = (uint32_t)min((uint64_t)32, n - v0);
-        for (uint32_t k = threadIdx.x; k < nv * ns; k += blockDim.x) tile[k / ns][k % ns] = lvl[v0 * ns + k];
+        for (uint32_t k = threadIdx.x; k < nv * ns; k += blockDim.x) {
+            const uint32_t vv = k / ns, s = k % ns;
+            tile[vv][s] = (seen[v0 + vv] >> s) & 1ull ? lvl[v0 * ns + k] : GGA_INFINITY;
+        }
         __syncthreads();
         for (uint32_t s = ty; s < ns; s += 8)
             if (tx < nv) out[(size_t)s * n + v0 + tx] = tile[tx][s];
@@ -610,7 +613,6 @@ gga_status gga_msbfs(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *sr
     GGA_CK(cudaMemsetAsync(m->seen, 0, (size_t)d->n * 8, c->st));
     GGA_CK(cudaMemsetAsync(m->nxt, 0, (size_t)d->n * 8, c->st));
     GGA_CK(cudaMemcpyAsync(m->srcs, srcs, nsrc * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
-    k_ms_fill<<<ctx_grid(c, words, 256), 256, 0, c->st>>>(levels, words, GGA_INFINITY);
     k_ms_sources<<<1, 64, 0, c->st>>>(a, m->srcs, nsrc);
     GGA_CK(cudaGetLastError());
     GGA_CK(cudaEventRecord(c->ev[0], c->st));
@@ -618,9 +620,10 @@ gga_status gga_msbfs(gga_ctx *c, gga_graph *g, uint32_t nsrc, const uint32_t *sr
     GGA_CK(cudaLaunchCooperativeKernel((const void *)k_msbfs, dim3(a.nblocks), dim3(MB_BS), args, ms_smem(), c->st));
     GGA_CK(cudaEventRecord(c->ev[1], c->st));
     GGA_CK(cudaMemcpyAsync(m->hctl, m->ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, c->st));
-    k_ms_transpose<<<ctx_grid(c, ((uint64_t)d->n + 31) / 32 * 256, 256), 256, 0, c->st>>>(levels, d->n, nsrc, out);
+    k_ms_transpose<<<ctx_grid(c, ((uint64_t)d->n + 31) / 32 * 256, 256), 256, 0, c->st>>>(levels, m->seen, d->n, nsrc,
+                                                                                       out);
     GGA_CK(cudaGetLastError());
-    uint32_t launches = 5;
+    uint32_t launches = 3; /* the sources, the traversal, the transpose */
     if (!dev_out) GGA_CK(cudaMemcpyAsync(dist_out, out, words * 4, cudaMemcpyDeviceToHost, c->st));
     if (stats) {
         unsigned long long *acc = (unsigned long long *)(c->dflag + 32);

@@ -43,7 +43,7 @@ def generate(which):
         body = transform("sssp32.cu", "constexpr uint32_t SU_BS", "/* Source-major output", ["k_sssp32"],
                          [("extern __shared__ uint32_t dyn[];", "uint32_t *dyn")])
     elif which == "msbfs":
-        body = transform("msbfs.cu", "constexpr uint32_t MB_BS", "__global__ void k_ms_fill", ["k_msbfs"],
+        body = transform("msbfs.cu", "constexpr uint32_t MB_BS", "/* Source-major output: out[s * n + v]", ["k_msbfs"],
                          [("extern __shared__ unsigned long long dyn64[];", "unsigned long long *dyn64")])
     elif which == "mq":
         hdr = _read("batch.cuh")
